@@ -1,0 +1,141 @@
+"""Generate the golden fixtures in tests/golden/ by running the reference
+solver itself (oracle/_ref/sdpa_gmp, built from the reference sources by
+oracle/build_ref.sh) on seeded synthetic problems and on the reference's own
+known-answer input (example1.dat-s).
+
+This script runs only where the reference sources exist (it builds the
+binary from them); the GPU-side tests read the JSON it writes and regenerate
+the same ``.dat-s`` text from the package's generators, checking its sha256.
+
+Each fixture records what the reference prints: the per-iteration table
+(mu, thetaP, thetaD, objP, objD, alphaP, alphaD, beta), the final block
+(phase, iteration count, mu, gaps, objectives, feasibility errors) and the
+final primal vector ``xVec`` to 40 significant digits (``%+50.40Fe``).
+
+Usage: python tests/golden/make_golden.py [--only NAME ...] [--ref DIR]
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import importlib
+import json
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+problems = importlib.import_module("sdpa-gmp_gb300.problems")
+
+# name -> (generator, kwargs, precision, max_iteration)
+CASES = {
+    "maxcut20": ("maxcut", dict(n=20, p=0.3, seed=1), 256),
+    "maxcut40": ("maxcut", dict(n=40, p=0.2, seed=2), 256),
+    "maxcut40_p512": ("maxcut", dict(n=40, p=0.2, seed=2), 512),
+    "maxcut40pm": ("maxcut", dict(n=40, p=0.15, seed=3, signed=True), 256),
+    "control20": ("control", dict(m=20, blocks=(10, 6), seed=2), 256),
+    "control30": ("control", dict(m=30, blocks=(24, 12), seed=1), 256),
+    "gpp40": ("gpp", dict(n=40, p=0.1, seed=1), 256),
+    "gpp60": ("gpp", dict(n=60, p=0.08, seed=4), 256),
+    "maxcut100": ("maxcut", dict(n=100, p=0.1, seed=0), 256),
+    "maxcut124pm": ("maxcut", dict(n=124, p=0.1, seed=0, signed=True), 256),
+    "control231": ("control", dict(m=231, blocks=(40, 20), seed=0), 256),
+}
+
+ITER_RE = re.compile(r"^\s*(\d+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s*$")
+FINAL_KEYS = ["mu", "relative gap", "gap", "digits", "objValPrimal", "objValDual",
+              "p.feas.error", "d.feas.error", "relative eps"]
+
+
+def parse_result(text: str) -> dict:
+    lines = text.splitlines()
+    out: dict = {"iterations_table": []}
+    i = 0
+    while i < len(lines) and not lines[i].lstrip().startswith("mu "):
+        i += 1
+    i += 1
+    while i < len(lines):
+        mt = ITER_RE.match(lines[i])
+        if not mt:
+            break
+        out["iterations_table"].append(list(mt.groups()))
+        i += 1
+    for ln in lines:
+        if ln.startswith("phase.value"):
+            out["phase"] = ln.split("=")[1].strip()
+        elif ln.strip().startswith("Iteration ="):
+            out["iteration"] = int(ln.split("=")[1])
+        else:
+            for k in FINAL_KEYS:
+                if ln.strip().startswith(k + " ") or ln.strip().startswith(k + "="):
+                    lhs = ln.split("=")[0].strip()
+                    if lhs == k:
+                        out[k] = ln.split("=")[1].strip()
+    xv = re.search(r"xVec = \n\{(.*?)\}\n", text, re.S)
+    if xv:
+        out["xVec"] = [s.strip() for s in xv.group(1).split(",")]
+    return out
+
+
+def run_case(binary: str, dat_text: str, param_text: str, workdir: str, name: str) -> dict:
+    dat = os.path.join(workdir, name + ".dat-s")
+    par = os.path.join(workdir, name + ".param")
+    res = os.path.join(workdir, name + ".result")
+    with open(dat, "w") as f:
+        f.write(dat_text)
+    with open(par, "w") as f:
+        f.write(param_text)
+    env = dict(os.environ, OMP_NUM_THREADS=str(os.cpu_count() or 1))
+    subprocess.run([binary, "-ds", dat, "-o", res, "-p", par], check=True, env=env,
+                   stdout=subprocess.DEVNULL)
+    with open(res) as f:
+        return parse_result(f.read())
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", nargs="*")
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    binary = os.path.join(ROOT, "oracle", "_ref", "sdpa_gmp")
+    subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh"), args.ref], check=True,
+                   stdout=subprocess.DEVNULL)
+    work = tempfile.mkdtemp(prefix="sdpg_golden_")
+    try:
+        if not args.only or "example1" in args.only:
+            shutil.copy(os.path.join(args.ref, "example1.dat-s"), os.path.join(HERE, "example1.dat-s"))
+            with open(os.path.join(HERE, "example1.dat-s")) as f:
+                dat_text = f.read()
+            with open(os.path.join(args.ref, "param.sdpa")) as f:
+                param_text = f.read()
+            with open(os.path.join(HERE, "example1.param"), "w") as f:
+                f.write(param_text)
+            r = run_case(binary, dat_text, param_text, work, "example1")
+            r.update(name="example1", source="reference example1.dat-s + param.sdpa",
+                     precision=200, sha256=hashlib.sha256(dat_text.encode()).hexdigest())
+            with open(os.path.join(HERE, "example1.json"), "w") as f:
+                json.dump(r, f, indent=1)
+            print("example1", r["phase"], r["iteration"], r["objValPrimal"])
+        for name, (gen, kw, prec) in CASES.items():
+            if args.only and name not in args.only:
+                continue
+            dat_text = getattr(problems, gen)(**kw).text()
+            param_text = problems.param_text(precision=prec)
+            r = run_case(binary, dat_text, param_text, work, name)
+            r.update(name=name, generator=gen, kwargs={k: (list(v) if isinstance(v, tuple) else v)
+                                                         for k, v in kw.items()},
+                     precision=prec, sha256=hashlib.sha256(dat_text.encode()).hexdigest())
+            with open(os.path.join(HERE, name + ".json"), "w") as f:
+                json.dump(r, f, indent=1)
+            print(name, r.get("phase"), r.get("iteration"), r.get("objValPrimal"))
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
+if __name__ == "__main__":
+    main()
