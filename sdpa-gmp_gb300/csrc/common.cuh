@@ -1,0 +1,63 @@
+// Shared host-side plumbing for the CUDA kernels: error codes, a growable
+// device workspace, and launch helpers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <stdexcept>
+#include <string>
+
+#include "ml.cuh"
+#include "sdpg.h"
+
+namespace sdpg {
+
+struct sdpg_error : std::runtime_error {
+    int code;
+    sdpg_error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define SDPG_CUDA(call)                                                                        \
+    do {                                                                                       \
+        cudaError_t _e = (call);                                                               \
+        if (_e != cudaSuccess)                                                                 \
+            throw ::sdpg::sdpg_error(SDPG_ERR_CUDA,                                    \
+                                     std::string(#call) + ": " + cudaGetErrorString(_e));       \
+    } while (0)
+
+#define SDPG_CHECK_LAUNCH() SDPG_CUDA(cudaGetLastError())
+
+// Device scratch that only grows; one per problem handle (or per C-ABI call).
+struct Workspace {
+    char *base = nullptr;
+    size_t cap = 0;
+    size_t used = 0;
+    ~Workspace() {
+        if (base) cudaFree(base);
+    }
+    void reserve(size_t bytes) {
+        if (bytes <= cap) return;
+        if (base) {
+            SDPG_CUDA(cudaDeviceSynchronize());
+            SDPG_CUDA(cudaFree(base));
+        }
+        base = nullptr;
+        cap = 0;
+        SDPG_CUDA(cudaMalloc(&base, bytes));
+        cap = bytes;
+    }
+    // carve `bytes` (256-aligned) out of a reservation of `total` made beforehand
+    void *carve(size_t bytes) {
+        size_t off = (used + 255) & ~(size_t)255;
+        if (off + bytes > cap) throw sdpg_error(SDPG_ERR_TOO_LARGE, "workspace exhausted");
+        used = off + bytes;
+        return base + off;
+    }
+    void reset() { used = 0; }
+};
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
+
+}  // namespace sdpg

@@ -1,0 +1,79 @@
+// Block-floating-point multi-limb GEMM (the GPU replacement of the reference's
+// Rgemm family, mplapack/Rgemm_omp.cpp:41-127 and Rgemm_{NN,NT,TN,TT}_omp.cpp).
+//
+//   C = alpha * op(A) * op(B) + beta * C     (column-major, optionally batched)
+//
+// Method.  Every row i of op(A) gets one exponent EA_i = max_k exponent(a_ik)
+// and every column j of op(B) one exponent EB_j.  Each entry becomes the
+// integer trunc(a_ik * 2^(R - EA_i)), |.| < 2^R, stored as D balanced
+// radix-2^28 digits in [-2^27, 2^27] (int32).  A digit product is then one
+// signed 32x32->64 multiply-add (IMAD.WIDE) into an int64 column accumulator.
+// Columns below D-1 of each digit product are dropped (truncation error below
+// 2^-(28D-6) of max|a_i.| * max|b_.j| per product); every CH k-steps the
+// column accumulators are carry-normalised so they never overflow.  The
+// epilogue turns the exact column sums back into an mlf, scales by alpha and
+// adds beta * C.
+//
+// Accuracy: |error(c_ij)| <= K * 2^-(R-2) * 2^(EA_i + EB_j), i.e. a normwise
+// (row-max x column-max) bound with R = 28D - 2 >= 32N + 22 guard bits; GMP's
+// sequential truncated summation in Rgemm has the same form with 2^-p.
+#pragma once
+#include "common.cuh"
+
+namespace sdpg {
+
+template <int N>
+struct Bfp {
+    static constexpr int D = (32 * N + 24 + 27) / 28;  // digits: N=8 -> 10, N=16 -> 20
+    static constexpr int R = 28 * D - 2;               // integer magnitude bound 2^R
+    static constexpr int C0 = D - 1;                   // lowest kept product column
+    static constexpr int NC = D + 2;                   // kept columns C0 .. 2D
+    static constexpr int CH = (D <= 12) ? 32 : 16;     // k-steps between carry normalisations
+};
+
+// One operand of a GEMM: element (o, k) of op(X) lives at X[b*sb + o*so + k*sk].
+template <int N>
+struct Operand {
+    const mlf<N> *X;
+    long long so, sk, sb;
+};
+
+template <int N>
+struct GemmProblem {
+    int M, Nn, K, batch;
+    Operand<N> A;  // op(A): M x K, outer index i
+    Operand<N> B;  // op(B): K x Nn, outer index j
+    mlf<N> *C;
+    long long ldc, sc;
+    mlf<N> alpha, beta;
+    int lower_only;  // 1: only entries with i >= j are written (SYRK-style update)
+};
+
+// Build operands from BLAS-style (trans, pointer, ld, batch stride) arguments.
+template <int N>
+inline Operand<N> operand_A(char trans, const mlf<N> *A, long long lda, long long sA) {
+    // op(A)[i,k] = A[i + k*lda] ('N') or A[k + i*lda] ('T')
+    if (trans == 'N' || trans == 'n') return Operand<N>{A, 1, lda, sA};
+    return Operand<N>{A, lda, 1, sA};
+}
+template <int N>
+inline Operand<N> operand_B(char trans, const mlf<N> *B, long long ldb, long long sB) {
+    // op(B)[k,j] = B[k + j*ldb] ('N') or B[j + k*ldb] ('T')
+    if (trans == 'N' || trans == 'n') return Operand<N>{B, ldb, 1, sB};
+    return Operand<N>{B, 1, ldb, sB};
+}
+
+// Workspace bytes ml_gemm needs for this problem.
+template <int N>
+size_t gemm_workspace_bytes(const GemmProblem<N> &p);
+
+// Runs the quantisers and the digit GEMM on `stream`; scratch is carved from ws
+// (which must already hold gemm_workspace_bytes(p) beyond ws.used).
+template <int N>
+void ml_gemm(const GemmProblem<N> &p, Workspace &ws, cudaStream_t stream);
+
+// Same, with caller-provided scratch of at least gemm_workspace_bytes(p) bytes.
+template <int N>
+void ml_gemm_scratch(const GemmProblem<N> &p, void *scratch, cudaStream_t stream);
+
+}  // namespace sdpg

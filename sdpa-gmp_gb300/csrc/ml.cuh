@@ -1,0 +1,475 @@
+// Multi-limb binary floating point ("mlf"): the number format that stands in
+// for the reference's GMP mpf_class values on the GPU and in host control code.
+//
+//   value = (-1)^s * M * 2^(e - 32N),   M = sum_k m[k] * 2^(32k)   (m[0] least significant)
+//
+// M is normalised (top bit of m[N-1] set), so |value| lies in [2^(e-1), 2^e).
+// Zero has M == 0 (m[N-1] == 0), e == 0, s == 0.  Results are truncated
+// toward zero like GMP's mpf operations (mpf/mul.c, mpf/add.c truncate);
+// add/sub keep two guard limbs and the product keeps the columns from N-2 up,
+// so each operation is accurate to a few units in the last place.
+//
+// N = 8 gives a 256-bit mantissa, N = 16 a 512-bit one.  GMP at precision P
+// carries ((P+127)/64) 64-bit limbs (gmp-impl.h __GMPF_BITS_TO_PREC), i.e. 257-320
+// bits for P = 200 or 256: the 256-bit format is at most 64 bits shorter.
+//
+// Everything here is __host__ __device__: the same code computes kernels on the
+// GPU and the IPM's scalar control logic (step lengths, centering, gaps) on the host.
+// All limb indices are compile-time after unrolling, so on the GPU the arrays
+// stay in registers; variable shifts use a logarithmic barrel shifter.
+#pragma once
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#if defined(__CUDACC__)
+#define MLHD __host__ __device__ __forceinline__
+#define ML_ALIGN __align__(8)
+#else
+#define MLHD inline
+#define ML_ALIGN alignas(8)
+#endif
+
+#if defined(__CUDA_ARCH__)
+#define ML_UNROLL _Pragma("unroll")
+#else
+#define ML_UNROLL
+#endif
+
+namespace sdpg {
+
+template <int N>
+struct ML_ALIGN mlf {
+    int32_t e;
+    uint32_t s;
+    uint32_t m[N];
+};
+
+MLHD int ml_clz32(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+    return __clz(x);
+#else
+    return x ? __builtin_clz(x) : 32;
+#endif
+}
+
+template <int N>
+MLHD mlf<N> ml_zero() {
+    mlf<N> r;
+    r.e = 0;
+    r.s = 0;
+    ML_UNROLL
+    for (int k = 0; k < N; ++k) r.m[k] = 0;
+    return r;
+}
+
+template <int N>
+MLHD bool ml_is_zero(const mlf<N> &a) { return a.m[N - 1] == 0; }
+
+template <int N>
+MLHD mlf<N> ml_neg(mlf<N> a) {
+    if (!ml_is_zero(a)) a.s ^= 1u;
+    return a;
+}
+
+template <int N>
+MLHD mlf<N> ml_abs(mlf<N> a) {
+    a.s = 0;
+    return a;
+}
+
+// value * 2^k (exact)
+template <int N>
+MLHD mlf<N> ml_ldexp(mlf<N> a, int k) {
+    if (!ml_is_zero(a)) a.e += k;
+    return a;
+}
+
+// --- limb-array helpers (compile-time length L) ---------------------------------
+
+// r = a >> (32*q) for a dynamic limb count q in [0, L]; logarithmic barrel shifter.
+template <int L>
+MLHD void ml_limb_shr(uint32_t (&a)[L], int q) {
+    ML_UNROLL
+    for (int step = 1; step < 2 * L; step <<= 1) {
+        if (step > L) break;
+        const bool take = (q & step) != 0;
+        ML_UNROLL
+        for (int k = 0; k < L; ++k) {
+            const uint32_t v = (k + step < L) ? a[k + step] : 0u;
+            a[k] = take ? v : a[k];
+        }
+    }
+}
+
+// a <<= 32*q (limbs), q in [0, L]
+template <int L>
+MLHD void ml_limb_shl(uint32_t (&a)[L], int q) {
+    ML_UNROLL
+    for (int step = 1; step < 2 * L; step <<= 1) {
+        if (step > L) break;
+        const bool take = (q & step) != 0;
+        ML_UNROLL
+        for (int k = L - 1; k >= 0; --k) {
+            const uint32_t v = (k - step >= 0) ? a[k - step] : 0u;
+            a[k] = take ? v : a[k];
+        }
+    }
+}
+
+// a >>= r bits, 0 <= r < 32
+template <int L>
+MLHD void ml_bit_shr(uint32_t (&a)[L], int r) {
+    if (r == 0) return;
+    ML_UNROLL
+    for (int k = 0; k < L; ++k) {
+        const uint32_t hi = (k + 1 < L) ? a[k + 1] : 0u;
+        a[k] = (a[k] >> r) | (hi << (32 - r));
+    }
+}
+
+// a <<= r bits, 0 <= r < 32
+template <int L>
+MLHD void ml_bit_shl(uint32_t (&a)[L], int r) {
+    if (r == 0) return;
+    ML_UNROLL
+    for (int k = L - 1; k >= 0; --k) {
+        const uint32_t lo = (k >= 1) ? a[k - 1] : 0u;
+        a[k] = (a[k] << r) | (lo >> (32 - r));
+    }
+}
+
+// Number of leading zero bits of the L-limb number a (32*L if zero).
+template <int L>
+MLHD int ml_clz_limbs(const uint32_t (&a)[L]) {
+    int lz = 0;
+    bool found = false;
+    ML_UNROLL
+    for (int k = L - 1; k >= 0; --k) {
+        if (!found) {
+            if (a[k] != 0) {
+                lz += ml_clz32(a[k]);
+                found = true;
+            } else {
+                lz += 32;
+            }
+        }
+    }
+    return lz;
+}
+
+// Normalise an L-limb magnitude (L >= N) into an mlf<N> whose exponent is
+// `e_top` when the top bit of a[L-1] is set.  Truncates the low limbs.
+template <int N, int L>
+MLHD mlf<N> ml_pack(uint32_t (&a)[L], int e_top, uint32_t sign) {
+    const int lz = ml_clz_limbs<L>(a);
+    if (lz >= 32 * L) return ml_zero<N>();
+    ml_limb_shl<L>(a, lz >> 5);
+    ml_bit_shl<L>(a, lz & 31);
+    mlf<N> r;
+    r.e = e_top - lz;
+    r.s = sign;
+    ML_UNROLL
+    for (int k = 0; k < N; ++k) r.m[k] = a[L - N + k];
+    return r;
+}
+
+// Compare magnitudes of mantissas: -1, 0, 1
+template <int N>
+MLHD int ml_cmp_mant(const uint32_t (&a)[N], const uint32_t (&b)[N]) {
+    int r = 0;
+    ML_UNROLL
+    for (int k = N - 1; k >= 0; --k) {
+        if (r == 0) r = (a[k] > b[k]) ? 1 : ((a[k] < b[k]) ? -1 : 0);
+    }
+    return r;
+}
+
+// |a| vs |b|
+template <int N>
+MLHD int ml_cmp_abs(const mlf<N> &a, const mlf<N> &b) {
+    const bool za = ml_is_zero(a), zb = ml_is_zero(b);
+    if (za || zb) return za ? (zb ? 0 : -1) : 1;
+    if (a.e != b.e) return a.e > b.e ? 1 : -1;
+    return ml_cmp_mant<N>(a.m, b.m);
+}
+
+template <int N>
+MLHD int ml_sign(const mlf<N> &a) { return ml_is_zero(a) ? 0 : (a.s ? -1 : 1); }
+
+template <int N>
+MLHD int ml_cmp(const mlf<N> &a, const mlf<N> &b) {
+    const int sa = ml_sign(a), sb = ml_sign(b);
+    if (sa != sb) return sa > sb ? 1 : -1;
+    if (sa == 0) return 0;
+    const int c = ml_cmp_abs(a, b);
+    return sa > 0 ? c : -c;
+}
+
+// --- addition -------------------------------------------------------------------
+
+template <int N>
+MLHD mlf<N> ml_add(const mlf<N> &a, const mlf<N> &b) {
+    if (ml_is_zero(b)) return a;
+    if (ml_is_zero(a)) return b;
+    const bool swap = ml_cmp_abs(b, a) > 0;
+    const mlf<N> &x = swap ? b : a;  // |x| >= |y|
+    const mlf<N> &y = swap ? a : b;
+    const int d = x.e - y.e;
+    constexpr int L = N + 2;
+    if (d >= 32 * L) return x;
+    uint32_t xx[L], yy[L];
+    xx[0] = 0;
+    xx[1] = 0;
+    yy[0] = 0;
+    yy[1] = 0;
+    ML_UNROLL
+    for (int k = 0; k < N; ++k) {
+        xx[k + 2] = x.m[k];
+        yy[k + 2] = y.m[k];
+    }
+    ml_limb_shr<L>(yy, d >> 5);
+    ml_bit_shr<L>(yy, d & 31);
+    if (x.s == y.s) {
+        uint64_t c = 0;
+        ML_UNROLL
+        for (int k = 0; k < L; ++k) {
+            c += (uint64_t)xx[k] + yy[k];
+            xx[k] = (uint32_t)c;
+            c >>= 32;
+        }
+        int e = x.e;
+        if (c) {
+            ml_bit_shr<L>(xx, 1);
+            xx[L - 1] |= 0x80000000u;
+            e += 1;
+        }
+        mlf<N> r;
+        r.e = e;
+        r.s = x.s;
+        ML_UNROLL
+        for (int k = 0; k < N; ++k) r.m[k] = xx[k + 2];
+        return r;
+    }
+    int64_t br = 0;
+    ML_UNROLL
+    for (int k = 0; k < L; ++k) {
+        br += (int64_t)xx[k] - (int64_t)yy[k];
+        xx[k] = (uint32_t)br;
+        br >>= 32;  // arithmetic: 0 or -1
+    }
+    return ml_pack<N, L>(xx, x.e, x.s);
+}
+
+template <int N>
+MLHD mlf<N> ml_sub(const mlf<N> &a, const mlf<N> &b) { return ml_add(a, ml_neg(b)); }
+
+// --- multiplication -------------------------------------------------------------
+
+template <int N>
+MLHD mlf<N> ml_mul(const mlf<N> &a, const mlf<N> &b) {
+    if (ml_is_zero(a) || ml_is_zero(b)) return ml_zero<N>();
+    // Columns N-2 .. 2N-1 of the 2N-limb product (lower columns dropped: truncation).
+    uint32_t r[N + 2];
+    uint64_t acc = 0;
+    uint32_t acc_hi = 0;
+    ML_UNROLL
+    for (int c = N - 2; c <= 2 * N - 2; ++c) {
+        ML_UNROLL
+        for (int p = 0; p < N; ++p) {
+            const int q = c - p;
+            if (q >= 0 && q < N) {
+                const uint64_t t = (uint64_t)a.m[p] * b.m[q];
+                acc += t;
+                acc_hi += (acc < t) ? 1u : 0u;
+            }
+        }
+        r[c - (N - 2)] = (uint32_t)acc;
+        acc = (acc >> 32) | ((uint64_t)acc_hi << 32);
+        acc_hi = 0;
+    }
+    r[N + 1] = (uint32_t)acc;
+    mlf<N> o;
+    o.s = a.s ^ b.s;
+    if (r[N + 1] & 0x80000000u) {
+        o.e = a.e + b.e;
+        ML_UNROLL
+        for (int k = 0; k < N; ++k) o.m[k] = r[k + 2];
+    } else {
+        o.e = a.e + b.e - 1;
+        ML_UNROLL
+        for (int k = 0; k < N; ++k) o.m[k] = (r[k + 2] << 1) | (r[k + 1] >> 31);
+    }
+    return o;
+}
+
+// a*b + c (product rounded, then the sum)
+template <int N>
+MLHD mlf<N> ml_fma(const mlf<N> &a, const mlf<N> &b, const mlf<N> &c) { return ml_add(ml_mul(a, b), c); }
+
+// --- conversions ----------------------------------------------------------------
+
+MLHD uint64_t ml_dbits(double x) {
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t u;
+    memcpy(&u, &x, 8);
+    return u;
+#endif
+}
+
+MLHD double ml_bitsd(uint64_t u) {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)u);
+#else
+    double x;
+    memcpy(&x, &u, 8);
+    return x;
+#endif
+}
+
+// Exact conversion from an IEEE double (finite values).
+template <int N>
+MLHD mlf<N> ml_from_double(double x) {
+    const uint64_t u = ml_dbits(x);
+    const uint32_t sign = (uint32_t)(u >> 63);
+    const int ex = (int)((u >> 52) & 0x7ff);
+    uint64_t frac = u & 0xfffffffffffffull;
+    int e2;  // value = frac * 2^e2 with frac an integer
+    if (ex == 0) {
+        if (frac == 0) return ml_zero<N>();
+        e2 = -1074;
+    } else {
+        frac |= 1ull << 52;
+        e2 = ex - 1075;
+    }
+    // normalise frac to 64 bits with top bit set
+    int lz = 0;
+    while (!(frac & 0x8000000000000000ull)) {
+        frac <<= 1;
+        ++lz;
+    }
+    mlf<N> r = ml_zero<N>();
+    r.s = sign;
+    r.m[N - 1] = (uint32_t)(frac >> 32);
+    r.m[N - 2] = (uint32_t)frac;
+    // value = frac64 * 2^(e2 - lz), frac64 in [2^63, 2^64) -> |value| in [2^(e-1), 2^e) with
+    r.e = e2 - lz + 64;
+    return r;
+}
+
+template <int N>
+MLHD mlf<N> ml_from_int(int64_t v) {
+    if (v == 0) return ml_zero<N>();
+    const uint32_t sign = v < 0 ? 1u : 0u;
+    uint64_t a = v < 0 ? (uint64_t)(-(v + 1)) + 1u : (uint64_t)v;
+    int lz = 0;
+    while (!(a & 0x8000000000000000ull)) {
+        a <<= 1;
+        ++lz;
+    }
+    mlf<N> r = ml_zero<N>();
+    r.s = sign;
+    r.m[N - 1] = (uint32_t)(a >> 32);
+    r.m[N - 2] = (uint32_t)a;
+    r.e = 64 - lz;
+    return r;
+}
+
+// Truncating conversion to double (exponents outside double range give 0 or inf).
+template <int N>
+MLHD double ml_to_double(const mlf<N> &a) {
+    if (ml_is_zero(a)) return 0.0;
+    const uint64_t top = ((uint64_t)a.m[N - 1] << 32) | a.m[N - 2];
+    const double v = ldexp((double)(top >> 11), a.e - 53);
+    return a.s ? -v : v;
+}
+
+// Mantissa as a double in [0.5, 1) (exponent dropped); used to seed Newton iterations.
+template <int N>
+MLHD double ml_mant_double(const mlf<N> &a) {
+    const uint64_t top = ((uint64_t)a.m[N - 1] << 32) | a.m[N - 2];
+    return (double)(top >> 11) * 0x1p-53;
+}
+
+template <int N>
+MLHD mlf<N> ml_one() { return ml_from_int<N>(1); }
+
+// --- division and square root (Newton-Raphson on the mantissa) -------------------
+
+template <int N>
+struct ml_newton_steps {
+    // bits doubled per step from a 50-bit seed until >= 32N + 8
+    static constexpr int value = (32 * N + 8 <= 100) ? 1 : (32 * N + 8 <= 200) ? 2 : (32 * N + 8 <= 400) ? 3
+                                 : (32 * N + 8 <= 800) ? 4 : 5;
+};
+
+// 1/b
+template <int N>
+MLHD mlf<N> ml_recip(const mlf<N> &b) {
+    if (ml_is_zero(b)) return ml_zero<N>();  // caller guards; no IEEE infinities in this format
+    mlf<N> bn = b;  // bn = mantissa in [1/2, 1)
+    bn.e = 0;
+    bn.s = 0;
+    const double md = ml_mant_double(bn);
+    mlf<N> x = ml_from_double<N>(1.0 / md);  // ~ 1/bn in (1, 2]
+    const mlf<N> one = ml_one<N>();
+    ML_UNROLL
+    for (int it = 0; it < ml_newton_steps<N>::value; ++it) {
+        const mlf<N> t = ml_sub(one, ml_mul(bn, x));
+        x = ml_add(x, ml_mul(x, t));
+    }
+    x.e -= b.e;
+    x.s = b.s;
+    return x;
+}
+
+// a/b with one residual correction
+template <int N>
+MLHD mlf<N> ml_div(const mlf<N> &a, const mlf<N> &b) {
+    if (ml_is_zero(a)) return ml_zero<N>();
+    const mlf<N> x = ml_recip(b);
+    mlf<N> q = ml_mul(a, x);
+    const mlf<N> r = ml_sub(a, ml_mul(b, q));
+    q = ml_add(q, ml_mul(r, x));
+    return q;
+}
+
+// 1/sqrt(a), a > 0
+template <int N>
+MLHD mlf<N> ml_rsqrt(const mlf<N> &a) {
+    if (ml_is_zero(a) || a.s) return ml_zero<N>();
+    // a = an * 2^(2k) with an in [1/4, 1)
+    int k = a.e >> 1;  // floor(e/2)
+    mlf<N> an = a;
+    an.e = a.e - 2 * k;  // 0 or 1
+    double ad = ml_mant_double(an) * (an.e == 1 ? 2.0 : 1.0);
+    mlf<N> y = ml_from_double<N>(1.0 / sqrt(ad));
+    const mlf<N> one = ml_one<N>();
+    ML_UNROLL
+    for (int it = 0; it < ml_newton_steps<N>::value; ++it) {
+        // y += y * (1 - an*y^2) / 2
+        const mlf<N> t = ml_sub(one, ml_mul(an, ml_mul(y, y)));
+        y = ml_add(y, ml_ldexp(ml_mul(y, t), -1));
+    }
+    y.e -= k;
+    return y;
+}
+
+template <int N>
+MLHD mlf<N> ml_sqrt(const mlf<N> &a) {
+    if (ml_is_zero(a) || a.s) return ml_zero<N>();
+    const mlf<N> y = ml_rsqrt(a);
+    mlf<N> s = ml_mul(a, y);
+    // s += y * (a - s^2) / 2
+    s = ml_add(s, ml_ldexp(ml_mul(y, ml_sub(a, ml_mul(s, s))), -1));
+    return s;
+}
+
+template <int N>
+MLHD mlf<N> ml_max(const mlf<N> &a, const mlf<N> &b) { return ml_cmp(a, b) >= 0 ? a : b; }
+template <int N>
+MLHD mlf<N> ml_min(const mlf<N> &a, const mlf<N> &b) { return ml_cmp(a, b) <= 0 ? a : b; }
+
+}  // namespace sdpg
