@@ -83,6 +83,103 @@ int sdpg_rgemm_device(int limbs, char transa, char transb, int m, int n, int k, 
                       const void *A, int lda, const void *B, int ldb, const void *beta, void *C, int ldc,
                       void *stream);
 
+
+/* ---- factorisations and eigenvalues (standalone, host buffers) ---------------- */
+
+/* In-place lower Cholesky; *info = 0 or the 1-based column of the first
+ * non-positive pivot -- replaces Rpotrf("Lower") (mplapack/Rpotrf.cpp:32-154) as
+ * called by Lal::choleskyFactorWithAdjust (sdpa_linear.cpp:608-616). */
+int sdpg_rpotrf(int limbs, int n, void *A, int lda, int *info);
+/* Linv (n x n, ld n) = L^{-1} for lower-triangular L -- replaces
+ * Lal::getInvLowTriangularMatrix (sdpa_linear.cpp:439-455, Rtrsm on I). */
+int sdpg_inv_lower(int limbs, int n, const void *L, int ldl, void *Linv);
+/* x := (L L^T)^{-1} x -- replaces Lal::solveSystems (sdpa_linear.cpp:683-695, two Rtrsv). */
+int sdpg_solve_systems(int limbs, int n, const void *L, int ldl, void *x);
+/* Smallest eigenvalue of the symmetric tridiagonal (d[0..k-1], e[0..k-2]) and the
+ * last component of its unit eigenvector (out2[0], out2[1]) -- the values
+ * Lal::getMinEigen reads from Rsteqr (sdpa_linear.cpp:65-112). */
+int sdpg_tridiag_min(int limbs, int k, const void *d, const void *e, void *out2);
+/* Smallest eigenvalue of a dense symmetric n x n (n <= 64, lower triangle read) --
+ * replaces Lal::getMinEigenValue (sdpa_linear.cpp:126-158, Rsyev 'N' 'L'). */
+int sdpg_sym_min_eigen(int limbs, int n, const void *A, void *out);
+
+/* ---- the interior-point solver ------------------------------------------------ */
+
+/* Parameter::{setDefaultParameter,readFile} (sdpa_parts.cpp:136-225); type 0 default,
+ * 1 stable-but-slow, 2 unstable-but-fast (the -pt presets). */
+typedef struct {
+    int maxIteration;
+    double epsilonStar, lambdaStar, omegaStar, lowerBound, upperBound, betaStar, betaBar, gammaStar,
+        epsilonDash;
+    int precision;
+} sdpg_param;
+int sdpg_param_default(sdpg_param *p, int type);
+int sdpg_param_read(sdpg_param *p, const char *path);
+
+/* Problem data in SDPA form (IO::read, sdpa_io.cpp:123-141, 410-663): F_0..F_m and c.
+ * Indices are 1-based as in .dat-s; entry k = 0 is F_0 (the solver's C = -F_0). */
+typedef struct sdpg_problem sdpg_problem;
+sdpg_problem *sdpg_problem_new(int m, int nBlock, const int *blockStruct, int *err);
+sdpg_problem *sdpg_problem_read(const char *path, int dense_format, int *err);
+void sdpg_problem_free(sdpg_problem *p);
+int sdpg_problem_set_c(sdpg_problem *p, int k, const char *text);
+int sdpg_problem_add_entry(sdpg_problem *p, int k, int block, int i, int j, const char *text);
+int sdpg_problem_add_entry_mpf(sdpg_problem *p, int k, int block, int i, int j, const sdpg_mpf_t *v);
+
+/* GPU-resident solver state (the reference's Solutions, Residuals, Newton and
+ * WorkVariables, sdpa_dataset.h:29-177, sdpa_newton.h:33-168).  stream may be NULL. */
+typedef struct sdpg_solver sdpg_solver;
+sdpg_solver *sdpg_solver_create(const sdpg_problem *p, const sdpg_param *param, int device, void *stream,
+                                int *err);
+void sdpg_solver_destroy(sdpg_solver *h);
+int sdpg_solver_limbs(sdpg_solver *h);
+int sdpg_solver_dims(sdpg_solver *h, int *m, int *nblocks, int *block_sizes, int cap);
+/* Solutions::initialize (sdpa_dataset.cpp:35-60) + initial Residuals, mu, theta, SolveInfo, Phase
+ * (sdpa_main.cpp:229-287). */
+int sdpg_solver_initialize(sdpg_solver *h);
+/* The predictor-corrector loop of pinpal (sdpa_main.cpp:294-398); writes the
+ * reference's iteration table and summary to out_path (may be NULL) and stdout
+ * when asked; returns the iteration count. */
+int sdpg_solver_run(sdpg_solver *h, const char *out_path, int print_to_stdout);
+/* Newton::Mehrotra (sdpa_newton.cpp:1375-1414); direction 0 predictor, 1 corrector.
+ * Returns SDPG_ERR_NOT_PD when the Schur Cholesky fails (the reference's FAILURE). */
+int sdpg_newton(sdpg_solver *h, int direction);
+/* StepLength::MehrotraPredictor / MehrotraCorrector (sdpa_parts.cpp:362-523). */
+int sdpg_step_length(sdpg_solver *h, int direction);
+/* Solutions::update + computeInverse (sdpa_dataset.cpp:96-143); SDPG_ERR_NOT_PD when
+ * the step is too short or X / Z lost positive definiteness ("cannot move"). */
+int sdpg_update(sdpg_solver *h);
+/* Residuals::compute (sdpa_dataset.cpp:625-646). */
+int sdpg_residuals(sdpg_solver *h);
+/* Newton::Make_bMat (sdpa_newton.cpp:1251-1272) at the current iterate: m x m Schur matrix. */
+int sdpg_make_schur(sdpg_solver *h, void *out_ml);
+/* Newton::Make_gVec (sdpa_newton.cpp:840-895): right-hand side g (m). */
+int sdpg_make_gvec(sdpg_solver *h, int direction, void *out_ml);
+/* Jal::getMinEigen (sdpa_jordan.cpp:55-88) of L_X^{-1} dX L_X^{-T} (side 0) or the Z side (1). */
+int sdpg_min_eigen(sdpg_solver *h, int side, void *out_ml);
+/* [phase, iteration, objValPrimal, objValDual, mu, relative gap, p.feas.error,
+ *  d.feas.error, alphaP, alphaD, beta, digits] as the reference prints them. */
+int sdpg_solution_info(sdpg_solver *h, double *out12);
+/* 0 objValPrimal, 1 objValDual, 2 mu, 3 relative gap, 4 p.feas.error, 5 d.feas.error as %e text. */
+int sdpg_solution_text(sdpg_solver *h, int which, int digits, char *buf, int cap);
+/* The printed xVec (= -y); form 0 doubles, 1 ml elements. */
+int sdpg_get_xvec(sdpg_solver *h, int form, void *out);
+/* which: 0 X, 1 Z, 2 dX, 3 dZ, 4 Z^-1, 5 L_X^-1, 6 L_Z^-1, 7 C, 8 dual residual (block 0-based). */
+int sdpg_get_block(sdpg_solver *h, int which, int block, int form, void *out);
+/* which: 0 y, 1 dy, 2 b, 3 primal residual p (ml elements, length m). */
+int sdpg_get_vector(sdpg_solver *h, int which, void *out_ml);
+/* Per-phase milliseconds: schur, cholesky, rMat+gVec, dX/dZ, step length, update, residual, total
+ * (the reference's ComputeTime, sdpa_parts.cpp:26-123). */
+int sdpg_solver_timers(sdpg_solver *h, double *out8);
+/* Iteration table rows (9 doubles each: it, mu, thetaP, thetaD, objP, objD, alphaP, alphaD, beta). */
+int sdpg_solver_history(sdpg_solver *h, double *out, int cap);
+long long sdpg_solver_gemm_macs(sdpg_solver *h);
+int sdpg_solver_reset_counters(sdpg_solver *h);
+/* Read data + param, solve, write the result file: `sdpa_gmp -ds data -o out -p param`
+ * (main / pinpal, sdpa_main.cpp:43-461, 501-677).  Returns iterations; info12 as above. */
+int sdpg_solve_file(const char *data_path, const char *param_path, const char *out_path, int device,
+                    double *info12);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,6 +29,28 @@ class SdpgError(RuntimeError):
 _lib = None
 
 
+class Param(ctypes.Structure):
+    """Interior-point parameters (the reference's Parameter, sdpa_parts.cpp:136-225)."""
+    _fields_ = [("maxIteration", ctypes.c_int), ("epsilonStar", ctypes.c_double),
+                ("lambdaStar", ctypes.c_double), ("omegaStar", ctypes.c_double),
+                ("lowerBound", ctypes.c_double), ("upperBound", ctypes.c_double),
+                ("betaStar", ctypes.c_double), ("betaBar", ctypes.c_double),
+                ("gammaStar", ctypes.c_double), ("epsilonDash", ctypes.c_double),
+                ("precision", ctypes.c_int)]
+
+    @classmethod
+    def default(cls, preset: int = 0) -> "Param":
+        p = cls()
+        check(lib().sdpg_param_default(ctypes.byref(p), preset))
+        return p
+
+    @classmethod
+    def read(cls, path: str) -> "Param":
+        p = cls.default()
+        check(lib().sdpg_param_read(ctypes.byref(p), path.encode()))
+        return p
+
+
 def _setup(lib: ctypes.CDLL) -> ctypes.CDLL:
     c = ctypes
     vp, i, ll, ch = c.c_void_p, c.c_int, c.c_longlong, c.c_char
@@ -46,6 +68,42 @@ def _setup(lib: ctypes.CDLL) -> ctypes.CDLL:
         "sdpg_ml_host_op": (i, [i, i, ll, vp, vp, vp]),
         "sdpg_rgemm": (i, [i, ch, ch, i, i, i, vp, vp, i, vp, i, vp, vp, i]),
         "sdpg_rgemm_device": (i, [i, ch, ch, i, i, i, vp, vp, i, vp, i, vp, vp, i, vp]),
+        "sdpg_rpotrf": (i, [i, i, vp, i, c.POINTER(i)]),
+        "sdpg_inv_lower": (i, [i, i, vp, i, vp]),
+        "sdpg_solve_systems": (i, [i, i, vp, i, vp]),
+        "sdpg_tridiag_min": (i, [i, i, vp, vp, vp]),
+        "sdpg_sym_min_eigen": (i, [i, i, vp, vp]),
+        "sdpg_param_default": (i, [c.POINTER(Param), i]),
+        "sdpg_param_read": (i, [c.POINTER(Param), c.c_char_p]),
+        "sdpg_problem_new": (vp, [i, i, c.POINTER(i), c.POINTER(i)]),
+        "sdpg_problem_read": (vp, [c.c_char_p, i, c.POINTER(i)]),
+        "sdpg_problem_free": (None, [vp]),
+        "sdpg_problem_set_c": (i, [vp, i, c.c_char_p]),
+        "sdpg_problem_add_entry": (i, [vp, i, i, i, i, c.c_char_p]),
+        "sdpg_problem_add_entry_mpf": (i, [vp, i, i, i, i, vp]),
+        "sdpg_solver_create": (vp, [vp, c.POINTER(Param), i, vp, c.POINTER(i)]),
+        "sdpg_solver_destroy": (None, [vp]),
+        "sdpg_solver_limbs": (i, [vp]),
+        "sdpg_solver_dims": (i, [vp, c.POINTER(i), c.POINTER(i), c.POINTER(i), i]),
+        "sdpg_solver_initialize": (i, [vp]),
+        "sdpg_solver_run": (i, [vp, c.c_char_p, i]),
+        "sdpg_newton": (i, [vp, i]),
+        "sdpg_step_length": (i, [vp, i]),
+        "sdpg_update": (i, [vp]),
+        "sdpg_residuals": (i, [vp]),
+        "sdpg_make_schur": (i, [vp, vp]),
+        "sdpg_make_gvec": (i, [vp, i, vp]),
+        "sdpg_min_eigen": (i, [vp, i, vp]),
+        "sdpg_solution_info": (i, [vp, c.POINTER(c.c_double)]),
+        "sdpg_solution_text": (i, [vp, i, i, c.c_char_p, i]),
+        "sdpg_get_xvec": (i, [vp, i, vp]),
+        "sdpg_get_block": (i, [vp, i, i, i, vp]),
+        "sdpg_get_vector": (i, [vp, i, vp]),
+        "sdpg_solver_timers": (i, [vp, c.POINTER(c.c_double)]),
+        "sdpg_solver_history": (i, [vp, c.POINTER(c.c_double), i]),
+        "sdpg_solver_gemm_macs": (c.c_longlong, [vp]),
+        "sdpg_solver_reset_counters": (i, [vp]),
+        "sdpg_solve_file": (i, [c.c_char_p, c.c_char_p, c.c_char_p, i, c.POINTER(c.c_double)]),
     }
     for name, (res, args) in sig.items():
         if hasattr(lib, name):
@@ -135,3 +193,177 @@ def rgemm(transa: str, transb: str, m: int, n: int, k: int, alpha: np.ndarray, A
     check(lib().sdpg_rgemm(limbs, transa.encode(), transb.encode(), m, n, k, alpha.ctypes.data,
                            A.ctypes.data, lda, B.ctypes.data, ldb, beta.ctypes.data, C.ctypes.data, ldc))
     return C
+
+
+PHASES = ["noINFO", "pFEAS", "dFEAS", "pdFEAS", "pdINF", "pFEAS_dINF", "pINF_dFEAS", "pdOPT", "pUNBD",
+          "dUNBD"]
+INFO_KEYS = ["phase", "iteration", "objValPrimal", "objValDual", "mu", "relative gap", "p.feas.error",
+             "d.feas.error", "alphaP", "alphaD", "beta", "digits"]
+
+
+class Problem:
+    """SDPA problem data (F_0..F_m, c), 1-based indices as in .dat-s files."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    @classmethod
+    def read(cls, path: str, dense: bool = False) -> "Problem":
+        err = ctypes.c_int(0)
+        h = lib().sdpg_problem_read(path.encode(), 1 if dense else 0, ctypes.byref(err))
+        if not h:
+            check(err.value)
+        return cls(h)
+
+    @classmethod
+    def new(cls, m: int, block_struct) -> "Problem":
+        bs = (ctypes.c_int * len(block_struct))(*block_struct)
+        err = ctypes.c_int(0)
+        h = lib().sdpg_problem_new(m, len(block_struct), bs, ctypes.byref(err))
+        if not h:
+            check(err.value)
+        return cls(h)
+
+    def set_c(self, k: int, value) -> None:
+        check(lib().sdpg_problem_set_c(self.h, k, str(value).encode()))
+
+    def add_entry(self, k: int, block: int, i: int, j: int, value) -> None:
+        check(lib().sdpg_problem_add_entry(self.h, k, block, i, j, str(value).encode()))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.sdpg_problem_free(self.h)
+            self.h = None
+
+
+class Solver:
+    """GPU-resident interior-point solver (one problem, one stream)."""
+
+    def __init__(self, problem: Problem, param: Param | None = None, device: int = 0, stream: int = 0):
+        param = param or Param.default()
+        err = ctypes.c_int(0)
+        self.h = lib().sdpg_solver_create(problem.h, ctypes.byref(param), device, stream or None,
+                                          ctypes.byref(err))
+        if not self.h:
+            check(err.value)
+        self.limbs = check(lib().sdpg_solver_limbs(self.h))
+        m, nb = ctypes.c_int(), ctypes.c_int()
+        sizes = (ctypes.c_int * 4096)()
+        check(lib().sdpg_solver_dims(self.h, ctypes.byref(m), ctypes.byref(nb), sizes, 4096))
+        self.m = m.value
+        self.block_sizes = [sizes[i] for i in range(nb.value)]
+
+    def close(self) -> None:
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.sdpg_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def initialize(self) -> None:
+        check(lib().sdpg_solver_initialize(self.h))
+
+    def run(self, out_path: str | None = None, verbose: bool = False) -> int:
+        return check(lib().sdpg_solver_run(self.h, out_path.encode() if out_path else None, 1 if verbose else 0))
+
+    def newton(self, direction: int) -> bool:
+        rc = lib().sdpg_newton(self.h, direction)
+        if rc == -3:
+            return False
+        check(rc)
+        return True
+
+    def step_length(self, direction: int) -> None:
+        check(lib().sdpg_step_length(self.h, direction))
+
+    def update(self) -> bool:
+        rc = lib().sdpg_update(self.h)
+        if rc == -3:
+            return False
+        check(rc)
+        return True
+
+    def residuals(self) -> None:
+        check(lib().sdpg_residuals(self.h))
+
+    def info(self) -> dict:
+        out = (ctypes.c_double * 12)()
+        check(lib().sdpg_solution_info(self.h, out))
+        d = dict(zip(INFO_KEYS, list(out)))
+        d["phase"] = PHASES[int(d["phase"])]
+        d["iteration"] = int(d["iteration"])
+        return d
+
+    def text(self, which: int, digits: int = 40) -> str:
+        buf = ctypes.create_string_buffer(digits + 32)
+        check(lib().sdpg_solution_text(self.h, which, digits, buf, len(buf)))
+        return buf.value.decode()
+
+    def xvec(self, ml: bool = False) -> np.ndarray:
+        if ml:
+            out = ml_empty(self.m, self.limbs)
+            check(lib().sdpg_get_xvec(self.h, 1, out.ctypes.data))
+            return out
+        out = np.zeros(self.m)
+        check(lib().sdpg_get_xvec(self.h, 0, out.ctypes.data))
+        return out
+
+    def block(self, which: int, l: int, ml: bool = False) -> np.ndarray:
+        n = self.block_sizes[l]
+        if ml:
+            out = ml_empty(n * n, self.limbs)
+            check(lib().sdpg_get_block(self.h, which, l, 1, out.ctypes.data))
+            return out
+        out = np.zeros(n * n)
+        check(lib().sdpg_get_block(self.h, which, l, 0, out.ctypes.data))
+        return out.reshape(n, n, order="F")
+
+    def vector(self, which: int) -> np.ndarray:
+        out = ml_empty(self.m, self.limbs)
+        check(lib().sdpg_get_vector(self.h, which, out.ctypes.data))
+        return out
+
+    def schur(self) -> np.ndarray:
+        out = ml_empty(self.m * self.m, self.limbs)
+        check(lib().sdpg_make_schur(self.h, out.ctypes.data))
+        return out
+
+    def gvec(self, direction: int = 0) -> np.ndarray:
+        out = ml_empty(self.m, self.limbs)
+        check(lib().sdpg_make_gvec(self.h, direction, out.ctypes.data))
+        return out
+
+    def min_eigen(self, side: int) -> np.ndarray:
+        out = ml_empty(1, self.limbs)
+        check(lib().sdpg_min_eigen(self.h, side, out.ctypes.data))
+        return out
+
+    def timers(self) -> dict:
+        out = (ctypes.c_double * 8)()
+        check(lib().sdpg_solver_timers(self.h, out))
+        return dict(zip(["schur", "cholesky", "rmat_gvec", "dxdz", "steplen", "update", "residual", "total"],
+                        list(out)))
+
+    def history(self) -> np.ndarray:
+        out = (ctypes.c_double * (9 * 4096))()
+        n = check(lib().sdpg_solver_history(self.h, out, 4096))
+        return np.array(list(out)[: 9 * n]).reshape(n, 9)
+
+    def gemm_macs(self) -> int:
+        return int(lib().sdpg_solver_gemm_macs(self.h))
+
+    def reset_counters(self) -> None:
+        check(lib().sdpg_solver_reset_counters(self.h))
+
+
+def solve_file(data_path: str, param_path: str | None = None, out_path: str | None = None,
+               device: int = 0) -> dict:
+    """``sdpa_gmp -ds data -o out -p param`` on the GPU; returns the final info."""
+    out = (ctypes.c_double * 12)()
+    check(lib().sdpg_solve_file(data_path.encode(), param_path.encode() if param_path else None,
+                                out_path.encode() if out_path else None, device, out))
+    d = dict(zip(INFO_KEYS, list(out)))
+    d["phase"] = PHASES[int(d["phase"])]
+    d["iteration"] = int(d["iteration"])
+    return d

@@ -7,6 +7,7 @@
 
 #include "capi_util.cuh"
 #include "gemm.cuh"
+#include "kernels.cuh"
 #include "ml_host.h"
 #include "sdpg.h"
 
@@ -191,6 +192,134 @@ int sdpg_rgemm(int limbs, char transa, char transb, int m, int n, int k, const v
         if (rc != SDPG_OK) return rc;
         SDPG_CUDA(cudaMemcpy(C, dC.p, nc * eb, cudaMemcpyDeviceToHost));
         return (int)SDPG_OK;
+    });
+}
+
+}  // extern "C"
+
+namespace {
+
+template <class F>
+int with_device_copy(int limbs, size_t count, const void *host, bool copy_back, void *host_out, F &&f) {
+    const int eb = 8 + 4 * limbs;
+    DeviceBuffer d(count * eb > 0 ? count * eb : 16);
+    if (count) SDPG_CUDA(cudaMemcpy(d.p, host, count * eb, cudaMemcpyHostToDevice));
+    int rc = f(d.p);
+    SDPG_CUDA(cudaDeviceSynchronize());
+    if (copy_back && count) SDPG_CUDA(cudaMemcpy(host_out, d.p, count * eb, cudaMemcpyDeviceToHost));
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sdpg_rpotrf(int limbs, int n, void *A, int lda, int *info) {
+    return sdpg_guard([&] {
+        if (n < 0 || lda < (n > 1 ? n : 1) || !A || !info) throw sdpg_error(SDPG_ERR_ARG, "bad arguments");
+        if (n == 0) {
+            *info = 0;
+            return (int)SDPG_OK;
+        }
+        return dispatch_limbs(limbs, [&](auto tag) {
+            constexpr int N = decltype(tag)::value;
+            DeviceBuffer dinfo(sizeof(int));
+            int rc = with_device_copy(limbs, (size_t)lda * n, A, true, A, [&](void *dA) {
+                Workspace &ws = thread_workspace();
+                ws.reset();
+                GemmProblem<N> p{};
+                p.M = n;
+                p.Nn = n;
+                p.K = 32;
+                p.batch = 1;
+                ws.reserve(gemm_workspace_bytes<N>(p) + (1 << 20));
+                ml_potrf<N>(n, (mlf<N> *)dA, lda, (int *)dinfo.p, ws, nullptr);
+                return (int)SDPG_OK;
+            });
+            SDPG_CUDA(cudaMemcpy(info, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost));
+            return rc;
+        });
+    });
+}
+
+int sdpg_inv_lower(int limbs, int n, const void *L, int ldl, void *Linv) {
+    return sdpg_guard([&] {
+        if (n <= 0 || ldl < n || !L || !Linv) throw sdpg_error(SDPG_ERR_ARG, "bad arguments");
+        return dispatch_limbs(limbs, [&](auto tag) {
+            constexpr int N = decltype(tag)::value;
+            DeviceBuffer dout((size_t)n * n * sizeof(mlf<N>));
+            int rc = with_device_copy(limbs, (size_t)ldl * n, L, false, nullptr, [&](void *dL) {
+                Workspace &ws = thread_workspace();
+                ws.reset();
+                GemmProblem<N> p{};
+                p.M = 32;
+                p.Nn = n;
+                p.K = n;
+                p.batch = 1;
+                ws.reserve(2 * gemm_workspace_bytes<N>(p) + (size_t)32 * n * sizeof(mlf<N>) + (1 << 20));
+                ml_trtri_lower<N>(n, (const mlf<N> *)dL, ldl, (mlf<N> *)dout.p, ws, nullptr);
+                return (int)SDPG_OK;
+            });
+            SDPG_CUDA(cudaMemcpy(Linv, dout.p, (size_t)n * n * sizeof(mlf<N>), cudaMemcpyDeviceToHost));
+            return rc;
+        });
+    });
+}
+
+int sdpg_solve_systems(int limbs, int n, const void *L, int ldl, void *x) {
+    return sdpg_guard([&] {
+        if (n <= 0 || ldl < n || !L || !x) throw sdpg_error(SDPG_ERR_ARG, "bad arguments");
+        return dispatch_limbs(limbs, [&](auto tag) {
+            constexpr int N = decltype(tag)::value;
+            DeviceBuffer dx((size_t)n * sizeof(mlf<N>));
+            SDPG_CUDA(cudaMemcpy(dx.p, x, (size_t)n * sizeof(mlf<N>), cudaMemcpyHostToDevice));
+            int rc = with_device_copy(limbs, (size_t)ldl * n, L, false, nullptr, [&](void *dL) {
+                Workspace &ws = thread_workspace();
+                ws.reset();
+                ws.reserve((size_t)n * sizeof(mlf<N>) + (1 << 20));
+                ml_potrs<N>(n, (const mlf<N> *)dL, ldl, (mlf<N> *)dx.p, ws, nullptr);
+                return (int)SDPG_OK;
+            });
+            SDPG_CUDA(cudaMemcpy(x, dx.p, (size_t)n * sizeof(mlf<N>), cudaMemcpyDeviceToHost));
+            return rc;
+        });
+    });
+}
+
+int sdpg_tridiag_min(int limbs, int k, const void *d, const void *e, void *out2) {
+    return sdpg_guard([&] {
+        if (k <= 0 || !d || !out2 || (k > 1 && !e)) throw sdpg_error(SDPG_ERR_ARG, "bad arguments");
+        return dispatch_limbs(limbs, [&](auto tag) {
+            constexpr int N = decltype(tag)::value;
+            const size_t eb = sizeof(mlf<N>);
+            DeviceBuffer dd(k * eb), de((k > 1 ? k - 1 : 1) * eb), dout(2 * eb), dst(sizeof(int));
+            SDPG_CUDA(cudaMemcpy(dd.p, d, k * eb, cudaMemcpyHostToDevice));
+            if (k > 1) SDPG_CUDA(cudaMemcpy(de.p, e, (k - 1) * eb, cudaMemcpyHostToDevice));
+            k_tridiag_min<N>(k, (const mlf<N> *)dd.p, (const mlf<N> *)de.p, (mlf<N> *)dout.p, (int *)dst.p, nullptr);
+            SDPG_CUDA(cudaDeviceSynchronize());
+            int st = 0;
+            SDPG_CUDA(cudaMemcpy(&st, dst.p, sizeof(int), cudaMemcpyDeviceToHost));
+            SDPG_CUDA(cudaMemcpy(out2, dout.p, 2 * eb, cudaMemcpyDeviceToHost));
+            if (st != 0) throw sdpg_error(SDPG_ERR_NOCONV, "tridiagonal eigenvalue iteration did not converge");
+            return (int)SDPG_OK;
+        });
+    });
+}
+
+int sdpg_sym_min_eigen(int limbs, int n, const void *A, void *out) {
+    return sdpg_guard([&] {
+        if (n <= 0 || n > 64 || !A || !out) throw sdpg_error(SDPG_ERR_ARG, "n must be in 1..64");
+        return dispatch_limbs(limbs, [&](auto tag) {
+            constexpr int N = decltype(tag)::value;
+            const size_t eb = sizeof(mlf<N>);
+            DeviceBuffer dA((size_t)n * n * eb), dd(n * eb), de(n * eb), dout(2 * eb), dst(sizeof(int));
+            SDPG_CUDA(cudaMemcpy(dA.p, A, (size_t)n * n * eb, cudaMemcpyHostToDevice));
+            k_tridiagonalize_small<N>(n, (mlf<N> *)dA.p, (mlf<N> *)dd.p, (mlf<N> *)de.p, nullptr);
+            k_tridiag_min<N>(n, (const mlf<N> *)dd.p, (const mlf<N> *)de.p, (mlf<N> *)dout.p, (int *)dst.p, nullptr);
+            SDPG_CUDA(cudaDeviceSynchronize());
+            SDPG_CUDA(cudaMemcpy(out, dout.p, eb, cudaMemcpyDeviceToHost));
+            return (int)SDPG_OK;
+        });
     });
 }
 

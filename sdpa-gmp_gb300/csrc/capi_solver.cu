@@ -1,0 +1,404 @@
+// C ABI: problem construction, the whole interior-point solve, and the
+// step-wise Newton / step-length / update entry points.
+#include <string.h>
+
+#include <memory>
+
+#include "capi_util.cuh"
+#include "ml_host.h"
+#include "problem.h"
+#include "sdpg.h"
+#include "solver.cuh"
+
+using namespace sdpg;
+
+struct sdpg_problem {
+    RawProblem P;
+};
+
+struct sdpg_solver {
+    std::unique_ptr<SolverBase> s;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    ~sdpg_solver() {
+        s.reset();
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+Param to_param(const sdpg_param *p) {
+    Param q;
+    if (!p) return q;
+    q.maxIteration = p->maxIteration;
+    q.epsilonStar = p->epsilonStar;
+    q.lambdaStar = p->lambdaStar;
+    q.omegaStar = p->omegaStar;
+    q.lowerBound = p->lowerBound;
+    q.upperBound = p->upperBound;
+    q.betaStar = p->betaStar;
+    q.betaBar = p->betaBar;
+    q.gammaStar = p->gammaStar;
+    q.epsilonDash = p->epsilonDash;
+    q.precision = p->precision;
+    return q;
+}
+
+void from_param(const Param &q, sdpg_param *p) {
+    p->maxIteration = q.maxIteration;
+    p->epsilonStar = q.epsilonStar;
+    p->lambdaStar = q.lambdaStar;
+    p->omegaStar = q.omegaStar;
+    p->lowerBound = q.lowerBound;
+    p->upperBound = q.upperBound;
+    p->betaStar = q.betaStar;
+    p->betaBar = q.betaBar;
+    p->gammaStar = q.gammaStar;
+    p->epsilonDash = q.epsilonDash;
+    p->precision = q.precision;
+}
+
+void check_param(const Param &q) {
+    if (q.maxIteration < 0 || !(q.epsilonStar > 0) || !(q.lambdaStar > 0) || !(q.omegaStar > 1) ||
+        q.betaStar < 0 || q.betaStar >= 1 || q.betaBar < 0 || q.betaBar >= 1 || q.betaStar > q.betaBar ||
+        !(q.gammaStar > 0) || q.gammaStar >= 1 || !(q.epsilonDash > 0) || q.precision <= 0)
+        throw sdpg_error(SDPG_ERR_ARG, "parameter out of its documented range (sdpa_parts.cpp:163-176)");
+    if (q.precision > 512) throw sdpg_error(SDPG_ERR_ARG, "precision above 512 bits is not supported");
+}
+
+sdpg_solver *wrap(const RawProblem &P, const Param &q, int device, void *stream) {
+    check_param(q);
+    auto *h = new sdpg_solver();
+    try {
+        SDPG_CUDA(cudaSetDevice(device));
+        if (stream) {
+            h->stream = (cudaStream_t)stream;
+        } else {
+            SDPG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+            h->own_stream = true;
+        }
+        h->s.reset(make_solver(P, q, device, h->stream));
+    } catch (...) {
+        delete h;
+        throw;
+    }
+    return h;
+}
+
+SolverBase &S(sdpg_solver *h) {
+    if (!h || !h->s) throw sdpg_error(SDPG_ERR_ARG, "null solver handle");
+    return *h->s;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sdpg_param_default(sdpg_param *p, int type) {
+    return sdpg_guard([&] {
+        if (!p) throw sdpg_error(SDPG_ERR_ARG, "null param");
+        Param q;
+        param_default(q, type);
+        from_param(q, p);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_param_read(sdpg_param *p, const char *path) {
+    return sdpg_guard([&] {
+        if (!p || !path) throw sdpg_error(SDPG_ERR_ARG, "null argument");
+        Param q = to_param(p);
+        std::string err;
+        if (!param_read(q, path, &err)) throw sdpg_error(SDPG_ERR_IO, err);
+        from_param(q, p);
+        return (int)SDPG_OK;
+    });
+}
+
+sdpg_problem *sdpg_problem_new(int m, int nBlock, const int *blockStruct, int *err) {
+    int rc = sdpg_guard([&] {
+        if (m <= 0 || nBlock <= 0 || !blockStruct) throw sdpg_error(SDPG_ERR_ARG, "bad problem dimensions");
+        for (int l = 0; l < nBlock; ++l)
+            if (blockStruct[l] == 0) throw sdpg_error(SDPG_ERR_ARG, "zero block size");
+        return (int)SDPG_OK;
+    });
+    if (err) *err = rc;
+    if (rc != SDPG_OK) return nullptr;
+    auto *p = new sdpg_problem();
+    p->P.m = m;
+    p->P.blockStruct.assign(blockStruct, blockStruct + nBlock);
+    p->P.c.assign(m, ml_zero<16>());
+    return p;
+}
+
+sdpg_problem *sdpg_problem_read(const char *path, int dense_format, int *err) {
+    auto *p = new sdpg_problem();
+    int rc = sdpg_guard([&] {
+        std::string e;
+        if (!path || !read_sdpa(path, dense_format != 0, p->P, &e)) throw sdpg_error(SDPG_ERR_IO, e);
+        return (int)SDPG_OK;
+    });
+    if (err) *err = rc;
+    if (rc != SDPG_OK) {
+        delete p;
+        return nullptr;
+    }
+    return p;
+}
+
+void sdpg_problem_free(sdpg_problem *p) { delete p; }
+
+int sdpg_problem_set_c(sdpg_problem *p, int k, const char *text) {
+    return sdpg_guard([&] {
+        if (!p || k < 1 || k > p->P.m || !text) throw sdpg_error(SDPG_ERR_ARG, "bad c index");
+        mlf<16> v;
+        if (!ml_parse<16>(text, &v)) throw sdpg_error(SDPG_ERR_ARG, "not a number");
+        p->P.c[k - 1] = v;
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_problem_add_entry(sdpg_problem *p, int k, int block, int i, int j, const char *text) {
+    return sdpg_guard([&] {
+        if (!p || !text || k < 0 || k > p->P.m || block < 1 || block > (int)p->P.blockStruct.size())
+            throw sdpg_error(SDPG_ERR_ARG, "entry index out of range");
+        const int bs = p->P.blockStruct[block - 1];
+        const int size = bs < 0 ? -bs : bs;
+        if (i < 1 || j < 1 || i > size || j > size) throw sdpg_error(SDPG_ERR_ARG, "out of range in input data");
+        RawEntry e;
+        if (!ml_parse<16>(text, &e.v)) throw sdpg_error(SDPG_ERR_ARG, "not a number");
+        e.k = k;
+        e.block = block - 1;
+        e.i = i - 1;
+        e.j = j - 1;
+        p->P.entries.push_back(e);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_problem_add_entry_mpf(sdpg_problem *p, int k, int block, int i, int j, const sdpg_mpf_t *v) {
+    return sdpg_guard([&] {
+        if (!p || !v) throw sdpg_error(SDPG_ERR_ARG, "null argument");
+        if (k < 0 || k > p->P.m || block < 1 || block > (int)p->P.blockStruct.size())
+            throw sdpg_error(SDPG_ERR_ARG, "entry index out of range");
+        const int bs = p->P.blockStruct[block - 1];
+        const int size = bs < 0 ? -bs : bs;
+        if (i < 1 || j < 1 || i > size || j > size) throw sdpg_error(SDPG_ERR_ARG, "out of range in input data");
+        RawEntry e;
+        e.v = ml_from_mpf<16>(v->_mp_size, v->_mp_exp, v->_mp_d);
+        e.k = k;
+        e.block = block - 1;
+        e.i = i - 1;
+        e.j = j - 1;
+        p->P.entries.push_back(e);
+        return (int)SDPG_OK;
+    });
+}
+
+sdpg_solver *sdpg_solver_create(const sdpg_problem *p, const sdpg_param *param, int device, void *stream, int *err) {
+    sdpg_solver *h = nullptr;
+    int rc = sdpg_guard([&] {
+        if (!p) throw sdpg_error(SDPG_ERR_ARG, "null problem");
+        Param q = param ? to_param(param) : Param();
+        h = wrap(p->P, q, device, stream);
+        return (int)SDPG_OK;
+    });
+    if (err) *err = rc;
+    return rc == SDPG_OK ? h : nullptr;
+}
+
+void sdpg_solver_destroy(sdpg_solver *h) { delete h; }
+
+int sdpg_solver_limbs(sdpg_solver *h) {
+    return sdpg_guard([&] { return S(h).limbs(); });
+}
+
+int sdpg_solver_initialize(sdpg_solver *h) {
+    return sdpg_guard([&] {
+        S(h).initialize();
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_solver_run(sdpg_solver *h, const char *out_path, int print_to_stdout) {
+    return sdpg_guard([&] {
+        FILE *out = nullptr;
+        if (out_path && out_path[0]) {
+            out = fopen(out_path, "w");
+            if (!out) throw sdpg_error(SDPG_ERR_IO, std::string("cannot open out file ") + out_path);
+        }
+        int it;
+        try {
+            it = S(h).run(out, print_to_stdout ? stdout : nullptr);
+        } catch (...) {
+            if (out) fclose(out);
+            throw;
+        }
+        if (out) fclose(out);
+        return it;
+    });
+}
+
+int sdpg_newton(sdpg_solver *h, int direction) {
+    return sdpg_guard([&] { return S(h).newton(direction) ? (int)SDPG_OK : (int)SDPG_ERR_NOT_PD; });
+}
+
+int sdpg_step_length(sdpg_solver *h, int direction) {
+    return sdpg_guard([&] {
+        S(h).step_length(direction);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_update(sdpg_solver *h) {
+    return sdpg_guard([&] { return S(h).update() ? (int)SDPG_OK : (int)SDPG_ERR_NOT_PD; });
+}
+
+int sdpg_residuals(sdpg_solver *h) {
+    return sdpg_guard([&] {
+        S(h).residuals();
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_solution_info(sdpg_solver *h, double *out12) {
+    return sdpg_guard([&] {
+        if (!out12) throw sdpg_error(SDPG_ERR_ARG, "null output");
+        S(h).info(out12);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_solution_text(sdpg_solver *h, int which, int digits, char *buf, int cap) {
+    return sdpg_guard([&] {
+        std::string s = S(h).info_text(which, digits > 1 ? digits : 2);
+        if (!buf || (int)s.size() + 1 > cap) throw sdpg_error(SDPG_ERR_ARG, "buffer too small");
+        memcpy(buf, s.c_str(), s.size() + 1);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_get_xvec(sdpg_solver *h, int form, void *out) {
+    return sdpg_guard([&] {
+        if (!out) throw sdpg_error(SDPG_ERR_ARG, "null output");
+        S(h).get_y(out, form);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_get_block(sdpg_solver *h, int which, int block, int form, void *out) {
+    return sdpg_guard([&] {
+        if (!out || block < 0 || block >= S(h).nblocks()) throw sdpg_error(SDPG_ERR_ARG, "bad block");
+        S(h).get_block(which, block, out, form);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_make_schur(sdpg_solver *h, void *out_ml) {
+    return sdpg_guard([&] {
+        if (!out_ml) throw sdpg_error(SDPG_ERR_ARG, "null output");
+        S(h).make_bmat(out_ml);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_make_gvec(sdpg_solver *h, int direction, void *out_ml) {
+    return sdpg_guard([&] {
+        if (!out_ml) throw sdpg_error(SDPG_ERR_ARG, "null output");
+        S(h).make_gvec(direction, out_ml);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_min_eigen(sdpg_solver *h, int side, void *out_ml) {
+    return sdpg_guard([&] {
+        if (!out_ml) throw sdpg_error(SDPG_ERR_ARG, "null output");
+        S(h).min_eigen(side, out_ml);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_get_vector(sdpg_solver *h, int which, void *out_ml) {
+    return sdpg_guard([&] {
+        if (!out_ml) throw sdpg_error(SDPG_ERR_ARG, "null output");
+        S(h).get_vec(which, out_ml);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_solver_dims(sdpg_solver *h, int *m, int *nblocks, int *block_sizes, int cap) {
+    return sdpg_guard([&] {
+        SolverBase &s = S(h);
+        if (m) *m = s.m();
+        if (nblocks) *nblocks = s.nblocks();
+        for (int l = 0; block_sizes && l < s.nblocks() && l < cap; ++l) block_sizes[l] = s.block_size(l);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_solver_timers(sdpg_solver *h, double *out8) {
+    return sdpg_guard([&] {
+        const Timers &t = S(h).timers();
+        double v[8] = {t.schur, t.cholesky, t.rmat_gvec, t.dxdz, t.steplen, t.update, t.residual, t.total};
+        memcpy(out8, v, sizeof v);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_solver_history(sdpg_solver *h, double *out, int cap) {
+    return sdpg_guard([&] {
+        const auto &hist = S(h).history();
+        const int n = (int)hist.size();
+        for (int i = 0; i < n && i < cap; ++i) {
+            const IterRecord &r = hist[i];
+            double v[9] = {(double)r.it, r.mu, r.thetaP, r.thetaD, r.objP, r.objD, r.alphaP, r.alphaD, r.beta};
+            memcpy(out + 9 * i, v, sizeof v);
+        }
+        return n;
+    });
+}
+
+long long sdpg_solver_gemm_macs(sdpg_solver *h) {
+    long long v = 0;
+    int rc = sdpg_guard([&] {
+        v = S(h).gemm_macs();
+        return (int)SDPG_OK;
+    });
+    return rc == SDPG_OK ? v : rc;
+}
+
+int sdpg_solver_reset_counters(sdpg_solver *h) {
+    return sdpg_guard([&] {
+        S(h).reset_counters();
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_solve_file(const char *data_path, const char *param_path, const char *out_path, int device, double *info12) {
+    return sdpg_guard([&] {
+        Param q;
+        std::string err;
+        if (param_path && param_path[0] && !param_read(q, param_path, &err)) throw sdpg_error(SDPG_ERR_IO, err);
+        RawProblem P;
+        if (!read_sdpa(data_path, false, P, &err)) throw sdpg_error(SDPG_ERR_IO, err);
+        std::unique_ptr<sdpg_solver> h(wrap(P, q, device, nullptr));
+        FILE *out = nullptr;
+        if (out_path && out_path[0]) {
+            out = fopen(out_path, "w");
+            if (!out) throw sdpg_error(SDPG_ERR_IO, std::string("cannot open out file ") + out_path);
+        }
+        int it;
+        try {
+            it = h->s->run(out, nullptr);
+        } catch (...) {
+            if (out) fclose(out);
+            throw;
+        }
+        if (out) fclose(out);
+        if (info12) h->s->info(info12);
+        return it;
+    });
+}
+
+}  // extern "C"

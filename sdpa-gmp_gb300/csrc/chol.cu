@@ -1,0 +1,236 @@
+// Cholesky factorisation, triangular inverse and triangular solves in
+// multi-limb arithmetic (replacing Rpotrf / Rtrsm / Rtrsv as called from
+// Lal::choleskyFactorWithAdjust, Lal::getCholesky, Lal::getInvLowTriangularMatrix
+// and Lal::solveSystems, sdpa_linear.cpp:342-455, 608-695).
+//
+// Blocked right-looking with 32-wide panels: the diagonal block is factored in
+// one CTA (pivot square roots and reciprocals in full multi-limb precision), the
+// panel below is solved one row per warp, and the trailing matrix is updated by
+// the block-floating-point GEMM (lower triangle only).
+#include "kernels.cuh"
+#include "mlwarp.cuh"
+
+namespace sdpg {
+
+namespace {
+
+constexpr int NB = 32;
+
+// Factor the kb x kb diagonal block at A (ld lda) in place; rinv[j] = 1/L[j][j].
+// info: 0, or (col0 + j + 1) for the first non-positive pivot.
+template <int N>
+__global__ void potf2_kernel(mlf<N> *A, int lda, int kb, int col0, int *info, mlf<N> *rinv) {
+    __shared__ int bad;
+    if (*info != 0) return;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    for (int j = 0; j < kb; ++j) {
+        if (threadIdx.x == 0) {
+            const mlf<N> d = A[j + (long long)j * lda];
+            if (ml_sign(d) <= 0) {
+                bad = col0 + j + 1;
+            } else {
+                const mlf<N> r = ml_rsqrt(d);
+                A[j + (long long)j * lda] = ml_mul(d, r);  // sqrt(d)
+                rinv[j] = r;
+            }
+        }
+        __syncthreads();
+        if (bad) break;
+        const mlf<N> r = rinv[j];
+        for (int i = j + 1 + threadIdx.x; i < kb; i += blockDim.x)
+            A[i + (long long)j * lda] = ml_mul(A[i + (long long)j * lda], r);
+        __syncthreads();
+        // trailing lower triangle of the block: A[i,t] -= L[i,j] L[t,j], j < t <= i < kb
+        const int w = kb - j - 1;
+        const int cnt = w * (w + 1) / 2;
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            // q -> (ii, tt) with 0 <= tt <= ii < w
+            int ii = (int)((sqrtf(8.0f * q + 1.0f) - 1.0f) * 0.5f);
+            while (ii * (ii + 1) / 2 > q) --ii;
+            while ((ii + 1) * (ii + 2) / 2 <= q) ++ii;
+            const int tt = q - ii * (ii + 1) / 2;
+            const int i = j + 1 + ii, t = j + 1 + tt;
+            mlf<N> *a = A + i + (long long)t * lda;
+            *a = ml_sub(*a, ml_mul(A[i + (long long)j * lda], A[t + (long long)j * lda]));
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && bad) *info = bad;
+}
+
+// Rows below the diagonal block: solve x * L11^T = a for each row (one warp per row).
+// L11 at Ld (ld lda, kb x kb lower), rows at R (ld lda), nrows rows.
+template <int N>
+__global__ void panel_trsm_kernel(const mlf<N> *Ld, mlf<N> *R, int lda, int kb, int nrows, const int *info,
+                                  const mlf<N> *rinv) {
+    if (*info != 0) return;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= nrows) return;
+    mlf<N> *row = R + warp;  // element t at row[t * lda]
+    mlf<N> a = lane < kb ? row[(long long)lane * lda] : ml_zero<N>();
+    for (int j = 0; j < kb; ++j) {
+        mlf<N> xj = ml_zero<N>();
+        if (lane == j) xj = ml_mul(a, rinv[j]);
+        xj = ml_shfl(xj, j);
+        if (lane == j) a = xj;
+        if (lane > j && lane < kb) a = ml_sub(a, ml_mul(xj, Ld[lane + (long long)j * lda]));
+    }
+    if (lane < kb) row[(long long)lane * lda] = a;
+}
+
+// Invert every kb x kb diagonal block of the lower-triangular L into Linv.
+template <int N>
+__global__ void trtri_diag_kernel(const mlf<N> *L, int ldl, mlf<N> *Linv, int ldi, int n) {
+    const int b = blockIdx.x;
+    const int o = b * NB;
+    const int kb = min(NB, n - o);
+    const mlf<N> *T = L + o + (long long)o * ldl;
+    mlf<N> *X = Linv + o + (long long)o * ldi;
+    __shared__ mlf<N> rv[NB];
+    if (threadIdx.x < kb) rv[threadIdx.x] = ml_recip(T[threadIdx.x + (long long)threadIdx.x * ldl]);
+    // X = I (lower part)
+    for (int q = threadIdx.x; q < kb * kb; q += blockDim.x) {
+        const int i = q % kb, c = q / kb;
+        if (i >= c) X[i + (long long)c * ldi] = (i == c) ? ml_one<N>() : ml_zero<N>();
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; ++j) {
+        // row j of X scaled by 1/T[j,j] (columns c <= j)
+        for (int c = threadIdx.x; c <= j; c += blockDim.x) X[j + (long long)c * ldi] = ml_mul(X[j + (long long)c * ldi], rv[j]);
+        __syncthreads();
+        // X[i,c] -= T[i,j] X[j,c] for i > j, c <= j
+        const int rows = kb - j - 1, cols = j + 1;
+        for (int q = threadIdx.x; q < rows * cols; q += blockDim.x) {
+            const int i = j + 1 + q % rows, c = q / rows;
+            mlf<N> *x = X + i + (long long)c * ldi;
+            *x = ml_sub(*x, ml_mul(T[i + (long long)j * ldl], X[j + (long long)c * ldi]));
+        }
+        __syncthreads();
+    }
+}
+
+template <int N>
+__global__ void recip_diag_kernel(int n, const mlf<N> *L, int ldl, mlf<N> *rinv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) rinv[i] = ml_recip(L[i + (long long)i * ldl]);
+}
+
+// x := L^{-T} L^{-1} x in one CTA (forward then backward substitution)
+template <int N>
+__global__ void potrs_kernel(int n, const mlf<N> *L, int ldl, const mlf<N> *rinv, mlf<N> *x) {
+    for (int j = 0; j < n; ++j) {
+        if (threadIdx.x == 0) x[j] = ml_mul(x[j], rinv[j]);
+        __syncthreads();
+        const mlf<N> xj = x[j];
+        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x)
+            x[i] = ml_sub(x[i], ml_mul(L[i + (long long)j * ldl], xj));
+        __syncthreads();
+    }
+    for (int j = n - 1; j >= 0; --j) {
+        if (threadIdx.x == 0) x[j] = ml_mul(x[j], rinv[j]);
+        __syncthreads();
+        const mlf<N> xj = x[j];
+        for (int i = threadIdx.x; i < j; i += blockDim.x)
+            x[i] = ml_sub(x[i], ml_mul(L[j + (long long)i * ldl], xj));
+        __syncthreads();
+    }
+}
+
+template <int N>
+GemmProblem<N> gemm_nn(int M, int Nn, int K, const mlf<N> &alpha, const mlf<N> *A, long long lda, char ta,
+                       const mlf<N> *B, long long ldb, char tb, const mlf<N> &beta, mlf<N> *C, long long ldc) {
+    GemmProblem<N> p{};
+    p.M = M;
+    p.Nn = Nn;
+    p.K = K;
+    p.batch = 1;
+    p.A = operand_A<N>(ta, A, lda, 0);
+    p.B = operand_B<N>(tb, B, ldb, 0);
+    p.C = C;
+    p.ldc = ldc;
+    p.sc = 0;
+    p.alpha = alpha;
+    p.beta = beta;
+    p.lower_only = 0;
+    return p;
+}
+
+}  // namespace
+
+template <int N>
+void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t s) {
+    SDPG_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
+    const size_t mark = ws.used;
+    mlf<N> *rinv = (mlf<N> *)ws.carve(NB * sizeof(mlf<N>));
+    const mlf<N> mone = ml_from_int<N>(-1), one = ml_one<N>();
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        const int kb = min(NB, n - k0);
+        mlf<N> *Akk = A + k0 + (long long)k0 * lda;
+        potf2_kernel<N><<<1, 256, 0, s>>>(Akk, lda, kb, k0, info, rinv);
+        SDPG_CHECK_LAUNCH();
+        const int rows = n - k0 - kb;
+        if (rows <= 0) break;
+        mlf<N> *A21 = A + (k0 + kb) + (long long)k0 * lda;
+        panel_trsm_kernel<N><<<ceil_div((long long)rows * 32, 256), 256, 0, s>>>(Akk, A21, lda, kb, rows, info, rinv);
+        SDPG_CHECK_LAUNCH();
+        GemmProblem<N> p = gemm_nn<N>(rows, rows, kb, mone, A21, lda, 'N', A21, lda, 'T', one,
+                                      A + (k0 + kb) + (long long)(k0 + kb) * lda, lda);
+        p.lower_only = 1;
+        const size_t m2 = ws.used;
+        ml_gemm<N>(p, ws, s);
+        ws.used = m2;
+    }
+    ws.used = mark;
+}
+
+template <int N>
+void ml_trtri_lower(int n, const mlf<N> *L, int ldl, mlf<N> *Linv, Workspace &ws, cudaStream_t s) {
+    // Linv assumed n x n with leading dimension n
+    SDPG_CUDA(cudaMemsetAsync(Linv, 0, (size_t)n * n * sizeof(mlf<N>), s));
+    const int nb = ceil_div(n, NB);
+    trtri_diag_kernel<N><<<nb, 256, 0, s>>>(L, ldl, Linv, n, n);
+    SDPG_CHECK_LAUNCH();
+    const size_t mark = ws.used;
+    mlf<N> *W = (mlf<N> *)ws.carve((size_t)NB * n * sizeof(mlf<N>));
+    const mlf<N> one = ml_one<N>(), zero = ml_zero<N>(), mone = ml_from_int<N>(-1);
+    for (int ib = 1; ib < nb; ++ib) {
+        const int i0 = ib * NB, kb = min(NB, n - i0);
+        // W (kb x i0) = L[i0:i0+kb, 0:i0] * Linv[0:i0, 0:i0]
+        {
+            GemmProblem<N> p = gemm_nn<N>(kb, i0, i0, one, L + i0, ldl, 'N', Linv, n, 'N', zero, W, kb);
+            const size_t m2 = ws.used;
+            ml_gemm<N>(p, ws, s);
+            ws.used = m2;
+        }
+        // Linv[i0:i0+kb, 0:i0] = -Linv[i0:, i0:] (kb x kb) * W
+        {
+            GemmProblem<N> p = gemm_nn<N>(kb, i0, kb, mone, Linv + i0 + (long long)i0 * n, n, 'N', W, kb, 'N', zero,
+                                          Linv + i0, n);
+            const size_t m2 = ws.used;
+            ml_gemm<N>(p, ws, s);
+            ws.used = m2;
+        }
+    }
+    ws.used = mark;
+}
+
+template <int N>
+void ml_potrs(int n, const mlf<N> *L, int ldl, mlf<N> *x, Workspace &ws, cudaStream_t s) {
+    const size_t mark = ws.used;
+    mlf<N> *rinv = (mlf<N> *)ws.carve((size_t)n * sizeof(mlf<N>));
+    recip_diag_kernel<N><<<ceil_div(n, 128), 128, 0, s>>>(n, L, ldl, rinv);
+    SDPG_CHECK_LAUNCH();
+    potrs_kernel<N><<<1, 512, 0, s>>>(n, L, ldl, rinv, x);
+    SDPG_CHECK_LAUNCH();
+    ws.used = mark;
+}
+
+#define SDPG_INST_CHOL(N)                                                                       \
+    template void ml_potrf<N>(int, mlf<N> *, int, int *, Workspace &, cudaStream_t);            \
+    template void ml_trtri_lower<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t); \
+    template void ml_potrs<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t);
+SDPG_INST_CHOL(8)
+SDPG_INST_CHOL(16)
+
+}  // namespace sdpg

@@ -1,0 +1,1156 @@
+// Interior-point solver: state resident on the GPU, control scalars on the host.
+//
+// Each method restates the reference routine named in its comment.  The
+// reference is SDPA-GMP 7.1.3 with REVERSE_PRIMAL_DUAL on (sdpa_tool.h:84):
+// internally it solves  min C.X  s.t. A_i.X = b_i, X >= 0  (C = -F0 of the
+// file) with the HRVW/KSH/M direction and Mehrotra predictor-corrector steps.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <map>
+
+#include "solver.cuh"
+
+namespace sdpg {
+
+const char *phase_name(int phase) {
+    switch (phase) {
+        case noINFO: return "noINFO    ";
+        case pFEAS: return "pFEAS     ";
+        case dFEAS: return "dFEAS     ";
+        case pdFEAS: return "pdFEAS    ";
+        case pdINF: return "pdINF     ";
+        case pFEAS_dINF: return "pFEAS_dINF";
+        case pINF_dFEAS: return "pINF_dFEAS";
+        case pdOPT: return "pdOPT     ";
+        case pUNBD: return "pUNBD     ";
+        case dUNBD: return "dUNBD     ";
+    }
+    return "phase error";
+}
+
+namespace {
+
+enum Formula { F1 = 0, F2 = 1, F3 = 2 };
+
+template <int N>
+class Solver final : public SolverBase {
+    using R = Real<N>;
+    using V = mlf<N>;
+
+    struct Blk {
+        int n = 0;
+        V *C, *X, *Z, *Zinv, *LX, *LZ, *Dx, *Dz, *Rm, *XRDZ, *W1, *W2, *Dres, *Lt, *F;
+        V *q, *qold, *r, *w, *tmp, *td, *te;
+        BlockDev<N> cons;
+        std::vector<int> f1_owners_h;
+        int *f1_owners = nullptr;
+        int nF1 = 0;
+        int lanczos_kmax = 0;
+    };
+
+  public:
+    Solver(const RawProblem &P, const Param &par, int device, cudaStream_t stream) : par_(par), st_(stream) {
+        SDPG_CUDA(cudaSetDevice(device));
+        setup(P);
+    }
+    ~Solver() override {
+        for (void *p : allocs_) cudaFree(p);
+        for (auto &e : ev_) cudaEventDestroy(e);
+    }
+
+    int limbs() const override { return N; }
+    int m() const override { return m_; }
+    int nblocks() const override { return (int)blk_.size(); }
+    int block_size(int l) const override { return blk_[l].n; }
+    int phase() const override { return phase_; }
+    int iteration() const override { return iter_; }
+    const Timers &timers() const override { return tm_; }
+    const std::vector<IterRecord> &history() const override { return hist_; }
+    void set_trace(FILE *f) override { trace_ = f; }
+    long long gemm_macs() const override { return gemm_macs_; }
+    void reset_counters() override {
+        gemm_macs_ = 0;
+        tm_ = Timers();
+    }
+    void sync() override { SDPG_CUDA(cudaStreamSynchronize(st_)); }
+
+    // ---------------------------------------------------------------- setup
+
+    void setup(const RawProblem &P) {
+        m_ = P.m;
+        if (m_ <= 0) throw sdpg_error(SDPG_ERR_ARG, "mDIM must be positive");
+        std::vector<int> sdp_of_file(P.blockStruct.size(), -1);
+        for (size_t l = 0; l < P.blockStruct.size(); ++l) {
+            const int bs = P.blockStruct[l];
+            if (bs >= 2) {
+                sdp_of_file[l] = (int)blk_.size();
+                blk_.emplace_back();
+                blk_.back().n = bs;
+            } else {
+                throw sdpg_error(SDPG_ERR_ARG, "LP (diagonal) blocks are not supported by this solver build");
+            }
+        }
+        nDim_ = 0;
+        for (auto &b : blk_) nDim_ += b.n;
+        // b = c
+        std::vector<V> bh(m_);
+        for (int k = 0; k < m_; ++k) bh[k] = narrow<N>(P.c[k]);
+        b_ = dalloc(m_);
+        y_ = dalloc(m_);
+        Dy_ = dalloc(m_);
+        g_ = dalloc(m_);
+        p_ = dalloc(m_);
+        B_ = dalloc((size_t)m_ * m_);
+        upload(b_, bh.data(), m_);
+        b_h_ = bh;
+        info_ = (int *)dalloc_raw(64);
+        status_ = (int *)dalloc_raw(64);
+        slot_ = dalloc(kSlots);
+        // entries per (constraint, block)
+        const int nb = (int)blk_.size();
+        std::vector<std::vector<std::vector<const RawEntry *>>> ent(m_ + 1, std::vector<std::vector<const RawEntry *>>(nb));
+        for (const auto &e : P.entries) {
+            const int l = sdp_of_file[e.block];
+            if (l < 0) continue;
+            ent[e.k][l].push_back(&e);
+        }
+        size_t max_ws = 0;
+        const mlf<N> kappa_v = ml_from_double<N>(1.2);  // Newton::computeFormula_SDP(..., KAPPA), sdpa_main.cpp:27
+        for (int l = 0; l < nb; ++l) {
+            Blk &B = blk_[l];
+            const int n = B.n;
+            const size_t nn = (size_t)n * n;
+            V **mats[] = {&B.C, &B.X, &B.Z, &B.Zinv, &B.LX, &B.LZ, &B.Dx, &B.Dz, &B.Rm, &B.XRDZ, &B.W1, &B.W2, &B.Dres, &B.Lt, &B.F};
+            for (V **mp : mats) *mp = dalloc(nn);
+            // C = -F0 (dense on the device; duplicates accumulate like sparse inner products)
+            {
+                std::vector<V> Ch(nn, ml_zero<N>());
+                for (const RawEntry *e : ent[0][l]) {
+                    const V v = ml_neg(narrow<N>(e->v));
+                    Ch[e->i + (size_t)n * e->j] = ml_add(Ch[e->i + (size_t)n * e->j], v);
+                    if (e->i != e->j) Ch[e->j + (size_t)n * e->i] = ml_add(Ch[e->j + (size_t)n * e->i], v);
+                }
+                upload(B.C, Ch.data(), nn);
+            }
+            // constraints touching this block, in increasing index (InputData::initialize_index_SDP)
+            std::vector<int> cids, nzc, nze, dense;
+            for (int k = 1; k <= m_; ++k) {
+                if (ent[k][l].empty()) continue;
+                cids.push_back(k - 1);
+                const int cnt = (int)ent[k][l].size();
+                nzc.push_back(cnt);
+                // SparseMatrix::changeToDense: stays sparse if NonZeroCount < nRow*nCol*0.20
+                const bool isdense = !((double)cnt < (double)(n * n) * 0.20);
+                dense.push_back(isdense ? 1 : 0);
+                int eff = 0;
+                if (isdense) eff = n * n;
+                else
+                    for (const RawEntry *e : ent[k][l]) eff += (e->i == e->j) ? 1 : 2;
+                nze.push_back(eff);
+            }
+            const int nc = (int)cids.size();
+            B.cons.n = n;
+            B.cons.nc = nc;
+            // formula choice (Newton::computeFormula_SDP, sdpa_newton.cpp:694-819)
+            std::vector<int> formula(nc);
+            for (int a = 0; a < nc; ++a) {
+                const int i = cids[a], inz = nze[a];
+                long up = inz;
+                for (int c = 0; c < nc; ++c) {
+                    const int j = cids[c], jnz = nze[c];
+                    if (jnz < inz) up += jnz;
+                    else if (jnz == inz && j < i) up += jnz;
+                }
+                const R K(kappa_v), nR(n), inzR(inz), upR(up);
+                const R f1 = K * nR * inzR + nR * nR * nR + K * upR;
+                const R f2 = K * nR * inzR + K * (nR + R(1)) * upR;
+                const R f3 = K * (R(2) * K * inzR + R(1)) * upR / K;
+                if (dense[a]) formula[a] = (f1 < f2) ? F1 : F2;
+                else if (f1 < f2 && f1 < f3) formula[a] = F1;
+                else if (f2 < f3) formula[a] = F2;
+                else formula[a] = F3;
+            }
+            // rank by (NonZeroEffect, index)
+            std::vector<int> order(nc), rank(nc);
+            for (int a = 0; a < nc; ++a) order[a] = a;
+            std::sort(order.begin(), order.end(), [&](int x, int y) {
+                return nze[x] != nze[y] ? nze[x] < nze[y] : cids[x] < cids[y];
+            });
+            for (int r = 0; r < nc; ++r) rank[order[r]] = r;
+            // sparse COO (symmetric expansion, duplicates merged) and dense matrices
+            std::vector<int> sp_off(nc + 1, 0), sp_row, sp_col, dn_slot(nc, -1), dn_cid, dn_local;
+            std::vector<V> sp_val, dn_val;
+            std::map<long long, std::vector<std::pair<int, V>>> pos;  // r + c*n -> (k, v)
+            for (int a = 0; a < nc; ++a) {
+                const auto &E = ent[cids[a] + 1][l];
+                if (dense[a]) {
+                    dn_slot[a] = (int)dn_cid.size();
+                    dn_cid.push_back(cids[a]);
+                    dn_local.push_back(a);
+                    std::vector<V> M(nn, ml_zero<N>());
+                    for (const RawEntry *e : E) {  // changeToDense: later duplicates overwrite
+                        const V v = narrow<N>(e->v);
+                        M[e->i + (size_t)n * e->j] = v;
+                        M[e->j + (size_t)n * e->i] = v;
+                    }
+                    dn_val.insert(dn_val.end(), M.begin(), M.end());
+                } else {
+                    std::map<long long, V> acc;
+                    for (const RawEntry *e : E) {
+                        const V v = narrow<N>(e->v);
+                        const long long k1 = e->i + (long long)n * e->j;
+                        acc[k1] = acc.count(k1) ? ml_add(acc[k1], v) : v;
+                        if (e->i != e->j) {
+                            const long long k2 = e->j + (long long)n * e->i;
+                            acc[k2] = acc.count(k2) ? ml_add(acc[k2], v) : v;
+                        }
+                    }
+                    for (auto &kv : acc) {
+                        sp_row.push_back((int)(kv.first % n));
+                        sp_col.push_back((int)(kv.first / n));
+                        sp_val.push_back(kv.second);
+                        pos[kv.first].push_back({cids[a], kv.second});
+                    }
+                }
+                sp_off[a + 1] = (int)sp_row.size();
+            }
+            B.cons.ndense = (int)dn_cid.size();
+            B.cons.cid = upload_new(cids);
+            B.cons.rank = upload_new(rank);
+            B.cons.formula = upload_new(formula);
+            B.cons.sp_off = upload_new(sp_off);
+            B.cons.sp_row = upload_new(sp_row);
+            B.cons.sp_col = upload_new(sp_col);
+            B.cons.sp_val = upload_new(sp_val);
+            B.cons.dn_slot = upload_new(dn_slot);
+            B.cons.dn_cid = upload_new(dn_cid);
+            B.cons.dn_local = upload_new(dn_local);
+            std::vector<long long> dn_off(dn_cid.size());
+            for (size_t d = 0; d < dn_off.size(); ++d) dn_off[d] = (long long)d * (long long)nn;
+            B.cons.dn_off = upload_new(dn_off);
+            B.cons.dense = upload_new(dn_val);
+            std::vector<int> pos_rc, pos_off(1, 0), pos_k;
+            std::vector<V> pos_v;
+            for (auto &kv : pos) {
+                pos_rc.push_back((int)kv.first);
+                for (auto &pr : kv.second) {
+                    pos_k.push_back(pr.first);
+                    pos_v.push_back(pr.second);
+                }
+                pos_off.push_back((int)pos_k.size());
+            }
+            B.cons.npos = (int)pos_rc.size();
+            B.cons.pos_rc = upload_new(pos_rc);
+            B.cons.pos_off = upload_new(pos_off);
+            B.cons.pos_k = upload_new(pos_k);
+            B.cons.pos_v = upload_new(pos_v);
+            for (int a = 0; a < nc; ++a)
+                if (formula[a] != F3) B.f1_owners_h.push_back(a);
+            B.nF1 = (int)B.f1_owners_h.size();
+            B.f1_owners = upload_new(B.f1_owners_h);
+            // Lanczos vectors; at most min(n, sqrt(n)+10) steps (sdpa_linear.cpp:43)
+            B.lanczos_kmax = std::min(n, (int)sqrt((double)n) + 12) + 2;
+            B.q = dalloc(n);
+            B.qold = dalloc(n);
+            B.r = dalloc(n);
+            B.w = dalloc(n);
+            B.tmp = dalloc(n);
+            B.td = dalloc(std::max(B.lanczos_kmax, n) + 2);
+            B.te = dalloc(std::max(B.lanczos_kmax, n) + 2);
+            // workspace need
+            max_ws = std::max(max_ws, gemm_bytes(n, n, n, 1));
+            const int chunk = f1_chunk(B);
+            if (B.nF1 > 0) {
+                max_ws = std::max(max_ws, gemm_bytes(n, n, n, chunk) + 3 * (size_t)chunk * nn * sizeof(V));
+                if (B.cons.ndense > 0) {
+                    max_ws = std::max(max_ws, gemm_bytes(chunk, B.cons.ndense, (int)nn, 1) +
+                                                  3 * (size_t)chunk * nn * sizeof(V) +
+                                                  (size_t)chunk * B.cons.ndense * sizeof(V) + (size_t)chunk * B.cons.ndense * 16);
+                }
+            }
+            max_ws = std::max(max_ws, gemm_bytes(32, n, n, 1) + 32 * (size_t)n * sizeof(V));
+        }
+        max_ws = std::max(max_ws, gemm_bytes(m_, m_, 32, 1));
+        ws_.reserve(max_ws + (64u << 20));
+        ev_.resize(2);
+        for (auto &e : ev_) SDPG_CUDA(cudaEventCreate(&e));
+    }
+
+    int f1_chunk(const Blk &B) const {
+        const size_t nn = (size_t)B.n * B.n;
+        size_t c = (size_t)(1ull << 30) / (3 * nn * sizeof(V) + 1);
+        if (c < 1) c = 1;
+        if ((int)c > B.nF1) c = B.nF1 > 0 ? B.nF1 : 1;
+        return (int)c;
+    }
+
+    static size_t gemm_bytes(int M, int Nn, int K, int batch) {
+        GemmProblem<N> p{};
+        p.M = M;
+        p.Nn = Nn;
+        p.K = K;
+        p.batch = batch;
+        p.A.sb = batch > 1 ? 1 : 0;
+        p.B.sb = batch > 1 ? 1 : 0;
+        return gemm_workspace_bytes<N>(p);
+    }
+
+    // ---------------------------------------------------------------- memory helpers
+
+    static constexpr int kSlots = 64;
+    std::vector<void *> allocs_;
+    void *dalloc_raw(size_t bytes) {
+        void *p = nullptr;
+        SDPG_CUDA(cudaMalloc(&p, bytes ? bytes : 16));
+        SDPG_CUDA(cudaMemset(p, 0, bytes ? bytes : 16));
+        allocs_.push_back(p);
+        return p;
+    }
+    V *dalloc(size_t count) { return (V *)dalloc_raw(count * sizeof(V)); }
+    template <class T>
+    T *upload_new(const std::vector<T> &h) {
+        T *d = (T *)dalloc_raw(h.size() * sizeof(T));
+        if (!h.empty()) SDPG_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+        return d;
+    }
+    void upload(V *d, const V *h, size_t count) {
+        SDPG_CUDA(cudaMemcpy(d, h, count * sizeof(V), cudaMemcpyHostToDevice));
+    }
+    // read device scalar slots [0, cnt)
+    std::vector<R> fetch(int cnt) {
+        std::vector<V> h(cnt);
+        SDPG_CUDA(cudaMemcpyAsync(h.data(), slot_, cnt * sizeof(V), cudaMemcpyDeviceToHost, st_));
+        SDPG_CUDA(cudaStreamSynchronize(st_));
+        std::vector<R> r(cnt);
+        for (int i = 0; i < cnt; ++i) r[i] = R(h[i]);
+        return r;
+    }
+    R fetch1(const V *d) {
+        V h;
+        SDPG_CUDA(cudaMemcpyAsync(&h, d, sizeof(V), cudaMemcpyDeviceToHost, st_));
+        SDPG_CUDA(cudaStreamSynchronize(st_));
+        return R(h);
+    }
+
+    // ---------------------------------------------------------------- Lal-level helpers
+
+    // C = alpha * op(A) * op(B) + beta * C on n x n blocks (Lal::multiply -> Rgemm)
+    void mm(int n, V *C, const V *A, char ta, const V *Bm, char tb, const R &alpha = R(1), const R &beta = R(0)) {
+        GemmProblem<N> p{};
+        p.M = n;
+        p.Nn = n;
+        p.K = n;
+        p.batch = 1;
+        p.A = operand_A<N>(ta, A, n, 0);
+        p.B = operand_B<N>(tb, Bm, n, 0);
+        p.C = C;
+        p.ldc = n;
+        p.sc = 0;
+        p.alpha = alpha.v;
+        p.beta = beta.v;
+        gemm(p);
+    }
+    void gemm(const GemmProblem<N> &p) {
+        const size_t mark = ws_.used;
+        ml_gemm<N>(p, ws_, st_);
+        ws_.used = mark;
+        gemm_macs_ += (long long)p.M * p.Nn * p.K * p.batch;
+    }
+    // ret = sum over blocks of A_l . B_l  (Lal::let(ret,'=',A,'.',B) on DenseLinearSpace)
+    R ip_blocks(V *Blk::*a, V *Blk::*b) {
+        for (size_t l = 0; l < blk_.size(); ++l) {
+            const size_t mark = ws_.used;
+            k_dot<N>((long long)blk_[l].n * blk_[l].n, blk_[l].*a, blk_[l].*b, slot_ + l, ws_, st_);
+            ws_.used = mark;
+        }
+        auto v = fetch((int)blk_.size());
+        R s(0);
+        for (auto &x : v) s += x;
+        return s;
+    }
+    R ip_vec(const V *a, const V *b) {
+        const size_t mark = ws_.used;
+        k_dot<N>(m_, a, b, slot_, ws_, st_);
+        ws_.used = mark;
+        return fetch(1)[0];
+    }
+    // g = sum over blocks of A_i . M  (InputData::multi_InnerProductToA, sdpa_dataset.cpp:477-485)
+    void multi_inner(V *Blk::*M, V *g) {
+        SDPG_CUDA(cudaMemsetAsync(g, 0, m_ * sizeof(V), st_));
+        for (auto &B : blk_) {
+            const size_t mark = ws_.used;
+            k_constraint_inner<N>(B.cons, B.*M, g, ws_, st_);
+            ws_.used = mark;
+        }
+    }
+    // M = sum_i A_i y_i  (InputData::multi_plusToA, sdpa_dataset.cpp:488-493)
+    void multi_plus(const V *y, V *Blk::*M) {
+        for (auto &B : blk_) k_constraint_plus<N>(B.cons, y, B.*M, st_);
+    }
+    void axpby_blocks(V *Blk::*out, const R &a, V *Blk::*x, const R &b, V *Blk::*y) {
+        for (auto &B : blk_) k_axpby<N>((long long)B.n * B.n, a.v, B.*x, b.v, y ? B.*y : nullptr, B.*out, st_);
+    }
+
+    // ---------------------------------------------------------------- Newton (sdpa_newton.cpp)
+
+    // Newton::compute_rMat, sdpa_newton.cpp:821-838
+    void compute_rMat(bool corrector) {
+        const R target = betaV_ * muCur_;
+        axpby_blocks(&Blk::Rm, target, &Blk::Zinv, R(0), nullptr);
+        axpby_blocks(&Blk::Rm, R(1), &Blk::Rm, R(-1), &Blk::X);
+        if (corrector) {
+            for (auto &B : blk_) {
+                mm(B.n, B.W2, B.Dx, 'N', B.Dz, 'N');
+                mm(B.n, B.W1, B.W2, 'N', B.Zinv, 'N');
+            }
+            axpby_blocks(&Blk::Rm, R(1), &Blk::Rm, R(-1), &Blk::W1);
+        }
+    }
+
+    // Newton::Make_gVec, sdpa_newton.cpp:840-895
+    void Make_gVec(bool corrector) {
+        compute_rMat(corrector);
+        if (phase_ == pFEAS || phase_ == noINFO) {
+            if (!corrector) {
+                for (auto &B : blk_) {
+                    mm(B.n, B.W2, B.X, 'N', B.Dres, 'N');
+                    mm(B.n, B.XRDZ, B.W2, 'N', B.Zinv, 'N');
+                }
+            }
+            axpby_blocks(&Blk::W1, R(1), &Blk::Rm, R(-1), &Blk::XRDZ);
+        } else {
+            for (auto &B : blk_) k_copy<N>((long long)B.n * B.n, B.Rm, B.W1, st_);
+        }
+        multi_inner(&Blk::W1, g_);
+        k_axpby<N>(m_, R(-1).v, g_, R(1).v, p_, g_, st_);  // g = -g + p
+    }
+
+    // Newton::compute_bMat_dense_SDP, sdpa_newton.cpp:1007-1096 (via Make_bMat :1251-1272)
+    void Make_bMat() {
+        SDPG_CUDA(cudaMemsetAsync(B_, 0, (size_t)m_ * m_ * sizeof(V), st_));
+        for (auto &B : blk_) {
+            k_schur_f3<N>(B.cons, B.X, B.Zinv, B_, m_, st_);
+            if (B.nF1 == 0) continue;
+            const int n = B.n;
+            const long long nn = (long long)n * n;
+            const int chunk = f1_chunk(B);
+            for (int c0 = 0; c0 < B.nF1; c0 += chunk) {
+                const int cnt = std::min(chunk, B.nF1 - c0);
+                const size_t mark = ws_.used;
+                V *Ad = (V *)ws_.carve((size_t)cnt * nn * sizeof(V));
+                V *T = (V *)ws_.carve((size_t)cnt * nn * sizeof(V));
+                const int *owners = B.f1_owners + c0;
+                k_densify<N>(B.cons, owners, cnt, Ad, st_);
+                // T_t = A_t Zinv ; G_t = X T_t   (F1: work1 = A_i*invZ, work2 = X*work1)
+                GemmProblem<N> p{};
+                p.M = n;
+                p.Nn = n;
+                p.K = n;
+                p.batch = cnt;
+                p.A = operand_A<N>('N', Ad, n, nn);
+                p.B = operand_B<N>('N', B.Zinv, n, 0);
+                p.C = T;
+                p.ldc = n;
+                p.sc = nn;
+                p.alpha = R(1).v;
+                p.beta = R(0).v;
+                gemm(p);
+                p.A = operand_A<N>('N', B.X, n, 0);
+                p.B = operand_B<N>('N', T, n, nn);
+                p.C = Ad;  // G overwrites the densified constraints
+                gemm(p);
+                V *G = Ad;
+                k_schur_f1_sparse<N>(B.cons, owners, cnt, G, B_, m_, st_);
+                const int nd = B.cons.ndense;
+                if (nd > 0) {
+                    V *P = (V *)ws_.carve((size_t)cnt * nd * sizeof(V));
+                    if ((long long)cnt * nd >= 1024) {
+                        GemmProblem<N> q{};
+                        q.M = cnt;
+                        q.Nn = nd;
+                        q.K = (int)nn;
+                        q.batch = 1;
+                        q.A = operand_A<N>('T', G, nn, 0);
+                        q.B = operand_B<N>('N', B.cons.dense, nn, 0);
+                        q.C = P;
+                        q.ldc = cnt;
+                        q.sc = 0;
+                        q.alpha = R(1).v;
+                        q.beta = R(0).v;
+                        gemm(q);
+                    } else {
+                        std::vector<long long> xo((size_t)cnt * nd), yo((size_t)cnt * nd);
+                        for (int d = 0; d < nd; ++d)
+                            for (int t = 0; t < cnt; ++t) {
+                                xo[t + (size_t)cnt * d] = (long long)t * nn;
+                                yo[t + (size_t)cnt * d] = (long long)d * nn;
+                            }
+                        long long *dxo = (long long *)ws_.carve(xo.size() * sizeof(long long));
+                        long long *dyo = (long long *)ws_.carve(yo.size() * sizeof(long long));
+                        SDPG_CUDA(cudaMemcpyAsync(dxo, xo.data(), xo.size() * 8, cudaMemcpyHostToDevice, st_));
+                        SDPG_CUDA(cudaMemcpyAsync(dyo, yo.data(), yo.size() * 8, cudaMemcpyHostToDevice, st_));
+                        k_dot_batched<N>(nn, G, dxo, B.cons.dense, dyo, cnt * nd, P, ws_, st_);
+                        SDPG_CUDA(cudaStreamSynchronize(st_));  // host offset arrays go out of scope
+                    }
+                    k_schur_f1_dense_scatter<N>(B.cons, owners, cnt, P, B_, m_, st_);
+                }
+                ws_.used = mark;
+            }
+        }
+    }
+
+    // Newton::compute_DyVec, sdpa_newton.cpp:1308-1344 (Lal::choleskyFactorWithAdjust + solveSystems)
+    bool compute_DyVec(bool corrector) {
+        if (!corrector) {
+            ml_potrf<N>(m_, B_, m_, info_, ws_, st_);
+            int info = 0;
+            SDPG_CUDA(cudaMemcpyAsync(&info, info_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+            SDPG_CUDA(cudaStreamSynchronize(st_));
+            if (info != 0) return false;
+        }
+        k_copy<N>(m_, g_, Dy_, st_);
+        ml_potrs<N>(m_, B_, m_, Dy_, ws_, st_);
+        return true;
+    }
+
+    // Newton::compute_DzMat, sdpa_newton.cpp:1346-1356
+    void compute_DzMat() {
+        multi_plus(Dy_, &Blk::Dz);
+        if (phase_ == pFEAS || phase_ == noINFO) axpby_blocks(&Blk::Dz, R(-1), &Blk::Dz, R(1), &Blk::Dres);
+        else axpby_blocks(&Blk::Dz, R(-1), &Blk::Dz, R(0), nullptr);
+    }
+
+    // Newton::compute_DxMat, sdpa_newton.cpp:1358-1373
+    void compute_DxMat() {
+        for (auto &B : blk_) {
+            mm(B.n, B.W2, B.X, 'N', B.Dz, 'N');
+            mm(B.n, B.W1, B.W2, 'N', B.Zinv, 'N');
+        }
+        axpby_blocks(&Blk::Dx, R(1), &Blk::Rm, R(-1), &Blk::W1);
+        for (auto &B : blk_) k_symmetrize<N>(B.n, B.Dx, st_);
+    }
+
+    // Newton::Mehrotra, sdpa_newton.cpp:1375-1414
+    bool newton(int corrector) override {
+        ev_start();
+        Make_gVec(corrector);
+        tm_.rmat_gvec += ev_stop();
+        if (!corrector) {
+            ev_start();
+            Make_bMat();
+            tm_.schur += ev_stop();
+        }
+        ev_start();
+        const bool ok = compute_DyVec(corrector);
+        tm_.cholesky += ev_stop();
+        if (!ok) return false;
+        ev_start();
+        compute_DzMat();
+        compute_DxMat();
+        tm_.dxdz += ev_stop();
+        return true;
+    }
+
+    // ---------------------------------------------------------------- eigenvalues (sdpa_jordan.cpp, sdpa_linear.cpp)
+
+    // Lal::getMinEigen (Lanczos), sdpa_linear.cpp:27-124; L = invCholesky block, Xm = direction block
+    R lanczos_min(Blk &B, V *L, V *Xm) {
+        const int n = B.n;
+        R min(1.0e+51), min_old(1.0e+52), error(1.0e+10);
+        k_transpose<N>(n, L, B.Lt, st_);
+        // r = 1, q = 0
+        {
+            const V one = ml_one<N>();
+            std::vector<V> h(n, one);
+            SDPG_CUDA(cudaMemcpyAsync(B.r, h.data(), n * sizeof(V), cudaMemcpyHostToDevice, st_));
+            SDPG_CUDA(cudaMemsetAsync(B.q, 0, n * sizeof(V), st_));
+            SDPG_CUDA(cudaStreamSynchronize(st_));
+        }
+        R beta = rsqrt_(R(n));
+        const R sq_n = rsqrt_(R(n));
+        const R sq_n9 = rsqrt_(R(n) + R(9));
+        int k = 0, kk = 0;
+        while (k < n && R(k) < sq_n + R(10) && beta > R(1.0e-16) &&
+               (rabs(min - min_old) > R(1.0e-5) * rabs(min) + R(1.0e-8) ||
+                rabs(error * beta) > R(1.0e-2) * rabs(min) + R(1.0e-4))) {
+            if (k + 1 >= B.lanczos_kmax) break;
+            const R rb = R(1) / beta;  // value = MONE / beta
+            {
+                V *rbd = slot_ + 40;
+                SDPG_CUDA(cudaMemcpyAsync(rbd, &rb.v, sizeof(V), cudaMemcpyHostToDevice, st_));
+                k_lanczos_next<N>(n, B.r, rbd, B.q, B.qold, st_);  // qold = q; q = r / beta
+            }
+            k_matvec<N>(n, L, 'T', 1, B.q, B.w, st_);       // w = L^T q
+            k_matvec<N>(n, Xm, 'T', 0, B.w, B.tmp, st_);    // tmp = X w (X symmetric)
+            k_matvec<N>(n, B.Lt, 'T', 2, B.tmp, B.w, st_);  // w = L tmp
+            {
+                const size_t mark = ws_.used;
+                k_dot<N>(n, B.q, B.w, B.td + k, ws_, st_);  // alpha = q . w -> diagVec[k]
+                ws_.used = mark;
+            }
+            {
+                V *bd = slot_ + 41;
+                SDPG_CUDA(cudaMemcpyAsync(bd, &beta.v, sizeof(V), cudaMemcpyHostToDevice, st_));
+                k_lanczos_update<N>(n, B.w, B.q, B.qold, B.td + k, bd, B.r, st_);
+            }
+            const bool eig = R(kk) >= rsqrt_(R(k)) || k == n - 1 || R(k) > sq_n9;
+            if (eig) {
+                kk = 0;
+                k_tridiag_min<N>(k + 1, B.td, B.te, slot_ + 42, status_, st_);
+            }
+            {
+                const size_t mark = ws_.used;
+                k_dot<N>(n, B.r, B.r, slot_ + 44, ws_, st_);  // value = r . r
+                ws_.used = mark;
+            }
+            std::vector<V> h(5);
+            SDPG_CUDA(cudaMemcpyAsync(h.data(), slot_ + 42, 3 * sizeof(V), cudaMemcpyDeviceToHost, st_));
+            SDPG_CUDA(cudaStreamSynchronize(st_));
+            if (eig) {
+                min_old = min;
+                min = R(h[0]);
+                error = R(h[1]);
+            }
+            beta = rsqrt_(R(h[2]));
+            SDPG_CUDA(cudaMemcpyAsync(B.te + k, &beta.v, sizeof(V), cudaMemcpyHostToDevice, st_));  // diagVec2[k]
+            SDPG_CUDA(cudaStreamSynchronize(st_));
+            ++k;
+            ++kk;
+        }
+        return min - rabs(error * beta);
+    }
+
+    // Lal::getMinEigenValue on L*X*L^T for blocks of size <= 20 (sdpa_jordan.cpp:63-68)
+    R small_min(Blk &B, V *L, V *Xm) {
+        const int n = B.n;
+        mm(n, B.W2, Xm, 'N', L, 'T');
+        mm(n, B.W1, L, 'N', B.W2, 'N');
+        k_tridiagonalize_small<N>(n, B.W1, B.td, B.te, st_);
+        k_tridiag_min<N>(n, B.td, B.te, slot_ + 42, status_, st_);
+        return fetch1(slot_ + 42);
+    }
+
+    // Jal::getMinEigen(lMat, xMat), sdpa_jordan.cpp:55-88
+    R getMinEigen(V *Blk::*L, V *Blk::*Xm) {
+        R mn(1.0E50);
+        for (auto &B : blk_) {
+            const R v = (B.n > 20) ? lanczos_min(B, B.*L, B.*Xm) : small_min(B, B.*L, B.*Xm);
+            if (v < mn) mn = v;
+        }
+        return mn;
+    }
+
+    // ---------------------------------------------------------------- step length (sdpa_parts.cpp)
+
+    // StepLength::computeStepLength, sdpa_parts.cpp:298-360
+    void computeStepLength() {
+        const R alphaBD(100.0);
+        const R minX = getMinEigen(&Blk::LX, &Blk::Dx);
+        if (-minX > R(1.0) / alphaBD) aP_ = -R(1.0) / minX;
+        else aP_ = alphaBD;
+        const R minZ = getMinEigen(&Blk::LZ, &Blk::Dz);
+        if (-minZ > R(1.0) / alphaBD) aD_ = -R(1.0) / minZ;
+        else aD_ = alphaBD;
+    }
+
+    // StepLength::MehrotraPredictor (:362-410) / MehrotraCorrector (:412-523)
+    void step_length(int corrector) override {
+        ev_start();
+        if (!corrector) {
+            aP_ = aD_ = R(0.9);
+        } else {
+            computeStepLength();
+            aP_ = R(par_.gammaStar) * aP_;
+            aD_ = R(par_.gammaStar) * aD_;
+        }
+        if (phase_ == noINFO || phase_ == dFEAS) {
+            if (aP_ > R(1.0)) aP_ = R(1.0);
+        } else {
+            const R incPrimalObj = ip_blocks(&Blk::C, &Blk::Dx);
+            if (incPrimalObj > R(0.0)) {
+                if (aP_ > aD_) aP_ = aD_;
+                if (aP_ > R(1.0)) aP_ = R(1.0);
+            }
+        }
+        if (phase_ == noINFO || phase_ == pFEAS) {
+            if (aD_ > R(1.0)) aD_ = R(1.0);
+        } else {
+            const R incDualObj = ip_vec(b_, Dy_);
+            if (incDualObj < R(0.0)) {
+                if (aD_ > aP_) aD_ = aP_;
+                if (aD_ > R(1.0)) aD_ = R(1.0);
+            }
+        }
+        if (corrector) {
+            const R xi(3.0);
+            if (reductionOn_ && (phase_ == noINFO || phase_ == pFEAS || phase_ == dFEAS)) {
+                const R xMatvMat = ip_blocks(&Blk::X, &Blk::Dz);
+                const R uMatzMat = ip_blocks(&Blk::Dx, &Blk::Z);
+                const R uMatvMat = ip_blocks(&Blk::Dx, &Blk::Dz);
+                R thetaMax = rmax((R(1.0) - aP_) * thP_, (R(1.0) - aD_) * thD_);
+                R muNew = muCur_ + (aP_ * uMatzMat + aD_ * xMatvMat + aP_ * aD_ * uMatvMat) / R(nDim_);
+                while (thetaMax * thetaMax * muInit_ > xi * muNew) {
+                    const R alphaMax = R(0.95) * rmax(aP_, aD_);
+                    aP_ = rmin(aP_, alphaMax);
+                    aD_ = rmin(aD_, alphaMax);
+                    thetaMax = rmax((R(1.0) - aP_) * thP_, (R(1.0) - aD_) * thD_);
+                    muNew = muCur_ + (aP_ * uMatzMat + aD_ * xMatvMat + aP_ * aD_ * uMatvMat) / R(nDim_);
+                    if (aP_ < R(1.0e-6) && aD_ < R(1.0e-6)) break;
+                }
+            }
+            if (phase_ == pdFEAS) {
+                const R objValDual = ip_vec(b_, y_);
+                const R objValPrimal = ip_blocks(&Blk::C, &Blk::X);
+                R incDualObj = ip_vec(b_, Dy_);
+                incDualObj *= aD_;
+                R incPrimalObj = ip_blocks(&Blk::C, &Blk::Dx);
+                incPrimalObj *= aP_;
+                const R maxRatio = (objValDual - objValPrimal) / (incPrimalObj - incDualObj);
+                if (maxRatio > R(0.0) && maxRatio < R(1.0)) {
+                    aP_ *= maxRatio;
+                    aD_ *= maxRatio;
+                }
+            }
+        }
+        tm_.steplen += ev_stop();
+    }
+
+    // DirectionParameter::MehrotraPredictor (:543-553) and Switch::MehrotraPredictor (:605-612)
+    void direction_predictor() {
+        reductionOn_ = (phase_ == noINFO || phase_ == pFEAS || phase_ == dFEAS) ? 1 : 0;
+        const R nu(2.0);
+        if (phase_ == pdFEAS) betaV_ = R(0.0);
+        else {
+            betaV_ = R(par_.betaBar);
+            if (!reductionOn_) betaV_ = nu;
+        }
+    }
+
+    // DirectionParameter::MehrotraCorrector, sdpa_parts.cpp:555-586
+    void direction_corrector() {
+        const R xMatvMat = ip_blocks(&Blk::X, &Blk::Dz);
+        const R uMatzMat = ip_blocks(&Blk::Dx, &Blk::Z);
+        const R uMatvMat = ip_blocks(&Blk::Dx, &Blk::Dz);
+        const R muTarget = muCur_ + (aP_ * uMatzMat + aD_ * xMatvMat + aP_ * aD_ * uMatvMat) / R(nDim_);
+        betaV_ = muTarget / muCur_;
+        if (betaV_ < R(1.0)) betaV_ = betaV_ * betaV_;
+        if (phase_ == pdFEAS) {
+            if (betaV_ < R(par_.betaStar)) betaV_ = R(par_.betaStar);
+            if (betaV_ > R(1.0)) betaV_ = R(1.0);
+        } else {
+            if (betaV_ < R(par_.betaBar)) betaV_ = R(par_.betaBar);
+        }
+    }
+
+    // ---------------------------------------------------------------- iterate update (sdpa_dataset.cpp)
+
+    // Jal::getInvChol / getInvCholAndInv (sdpa_jordan.cpp:123-171) for one block
+    bool inv_chol(Blk &B, V *A, V *Linv, V *Inv) {
+        const int n = B.n;
+        k_copy<N>((long long)n * n, A, B.F, st_);
+        ml_potrf<N>(n, B.F, n, info_, ws_, st_);
+        int info = 0;
+        SDPG_CUDA(cudaMemcpyAsync(&info, info_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+        SDPG_CUDA(cudaStreamSynchronize(st_));
+        if (info != 0) return false;
+        k_zero_strict_upper<N>(n, B.F, st_);
+        ml_trtri_lower<N>(n, B.F, n, Linv, ws_, st_);
+        if (Inv) mm(n, Inv, Linv, 'T', Linv, 'N');  // Rtrmm: Inv = Linv^T * Linv
+        return true;
+    }
+
+    // Solutions::computeInverse, sdpa_dataset.cpp:96-118
+    bool computeInverse() {
+        bool ok = true;
+        for (auto &B : blk_)
+            if (!inv_chol(B, B.X, B.LX, nullptr)) ok = false;
+        for (auto &B : blk_)
+            if (!inv_chol(B, B.Z, B.LZ, B.Zinv)) ok = false;
+        return ok;
+    }
+
+    // Solutions::update, sdpa_dataset.cpp:120-143
+    bool update() override {
+        ev_start();
+        axpby_blocks(&Blk::X, R(1), &Blk::X, aP_, &Blk::Dx);
+        k_axpby<N>(m_, R(1).v, y_, aD_.v, Dy_, y_, st_);
+        axpby_blocks(&Blk::Z, R(1), &Blk::Z, aD_, &Blk::Dz);
+        const R cannot_move(1.0e-4);
+        if (aP_ < cannot_move && aD_ < cannot_move) {
+            tm_.update += ev_stop();
+            return false;
+        }
+        const bool ok = computeInverse();
+        tm_.update += ev_stop();
+        return ok;
+    }
+
+    // ---------------------------------------------------------------- residuals and control
+
+    // Residuals::compute, sdpa_dataset.cpp:625-646
+    void residuals() override {
+        ev_start();
+        multi_inner(&Blk::X, p_);
+        k_axpby<N>(m_, R(-1).v, p_, R(1).v, b_, p_, st_);
+        multi_plus(y_, &Blk::Dres);
+        axpby_blocks(&Blk::Dres, R(-1), &Blk::Dres, R(1), &Blk::C);
+        axpby_blocks(&Blk::Dres, R(1), &Blk::Dres, R(-1), &Blk::Z);
+        {
+            const size_t mark = ws_.used;
+            k_maxabs<N>(m_, p_, slot_, ws_, st_);
+            for (size_t l = 0; l < blk_.size(); ++l)
+                k_maxabs<N>((long long)blk_[l].n * blk_[l].n, blk_[l].Dres, slot_ + 1 + l, ws_, st_);
+            ws_.used = mark;
+        }
+        auto v = fetch(1 + (int)blk_.size());
+        normP_ = v[0];
+        normD_ = R(0.0);
+        for (size_t l = 0; l < blk_.size(); ++l)
+            if (v[1 + l] > normD_) normD_ = v[1 + l];
+        tm_.residual += ev_stop();
+    }
+
+    // Phase::updateCheck, sdpa_parts.cpp:932-1011 (REVERSE_PRIMAL_DUAL bounds)
+    bool phase_updateCheck() {
+        const R NONZERO(1.0e-6);
+        const R accuracy(par_.epsilonDash);
+        phase_ = noINFO;
+        if (normP_ <= accuracy) phase_ = (normD_ <= accuracy) ? pdFEAS : pFEAS;
+        if (phase_ == noINFO && normD_ <= accuracy) phase_ = dFEAS;
+        if (phase_ == pdFEAS) {
+            const R mean = (rabs(objP_) + rabs(objD_)) / R(2.0);
+            const R PDgap = rabs(objP_ - objD_);
+            const R dominator = (mean < R(1.0)) ? R(1.0) : mean;
+            if (PDgap / dominator <= R(par_.epsilonStar)) {
+                phase_ = pdOPT;
+                return false;
+            }
+        }
+        if (phase_ == noINFO && rho_ > R(1.0) + NONZERO) {
+            phase_ = pdINF;
+            return false;
+        }
+        if (phase_ == pFEAS) {
+            if (objP_ <= -R(par_.upperBound)) {
+                phase_ = pUNBD;
+                return false;
+            }
+            if (rho_ > R(1.0) + NONZERO) {
+                phase_ = pFEAS_dINF;
+                return false;
+            }
+        }
+        if (phase_ == dFEAS) {
+            if (objD_ >= -R(par_.lowerBound)) {
+                phase_ = dUNBD;
+                return false;
+            }
+            if (rho_ > R(1.0) + NONZERO) {
+                phase_ = pINF_dFEAS;
+                return false;
+            }
+        }
+        return true;
+    }
+
+    // SolveInfo::update(lambda, ...), sdpa_parts.cpp:798-860
+    void solveInfo_update() {
+        objP_ = ip_blocks(&Blk::C, &Blk::X);
+        objD_ = ip_vec(b_, y_);
+        const R primal = thP_, dual = thD_, omega(par_.omegaStar);
+        rho_ = R(0.0);
+        const R x0z0 = R(nDim_) * muInit_;
+        const R xMatzMat = R(nDim_) * muCur_;
+        R x0zMat(0.0), xMatz0(0.0);
+        const R lambda(par_.lambdaStar);
+        for (size_t l = 0; l < blk_.size(); ++l) {
+            k_trace<N>(blk_[l].n, blk_[l].Z, slot_ + 2 * l, st_);
+            k_trace<N>(blk_[l].n, blk_[l].X, slot_ + 2 * l + 1, st_);
+        }
+        auto tr = fetch(2 * (int)blk_.size());
+        // the reference accumulates lambda * Z_ii element by element; the sum of the
+        // traces times lambda agrees to the working precision
+        for (size_t l = 0; l < blk_.size(); ++l) {
+            x0zMat += lambda * tr[2 * l];
+            xMatz0 += lambda * tr[2 * l + 1];
+        }
+        const R accuracy(par_.epsilonDash);
+        if (normP_ <= accuracy && xMatz0 < etaP_) etaP_ = xMatz0;
+        if (normD_ <= accuracy && x0zMat < etaD_) etaD_ = x0zMat;
+        if (normP_ > accuracy && normD_ <= accuracy)
+            rho_ = primal * x0zMat / ((primal + (R(1.0) - primal) * omega) * etaD_ + xMatzMat);
+        if (normP_ <= accuracy && normD_ > accuracy)
+            rho_ = dual * xMatz0 / ((dual + (R(1.0) - dual) * omega) * etaP_ + xMatzMat);
+        if (normP_ > accuracy && normD_ > accuracy)
+            rho_ = (dual * xMatz0 + primal * x0zMat) /
+                   ((primal * dual + omega * (primal * (R(1.0) - dual) + (R(1.0) - primal) * dual)) * x0z0 + xMatzMat);
+    }
+
+    // Solutions::initialize (sdpa_dataset.cpp:35-60) and the set-up part of pinpal (sdpa_main.cpp:229-287)
+    void initialize() override {
+        const R lambda(par_.lambdaStar);
+        const R invsq = R(1.0) / rsqrt_(lambda);
+        const R inv = R(1.0) / lambda;
+        for (auto &B : blk_) {
+            k_set_identity<N>(B.n, B.X, lambda.v, st_);
+            k_set_identity<N>(B.n, B.Z, lambda.v, st_);
+            k_set_identity<N>(B.n, B.LX, invsq.v, st_);
+            k_set_identity<N>(B.n, B.LZ, invsq.v, st_);
+            k_set_identity<N>(B.n, B.Zinv, inv.v, st_);
+        }
+        SDPG_CUDA(cudaMemsetAsync(y_, 0, m_ * sizeof(V), st_));
+        residuals();
+        initNormP_ = normP_;
+        initNormD_ = normD_;
+        aP_ = aD_ = R(0.0);
+        betaV_ = R(par_.betaStar);
+        reductionOn_ = 1;
+        muInit_ = lambda * lambda;
+        muCur_ = muInit_;
+        const R accuracy(par_.epsilonDash);
+        thP_ = (initNormP_ < accuracy) ? R(0.0) : R(1.0);
+        thD_ = (initNormD_ < accuracy) ? R(0.0) : R(1.0);
+        rho_ = R(1.0);
+        etaP_ = R(par_.omegaStar) * R(nDim_) * muInit_;
+        etaD_ = etaP_;
+        objP_ = ip_blocks(&Blk::C, &Blk::X);
+        objD_ = ip_vec(b_, y_);
+        phase_updateCheck();
+        iter_ = 0;
+        hist_.clear();
+        initialized_ = true;
+    }
+
+    void record_iteration() {
+        IterRecord r;
+        r.it = iter_;
+        r.mu = muCur_.d();
+        r.thetaP = thD_.d();  // printed with REVERSE_PRIMAL_DUAL (sdpa_io.cpp:764-796)
+        r.thetaD = thP_.d();
+        r.objP = (-objD_).d();
+        r.objD = (-objP_).d();
+        r.alphaP = aD_.d();
+        r.alphaD = aP_.d();
+        r.beta = betaV_.d();
+        hist_.push_back(r);
+    }
+
+    // IO::printOneIteration (REVERSE_PRIMAL_DUAL branch), sdpa_io.cpp:764-796
+    void print_iteration(FILE *f) {
+        if (!f) return;
+        fprintf(f, "%2d %s %s %s %s %s %s %s %s\n", iter_, muCur_.fmt(1).c_str(), thD_.fmt(1).c_str(),
+                thP_.fmt(1).c_str(), (-objD_).fmt(2, true).c_str(), (-objP_).fmt(2, true).c_str(),
+                aD_.fmt(1).c_str(), aP_.fmt(1).c_str(), betaV_.fmt(2).c_str());
+        fflush(f);
+    }
+
+    void trace_line() {
+        if (!trace_) return;
+        fprintf(trace_, "it=%d mu=%s objP=%s objD=%s aP=%s aD=%s beta=%s\n", iter_, muCur_.fmt(30).c_str(),
+                objP_.fmt(30).c_str(), objD_.fmt(30).c_str(), aP_.fmt(30).c_str(), aD_.fmt(30).c_str(),
+                betaV_.fmt(30).c_str());
+        fflush(trace_);
+    }
+
+    // pinpal's main loop, sdpa_main.cpp:294-385
+    int run(FILE *out, FILE *display) override {
+        auto t0 = std::chrono::steady_clock::now();
+        if (!initialized_) initialize();
+        const char *hdr = "   mu      thetaP  thetaD  objP      objD      alphaP  alphaD  beta \n";
+        if (out) fputs(hdr, out);
+        if (display) fputs(hdr, display);
+        while (phase_updateCheck() && iter_ < par_.maxIteration) {
+            direction_predictor();
+            if (!newton(0)) break;
+            step_length(0);
+            direction_corrector();
+            if (phase_ == pdFEAS && (betaV_ > R(5) || objP_ < objD_)) break;
+            newton(1);
+            step_length(1);
+            record_iteration();
+            print_iteration(out);
+            print_iteration(display);
+            trace_line();
+            if (!update()) {
+                if (display) fprintf(display, "cannot move\n");
+                break;
+            }
+            // RatioInitResCurrentRes::update (:692-698)
+            if (reductionOn_) {
+                thP_ = rabs((R(1.0) - aP_) * thP_);
+                thD_ = rabs((R(1.0) - aD_) * thD_);
+            }
+            // AverageComplementarity::update (:647-651)
+            muCur_ = ip_blocks(&Blk::X, &Blk::Z) / R(nDim_);
+            residuals();
+            // RatioInitResCurrentRes::update_exact (:700-708)
+            thP_ = (initNormP_ > R(1.0e-10)) ? normP_ / initNormP_ : R(0.0);
+            thD_ = (initNormD_ > R(1.0e-10)) ? normD_ / initNormD_ : R(0.0);
+            solveInfo_update();
+            ++iter_;
+        }
+        residuals();
+        final_phase_ = reverse_phase(phase_);
+        tm_.total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        print_last(out);
+        print_last(display);
+        return iter_;
+    }
+
+    static int reverse_phase(int ph) {
+        switch (ph) {
+            case pFEAS: return dFEAS;
+            case dFEAS: return pFEAS;
+            case pFEAS_dINF: return pINF_dFEAS;
+            case pINF_dFEAS: return pFEAS_dINF;
+            case pUNBD: return dUNBD;
+            case dUNBD: return pUNBD;
+        }
+        return ph;
+    }
+
+    // values of IO::printLastInfo (sdpa_io.cpp:996-1184), REVERSE_PRIMAL_DUAL branch
+    R relgap() const {
+        const R mean = (rabs(objP_) + rabs(objD_)) / R(2.0);
+        const R PDgap = rabs(objP_ - objD_);
+        return (mean < R(1.0)) ? PDgap : PDgap / mean;
+    }
+    R digits() const {
+        const R mean = (rabs(objP_) + rabs(objD_)) / R(2.0);
+        const R PDgap = rabs(objP_ - objD_);
+        if (PDgap == R(0.0) || mean == R(0.0)) return R(0.0);
+        return R(-log10(fabs((PDgap / mean).d())));
+    }
+
+    void print_last(FILE *f) {
+        if (!f) return;
+        print_iteration(f);
+        fprintf(f, "\nphase.value = %s\n", phase_name(final_phase_));
+        fprintf(f, "   Iteration = %d\n", iter_);
+        fprintf(f, "          mu = %s\n", muCur_.fmt(16).c_str());
+        fprintf(f, "relative gap = %s\n", relgap().fmt(16).c_str());
+        fprintf(f, "         gap = %s\n", (muCur_ * R(nDim_)).fmt(16).c_str());
+        fprintf(f, "      digits = %s\n", digits().fmt(16).c_str());
+        fprintf(f, "objValPrimal = %s\n", (-objD_).fmt(16).c_str());
+        fprintf(f, "objValDual   = %s\n", (-objP_).fmt(16).c_str());
+        fprintf(f, "p.feas.error = %s\n", normD_.fmt(16).c_str());
+        fprintf(f, "d.feas.error = %s\n", normP_.fmt(16).c_str());
+        fprintf(f, "relative eps = %s\n", R(ml_ldexp(ml_one<N>(), -32 * N)).fmt(16).c_str());
+        fprintf(f, "total time   = %.3f\n", tm_.total / 1000.0);
+        fflush(f);
+    }
+
+    // info: [phase, iteration, objValPrimal, objValDual, mu, relgap, p.feas.error, d.feas.error,
+    //        alphaP, alphaD, beta, digits] as printed by the reference (primal/dual swapped back)
+    void info(double *o) const override {
+        o[0] = final_phase_;
+        o[1] = iter_;
+        o[2] = (-objD_).d();
+        o[3] = (-objP_).d();
+        o[4] = muCur_.d();
+        o[5] = relgap().d();
+        o[6] = normD_.d();
+        o[7] = normP_.d();
+        o[8] = aD_.d();
+        o[9] = aP_.d();
+        o[10] = betaV_.d();
+        o[11] = digits().d();
+    }
+    std::string info_text(int which, int digits_) const override {
+        switch (which) {
+            case 0: return (-objD_).fmt(digits_ - 1);
+            case 1: return (-objP_).fmt(digits_ - 1);
+            case 2: return muCur_.fmt(digits_ - 1);
+            case 3: return relgap().fmt(digits_ - 1);
+            case 4: return normD_.fmt(digits_ - 1);
+            case 5: return normP_.fmt(digits_ - 1);
+        }
+        return "";
+    }
+    // The reference prints xVec = -y (IO::printLastInfo, Vector::display with scalar -1).
+    void get_y(void *out, int form) const override {
+        std::vector<V> h(m_);
+        SDPG_CUDA(cudaMemcpy(h.data(), y_, m_ * sizeof(V), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < m_; ++i) {
+            if (form == 0) ((double *)out)[i] = ml_to_double(ml_neg(h[i]));
+            else ((V *)out)[i] = ml_neg(h[i]);
+        }
+    }
+    void get_block(int which, int l, void *out, int form) const override {
+        const Blk &B = blk_.at(l);
+        const size_t nn = (size_t)B.n * B.n;
+        std::vector<V> h(nn);
+        const V *srcs[] = {B.X, B.Z, B.Dx, B.Dz, B.Zinv, B.LX, B.LZ, B.C, B.Dres};
+        if (which < 0 || which > 8) throw sdpg_error(SDPG_ERR_ARG, "bad matrix selector");
+        const V *src = srcs[which];
+        SDPG_CUDA(cudaMemcpy(h.data(), src, nn * sizeof(V), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < nn; ++i) {
+            if (form == 0) ((double *)out)[i] = ml_to_double(h[i]);
+            else ((V *)out)[i] = h[i];
+        }
+    }
+
+    void make_bmat(void *out) override {
+        Make_bMat();
+        SDPG_CUDA(cudaMemcpyAsync(out, B_, (size_t)m_ * m_ * sizeof(V), cudaMemcpyDeviceToHost, st_));
+        SDPG_CUDA(cudaStreamSynchronize(st_));
+    }
+    void make_gvec(int corrector, void *out) override {
+        Make_gVec(corrector != 0);
+        SDPG_CUDA(cudaMemcpyAsync(out, g_, m_ * sizeof(V), cudaMemcpyDeviceToHost, st_));
+        SDPG_CUDA(cudaStreamSynchronize(st_));
+    }
+    void min_eigen(int side, void *out) override {
+        const R v = side == 0 ? getMinEigen(&Blk::LX, &Blk::Dx) : getMinEigen(&Blk::LZ, &Blk::Dz);
+        memcpy(out, &v.v, sizeof(V));
+    }
+    void get_vec(int which, void *out) const override {
+        const V *srcs[] = {y_, Dy_, b_, p_};
+        if (which < 0 || which > 3) throw sdpg_error(SDPG_ERR_ARG, "bad vector selector");
+        SDPG_CUDA(cudaMemcpy(out, srcs[which], m_ * sizeof(V), cudaMemcpyDeviceToHost));
+    }
+
+    // ---------------------------------------------------------------- timing
+
+    void ev_start() { SDPG_CUDA(cudaEventRecord(ev_[0], st_)); }
+    double ev_stop() {
+        SDPG_CUDA(cudaEventRecord(ev_[1], st_));
+        SDPG_CUDA(cudaEventSynchronize(ev_[1]));
+        float ms = 0;
+        SDPG_CUDA(cudaEventElapsedTime(&ms, ev_[0], ev_[1]));
+        return ms;
+    }
+
+  private:
+    Param par_;
+    cudaStream_t st_;
+    Workspace ws_;
+    std::vector<Blk> blk_;
+    int m_ = 0, nDim_ = 0;
+    std::vector<V> b_h_;
+    V *b_ = nullptr, *y_ = nullptr, *Dy_ = nullptr, *g_ = nullptr, *p_ = nullptr, *B_ = nullptr, *slot_ = nullptr;
+    int *info_ = nullptr, *status_ = nullptr;
+    R muInit_, muCur_, thP_, thD_, aP_, aD_, betaV_, rho_, etaP_, etaD_, objP_, objD_, normP_, normD_;
+    R initNormP_, initNormD_;
+    int phase_ = noINFO, final_phase_ = noINFO, reductionOn_ = 1, iter_ = 0;
+    bool initialized_ = false;
+    Timers tm_;
+    std::vector<IterRecord> hist_;
+    std::vector<cudaEvent_t> ev_;
+    FILE *trace_ = nullptr;
+    long long gemm_macs_ = 0;
+};
+
+}  // namespace
+
+SolverBase *make_solver(const RawProblem &P, const Param &param, int device, cudaStream_t stream) {
+    const int bits = param.precision;
+    if (bits <= 256) return new Solver<8>(P, param, device, stream);
+    if (bits <= 512) return new Solver<16>(P, param, device, stream);
+    throw sdpg_error(SDPG_ERR_ARG, "precision above 512 bits is not supported");
+}
+
+}  // namespace sdpg

@@ -1,0 +1,76 @@
+// The GPU-resident interior-point state and the Newton step (SDPA-GMP's
+// Newton / Jal / Lal hot path with its Solutions, Residuals and IPM control).
+#pragma once
+#include <stdio.h>
+
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "problem.h"
+#include "real.h"
+
+namespace sdpg {
+
+// Phase values (SolveInfo::phaseType, sdpa_parts.h).
+enum Phase {
+    noINFO = 0,
+    pFEAS,
+    dFEAS,
+    pdFEAS,
+    pdINF,
+    pFEAS_dINF,
+    pINF_dFEAS,
+    pdOPT,
+    pUNBD,
+    dUNBD
+};
+const char *phase_name(int phase);
+
+// Per-phase wall-clock accounting (ComputeTime, sdpa_parts.h:46-83), milliseconds.
+struct Timers {
+    double schur = 0, cholesky = 0, rmat_gvec = 0, dxdz = 0, steplen = 0, update = 0, residual = 0, total = 0;
+};
+
+struct IterRecord {
+    int it;
+    double mu, thetaP, thetaD, objP, objD, alphaP, alphaD, beta;
+};
+
+// Type-erased solver interface used by the C ABI.
+class SolverBase {
+  public:
+    virtual ~SolverBase() {}
+    virtual int limbs() const = 0;
+    virtual void initialize() = 0;                          // Solutions::initialize + residuals
+    virtual int run(FILE *out, FILE *display) = 0;          // pinpal main loop; returns iterations
+    virtual bool newton(int corrector) = 0;                 // Newton::Mehrotra
+    virtual void step_length(int corrector) = 0;            // StepLength::Mehrotra{Predictor,Corrector}
+    virtual bool update() = 0;                              // Solutions::update
+    virtual void residuals() = 0;                           // Residuals::compute
+    virtual int phase() const = 0;
+    virtual int iteration() const = 0;
+    virtual void info(double *out12) const = 0;             // see sdpg_solution_info
+    virtual std::string info_text(int which, int digits) const = 0;
+    virtual void get_y(void *out, int form) const = 0;      // form 0: double, 1: ml
+    // which: 0 X, 1 Z, 2 dX, 3 dZ, 4 Z^-1, 5 L_X^-1, 6 L_Z^-1, 7 C, 8 dual residual
+    virtual void get_block(int which, int block, void *out, int form) const = 0;
+    virtual void make_bmat(void *out_ml) = 0;               // Newton::Make_bMat at the current iterate
+    virtual void make_gvec(int corrector, void *out_ml) = 0;  // Newton::Make_gVec
+    virtual void min_eigen(int side, void *out_ml) = 0;     // Jal::getMinEigen(L_X^-1,dX) / (L_Z^-1,dZ)
+    virtual void get_vec(int which, void *out_ml) const = 0;  // 0 y, 1 dy, 2 b, 3 primal residual p
+    virtual const Timers &timers() const = 0;
+    virtual const std::vector<IterRecord> &history() const = 0;
+    virtual void set_trace(FILE *f) = 0;
+    virtual int m() const = 0;
+    virtual int nblocks() const = 0;
+    virtual int block_size(int l) const = 0;
+    virtual long long gemm_macs() const = 0;                // multi-limb MACs issued through the GEMM
+    virtual void reset_counters() = 0;
+    virtual void sync() = 0;
+};
+
+// Build a solver for the SDP blocks of P at the precision in `param`.
+SolverBase *make_solver(const RawProblem &P, const Param &param, int device, cudaStream_t stream);
+
+}  // namespace sdpg

@@ -1,0 +1,35 @@
+"""Helpers shared by the parity tests: load a golden fixture (the reference
+solver's own output, see tests/golden/make_golden.py) and write its input."""
+import hashlib
+import importlib
+import json
+import os
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    with open(os.path.join(GOLDEN, name + ".json")) as f:
+        return json.load(f)
+
+
+def write_inputs(name, directory):
+    """Write <name>.dat-s and <name>.param for a golden case; returns (dat, param, golden)."""
+    g = load(name)
+    if name == "example1":
+        return os.path.join(GOLDEN, "example1.dat-s"), os.path.join(GOLDEN, "example1.param"), g
+    problems = importlib.import_module("sdpa-gmp_gb300.problems")
+    kw = {k: (tuple(v) if isinstance(v, list) else v) for k, v in g["kwargs"].items()}
+    text = getattr(problems, g["generator"])(**kw).text()
+    assert hashlib.sha256(text.encode()).hexdigest() == g["sha256"], "generator drifted from the golden input"
+    dat = os.path.join(directory, name + ".dat-s")
+    par = os.path.join(directory, name + ".param")
+    with open(dat, "w") as f:
+        f.write(text)
+    with open(par, "w") as f:
+        f.write(problems.param_text(precision=g["precision"]))
+    return dat, par, g
+
+
+def fnum(s):
+    return float(s)

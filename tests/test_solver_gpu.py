@@ -1,0 +1,94 @@
+"""Whole-solve parity with the reference solver (sdpa_gmp, run in the
+container that generated tests/golden/) on the same inputs and precision.
+
+Checked per case:
+  * final phase and iteration count identical;
+  * objValPrimal / objValDual equal to the printed 17 significant digits
+    (relative 1e-15);
+  * the printed solution vector xVec (40 digits) within 1e-20 relative to
+    max(1, |x|) -- the IPM stops at relative gap 1e-30, and late iterates of
+    two correctly rounded implementations differ well above 2^-(p-16);
+  * every row of the iteration table (mu, objP, objD, alphaP, alphaD, beta as
+    printed with 2-3 digits) within 2 units of the last printed digit.
+"""
+import math
+import os
+
+import pytest
+
+from golden_cases import write_inputs
+
+pytestmark = pytest.mark.gpu
+
+SMALL = ["example1", "maxcut20", "maxcut40", "maxcut40pm", "control20", "control30", "maxcut40_p512",
+         "gpp40"]
+LARGE = ["gpp60", "maxcut100", "maxcut124pm", "control231"]
+
+
+def close_printed(a: float, b_str: str, digits: int) -> bool:
+    b = float(b_str)
+    if b == 0.0:
+        return abs(a) < 1e-300 or a == 0.0
+    if abs(b) < 1e-60:  # residual ratios at rounding-noise level differ by construction
+        return abs(a) < 1e-55
+    ulp = 10.0 ** (math.floor(math.log10(abs(b))) - digits)
+    return abs(a - b) <= 2.0 * ulp + 1e-12 * abs(b)
+
+
+def run_case(sdpg, name, tmp_path):
+    dat, par, g = write_inputs(name, str(tmp_path))
+    prob = sdpg.Problem.read(dat)
+    solver = sdpg.Solver(prob, sdpg.Param.read(par))
+    out = str(tmp_path / (name + ".out"))
+    solver.run(out)
+    return solver, g
+
+
+def check_case(sdpg, name, tmp_path):
+    solver, g = run_case(sdpg, name, tmp_path)
+    info = solver.info()
+    assert info["phase"] == g["phase"], (info["phase"], g["phase"])
+    assert info["iteration"] == g["iteration"], (info["iteration"], g["iteration"])
+    for key in ("objValPrimal", "objValDual"):
+        ref = float(g[key])
+        assert abs(info[key] - ref) <= 1e-15 * max(1.0, abs(ref)), (key, info[key], ref)
+    # iteration table
+    hist = solver.history()
+    table = g["iterations_table"]
+    assert len(hist) == len(table) - 1 or len(hist) == len(table)
+    for row, ref in zip(hist, table):
+        it, mu, thp, thd, objp, objd, ap, ad, beta = row
+        assert int(it) == int(ref[0])
+        assert close_printed(mu, ref[1], 1), ("mu", int(it), mu, ref[1])
+        assert close_printed(objp, ref[4], 2), ("objP", int(it), objp, ref[4])
+        assert close_printed(objd, ref[5], 2), ("objD", int(it), objd, ref[5])
+        # a step length is compared unless both sides took a full step (>= 0.95): when a
+        # direction is at rounding-noise level (a feasible side whose residual is zero)
+        # its eigenvalue test flips between the 0.9*100 cap and ~1 on rounding alone
+        for key, got, refv in (("alphaP", ap, ref[6]), ("alphaD", ad, ref[7])):
+            if got >= 0.95 and float(refv) >= 0.95:
+                continue
+            assert close_printed(got, refv, 1), (key, int(it), got, refv)
+        assert close_printed(beta, ref[8], 2), ("beta", int(it), beta, ref[8])
+    # xVec to 40 digits (compare as exact decimals through the ml format)
+    if "xVec" in g:
+        x = sdpg.ml_format(solver.xvec(ml=True), 45)
+        worst = 0.0
+        for got, ref in zip(x, g["xVec"]):
+            from decimal import Decimal, getcontext
+            getcontext().prec = 80
+            d = abs(Decimal(got) - Decimal(ref))
+            scale = max(Decimal(1), abs(Decimal(ref)))
+            worst = max(worst, float(d / scale))
+        assert worst <= 1e-20, worst
+    return solver
+
+
+@pytest.mark.parametrize("name", SMALL)
+def test_small_cases_match_reference(sdpg, name, tmp_path):
+    check_case(sdpg, name, tmp_path)
+
+
+@pytest.mark.parametrize("name", LARGE)
+def test_config_shapes_match_reference(sdpg, name, tmp_path):
+    check_case(sdpg, name, tmp_path)
