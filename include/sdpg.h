@@ -141,6 +141,10 @@ int sdpg_solver_initialize(sdpg_solver *h);
  * reference's iteration table and summary to out_path (may be NULL) and stdout
  * when asked; returns the iteration count. */
 int sdpg_solver_run(sdpg_solver *h, const char *out_path, int print_to_stdout);
+/* One pass of the main-loop body (predictor, step, corrector, step, update, residuals,
+ * sdpa_main.cpp:294-384): returns 1 when an iteration was made, 0 once the loop has
+ * stopped (phase decided, iteration limit, Schur Cholesky failure, or cannot move). */
+int sdpg_solver_iterate(sdpg_solver *h);
 /* Newton::Mehrotra (sdpa_newton.cpp:1375-1414); direction 0 predictor, 1 corrector.
  * Returns SDPG_ERR_NOT_PD when the Schur Cholesky fails (the reference's FAILURE). */
 int sdpg_newton(sdpg_solver *h, int direction);

@@ -87,6 +87,7 @@ def _setup(lib: ctypes.CDLL) -> ctypes.CDLL:
         "sdpg_solver_dims": (i, [vp, c.POINTER(i), c.POINTER(i), c.POINTER(i), i]),
         "sdpg_solver_initialize": (i, [vp]),
         "sdpg_solver_run": (i, [vp, c.c_char_p, i]),
+        "sdpg_solver_iterate": (i, [vp]),
         "sdpg_newton": (i, [vp, i]),
         "sdpg_step_length": (i, [vp, i]),
         "sdpg_update": (i, [vp]),
@@ -266,6 +267,10 @@ class Solver:
 
     def run(self, out_path: str | None = None, verbose: bool = False) -> int:
         return check(lib().sdpg_solver_run(self.h, out_path.encode() if out_path else None, 1 if verbose else 0))
+
+    def iterate(self) -> bool:
+        """One predictor-corrector iteration; False once the solve has stopped."""
+        return check(lib().sdpg_solver_iterate(self.h)) == 1
 
     def newton(self, direction: int) -> bool:
         rc = lib().sdpg_newton(self.h, direction)

@@ -240,6 +240,10 @@ int sdpg_solver_run(sdpg_solver *h, const char *out_path, int print_to_stdout) {
     });
 }
 
+int sdpg_solver_iterate(sdpg_solver *h) {
+    return sdpg_guard([&] { return S(h).iterate(nullptr); });
+}
+
 int sdpg_newton(sdpg_solver *h, int direction) {
     return sdpg_guard([&] { return S(h).newton(direction) ? (int)SDPG_OK : (int)SDPG_ERR_NOT_PD; });
 }

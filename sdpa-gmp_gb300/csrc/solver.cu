@@ -921,7 +921,10 @@ class Solver final : public SolverBase {
         phase_updateCheck();
         iter_ = 0;
         hist_.clear();
+        printed_.clear();
         initialized_ = true;
+        stopped_ = false;
+        cannot_move_ = false;
     }
 
     void record_iteration() {
@@ -939,11 +942,18 @@ class Solver final : public SolverBase {
     }
 
     // IO::printOneIteration (REVERSE_PRIMAL_DUAL branch), sdpa_io.cpp:764-796
+    std::string iteration_line() const {
+        char buf[512];
+        snprintf(buf, sizeof buf, "%2d %s %s %s %s %s %s %s %s\n", iter_, muCur_.fmt(1).c_str(), thD_.fmt(1).c_str(),
+                 thP_.fmt(1).c_str(), (-objD_).fmt(2, true).c_str(), (-objP_).fmt(2, true).c_str(),
+                 aD_.fmt(1).c_str(), aP_.fmt(1).c_str(), betaV_.fmt(2).c_str());
+        return buf;
+    }
     void print_iteration(FILE *f) {
+        const std::string line = iteration_line();
+        if (printed_.size() < hist_.size()) printed_.push_back(line);
         if (!f) return;
-        fprintf(f, "%2d %s %s %s %s %s %s %s %s\n", iter_, muCur_.fmt(1).c_str(), thD_.fmt(1).c_str(),
-                thP_.fmt(1).c_str(), (-objD_).fmt(2, true).c_str(), (-objP_).fmt(2, true).c_str(),
-                aD_.fmt(1).c_str(), aP_.fmt(1).c_str(), betaV_.fmt(2).c_str());
+        fputs(line.c_str(), f);
         fflush(f);
     }
 
@@ -955,6 +965,46 @@ class Solver final : public SolverBase {
         fflush(trace_);
     }
 
+    // one pass of pinpal's main loop body, sdpa_main.cpp:294-384
+    int iterate(FILE *out) override {
+        if (!initialized_) initialize();
+        if (stopped_) return 0;
+        if (!(phase_updateCheck() && iter_ < par_.maxIteration)) return stop();
+        direction_predictor();
+        if (!newton(0)) return stop();
+        step_length(0);
+        direction_corrector();
+        if (phase_ == pdFEAS && (betaV_ > R(5) || objP_ < objD_)) return stop();
+        newton(1);
+        step_length(1);
+        record_iteration();
+        print_iteration(out);
+        trace_line();
+        if (!update()) {
+            cannot_move_ = true;
+            return stop();
+        }
+        // RatioInitResCurrentRes::update (:692-698)
+        if (reductionOn_) {
+            thP_ = rabs((R(1.0) - aP_) * thP_);
+            thD_ = rabs((R(1.0) - aD_) * thD_);
+        }
+        // AverageComplementarity::update (:647-651)
+        muCur_ = ip_blocks(&Blk::X, &Blk::Z) / R(nDim_);
+        residuals();
+        // RatioInitResCurrentRes::update_exact (:700-708)
+        thP_ = (initNormP_ > R(1.0e-10)) ? normP_ / initNormP_ : R(0.0);
+        thD_ = (initNormD_ > R(1.0e-10)) ? normD_ / initNormD_ : R(0.0);
+        solveInfo_update();
+        ++iter_;
+        return 1;
+    }
+
+    int stop() {
+        stopped_ = true;
+        return 0;
+    }
+
     // pinpal's main loop, sdpa_main.cpp:294-385
     int run(FILE *out, FILE *display) override {
         auto t0 = std::chrono::steady_clock::now();
@@ -962,42 +1012,25 @@ class Solver final : public SolverBase {
         const char *hdr = "   mu      thetaP  thetaD  objP      objD      alphaP  alphaD  beta \n";
         if (out) fputs(hdr, out);
         if (display) fputs(hdr, display);
-        while (phase_updateCheck() && iter_ < par_.maxIteration) {
-            direction_predictor();
-            if (!newton(0)) break;
-            step_length(0);
-            direction_corrector();
-            if (phase_ == pdFEAS && (betaV_ > R(5) || objP_ < objD_)) break;
-            newton(1);
-            step_length(1);
-            record_iteration();
-            print_iteration(out);
-            print_iteration(display);
-            trace_line();
-            if (!update()) {
-                if (display) fprintf(display, "cannot move\n");
-                break;
-            }
-            // RatioInitResCurrentRes::update (:692-698)
-            if (reductionOn_) {
-                thP_ = rabs((R(1.0) - aP_) * thP_);
-                thD_ = rabs((R(1.0) - aD_) * thD_);
-            }
-            // AverageComplementarity::update (:647-651)
-            muCur_ = ip_blocks(&Blk::X, &Blk::Z) / R(nDim_);
-            residuals();
-            // RatioInitResCurrentRes::update_exact (:700-708)
-            thP_ = (initNormP_ > R(1.0e-10)) ? normP_ / initNormP_ : R(0.0);
-            thD_ = (initNormD_ > R(1.0e-10)) ? normD_ / initNormD_ : R(0.0);
-            solveInfo_update();
-            ++iter_;
+        while (true) {
+            const size_t before = hist_.size();
+            const int r = iterate(out);
+            if (display && hist_.size() > before) print_iteration_row(display, hist_.size() - 1);
+            if (!r) break;
         }
+        if (cannot_move_ && display) fprintf(display, "cannot move\n");
         residuals();
         final_phase_ = reverse_phase(phase_);
         tm_.total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         print_last(out);
         print_last(display);
         return iter_;
+    }
+
+    void print_iteration_row(FILE *f, size_t i) {
+        if (!f || i >= printed_.size()) return;
+        fputs(printed_[i].c_str(), f);
+        fflush(f);
     }
 
     static int reverse_phase(int ph) {
@@ -1136,7 +1169,8 @@ class Solver final : public SolverBase {
     R muInit_, muCur_, thP_, thD_, aP_, aD_, betaV_, rho_, etaP_, etaD_, objP_, objD_, normP_, normD_;
     R initNormP_, initNormD_;
     int phase_ = noINFO, final_phase_ = noINFO, reductionOn_ = 1, iter_ = 0;
-    bool initialized_ = false;
+    bool initialized_ = false, stopped_ = false, cannot_move_ = false;
+    std::vector<std::string> printed_;
     Timers tm_;
     std::vector<IterRecord> hist_;
     std::vector<cudaEvent_t> ev_;

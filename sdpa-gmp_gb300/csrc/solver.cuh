@@ -44,6 +44,9 @@ class SolverBase {
     virtual int limbs() const = 0;
     virtual void initialize() = 0;                          // Solutions::initialize + residuals
     virtual int run(FILE *out, FILE *display) = 0;          // pinpal main loop; returns iterations
+    // One pass of the main-loop body (sdpa_main.cpp:294-384): 1 = iterated, 0 = the loop
+    // condition or a break stopped it (phase decided, Cholesky failure, cannot move).
+    virtual int iterate(FILE *out) = 0;
     virtual bool newton(int corrector) = 0;                 // Newton::Mehrotra
     virtual void step_length(int corrector) = 0;            // StepLength::Mehrotra{Predictor,Corrector}
     virtual bool update() = 0;                              // Solutions::update
