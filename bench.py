@@ -1,0 +1,336 @@
+"""Benchmark: 256-bit interior-point iterations per second on the graph-partition
+workload with n = 500, m = 501 (one dense 500 x 500 block, C = -L of an
+Erdos-Renyi graph with edge probability 0.02, diag(X) = 1 and (11^T).X = 0).
+
+A "step" is one predictor-corrector iteration of the solver (Newton predictor,
+step length, Newton corrector, Lanczos step length, iterate update with the
+X / Z inverse Cholesky, residuals): one pass of the reference's main-loop body.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--precision 256|512] [--no-e2e] [--no-cpu]
+
+Our arm (default): the multi-limb GPU solver.  Timed with CUDA events on the
+solver's stream around exactly K iterations after W warm-up iterations, with a
+barrier and device synchronisation on both sides; max over ranks.  With N > 1
+each rank solves its own replica (the single solve does not shard): scaling
+"weak", value = iterations of all ranks / max time.
+
+Reference arm (--impl reference): the CPU port of the reference solver
+(oracle/sdpa_port.cpp, GMP mpf, OpenMP over all host cores in the NN matrix
+product exactly where the reference parallelises) running the same iterations
+of the same problem; rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import re
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "256-bit IPM iters/s (gpp n=500 m=501)"
+UNIT = "iters/s"
+
+
+def workload(precision: int):
+    problems = importlib.import_module("sdpa-gmp_gb300.problems")
+    d = tempfile.mkdtemp(prefix="sdpg_bench_")
+    dat = os.path.join(d, "gpp500.dat-s")
+    par = os.path.join(d, "gpp500.param")
+    problems.gpp(500, 0.02, 0).write(dat)
+    with open(par, "w") as f:
+        f.write(problems.param_text(precision=precision))
+    return d, dat, par
+
+
+def config(precision: int, ws_mb: float | None = None) -> dict:
+    return {"workload": f"gpp n=500 m=501 p=0.02 seed=0, {precision}-bit mantissa, default param.sdpa",
+            "n": 500, "m": 501, "precision_bits": precision,
+            "l2": f"no flush; per-iteration working set {ws_mb:.0f} MB > 129 MB L2" if ws_mb else "n/a",
+            "parallelism": "replicas"}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        if not shutil.which("nvidia-smi"):
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        self.f = open(self.path, "w")
+        self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits", "-lms", "100"],
+                                     stdout=self.f, stderr=subprocess.DEVNULL)
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def cpu_port_binary() -> str:
+    exe = os.path.join(ROOT, "oracle", "_port", "sdpa_port")
+    if not os.path.exists(exe):
+        subprocess.run([os.path.join(ROOT, "oracle", "build_port.sh")], check=True, stdout=subprocess.DEVNULL)
+    return exe
+
+
+def run_cpu_port(dat: str, par_dir: str, precision: int, iters: int) -> tuple[list[float], int]:
+    """Run the CPU port for `iters` iterations; returns per-iteration seconds and threads."""
+    problems = importlib.import_module("sdpa-gmp_gb300.problems")
+    par = os.path.join(par_dir, f"cpu{iters}.param")
+    with open(par, "w") as f:
+        f.write(problems.param_text(precision=precision, max_iteration=iters))
+    threads = os.cpu_count() or 1
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    r = subprocess.run([cpu_port_binary(), "-ds", dat, "-p", par, "-times"], env=env, capture_output=True, text=True,
+                       check=True)
+    times = [float(m.group(2)) for m in re.finditer(r"^ITER (\d+) ([0-9.eE+-]+)$", r.stderr, re.M)]
+    return times, threads
+
+
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def bench_ours(args) -> None:
+    import torch
+    world, rank, local, dist = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    sdpg = importlib.import_module("sdpa-gmp_gb300")
+    d, dat, par = workload(args.precision)
+    stream = torch.cuda.Stream(device=local)
+    param = sdpg.Param.read(par)
+
+    def new_solver():
+        s = sdpg.Solver(sdpg.Problem.read(dat), param, device=local, stream=stream.cuda_stream)
+        s.initialize()
+        return s
+
+    solver = new_solver()
+    for _ in range(args.warmup):
+        if not solver.iterate():
+            solver = new_solver()
+    solver.reset_counters()
+    solver.gemm_profile(enable=1)
+    launches0 = sdpg.launch_count()
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks.start()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    done = 0
+    restarts = 0
+    while done < args.steps:
+        if solver.iterate():
+            done += 1
+        else:  # the solve finished before K steps: start the same solve again
+            solver = new_solver()
+            solver.gemm_profile(enable=1)
+            restarts += 1
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(dist)
+    launches = sdpg.launch_count() - launches0
+    ms = e0.elapsed_time(e1)
+    ms_max = max_over_ranks(dist, ms)
+    total_steps = sum_over_ranks(dist, float(args.steps))
+    prof = solver.gemm_profile(enable=0)
+    timers = solver.timers()
+
+    # roofline of the dominant kernel (the multi-limb digit GEMM) against the measured
+    # IMAD.WIDE throughput of this GPU
+    imad_peak = sdpg.probe_imad_wide(local)
+    D = 10 if args.precision <= 256 else 20
+    imad_per_mac = D * (D + 1) // 2
+    gemm_ms = prof["kernel_ms"]
+    mac_rate = prof["macs"] / (gemm_ms * 1e-3) if gemm_ms > 0 else 0.0
+    achieved_imad = mac_rate * imad_per_mac
+    roofline = {"bound": "int", "kernel": "bfp_gemm_kernel",
+                "achieved": achieved_imad / 1e12, "peak": imad_peak / 1e12, "unit": "TIMAD.WIDE/s",
+                "frac": achieved_imad / imad_peak if imad_peak else None,
+                "peak_source": "measured in-run by sdpg_probe_imad_wide (MEASURED_PEAKS.json has no integer-pipe figure)",
+                "mac_rate_gmacs": mac_rate / 1e9, "imad_wide_per_mac": imad_per_mac,
+                "launches": prof["launches"], "avg_launch_us": 1e3 * gemm_ms / max(1, prof["launches"]),
+                "share_of_step": gemm_ms / ms if ms > 0 else None,
+                "traffic": None}
+
+    # end to end through the public API: host .dat-s -> parse -> upload -> full solve -> xVec back
+    e2e = None
+    if not args.no_e2e:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        prob = sdpg.Problem.read(dat)
+        s2 = sdpg.Solver(prob, param, device=local, stream=stream.cuda_stream)
+        its = s2.run()
+        x = s2.xvec()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        h2d, d2h = s2.io_bytes()
+        e2e = {"value": its / (t1 - t0), "unit": UNIT, "iterations": its, "seconds": t1 - t0,
+               "h2d_bytes_per_step": int(h2d / max(1, its)), "d2h_bytes_per_step": int((d2h + x.nbytes) / max(1, its)),
+               "phase": s2.info()["phase"], "scope": "Problem.read + Solver + run() + xvec(), host file to host result"}
+        s2.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            times, threads = run_cpu_port(dat, d, args.precision, 2)
+            sample = times[-1]
+            cpu = {"value": 1.0 / sample, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"iteration 1 of gpp500 at {args.precision}-bit on the host CPU "
+                             f"({sample:.1f} s; iteration 0 {times[0]:.1f} s)"}
+        except Exception as exc:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {exc}"}
+
+    if rank == 0:
+        ws_mb = (15 * 500 * 500 + 501 * 501) * (8 + 4 * (8 if args.precision <= 256 else 16)) / 1e6
+        line = {"metric": METRIC if args.precision <= 256 else METRIC.replace("256", str(args.precision)),
+                "value": total_steps / (ms_max * 1e-3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": f"u32x{8 if args.precision <= 256 else 16} multi-limb",
+                "data": "synthetic (seeded generator standing in for SDPLIB gpp500)",
+                "config": config(args.precision, ws_mb),
+                "impl": "ours", "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+                "clocks": clk, "phase_ms": {k: round(v, 3) for k, v in timers.items()},
+                "restarts": restarts, "peaks": {k: measured_peaks().get(k) for k in ("hbm_gbs", "bf16_tflops")}}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    shutil.rmtree(d, ignore_errors=True)
+
+
+def bench_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    d, dat, par = workload(args.precision)
+    try:
+        times, threads = run_cpu_port(dat, d, args.precision, args.warmup + args.steps)
+        timed = times[args.warmup: args.warmup + args.steps]
+        if len(timed) < args.steps:
+            raise RuntimeError("the CPU run stopped early")
+        total = sum(timed)
+        value = len(timed) / total
+        line = {"metric": METRIC if args.precision <= 256 else METRIC.replace("256", str(args.precision)),
+                "value": value, "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(timed),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "GMP mpf",
+                "data": "synthetic (seeded generator standing in for SDPLIB gpp500)", "config": config(args.precision),
+                "impl": "reference",
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"iterations {args.warmup}..{args.warmup + args.steps - 1} of gpp500, "
+                                           f"CPU port of the reference (GMP mpf, OpenMP NN product)"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    except Exception as exc:
+        line = {"impl": "reference", "unavailable": f"CPU port failed: {exc}"}
+    print(json.dumps(line))
+    shutil.rmtree(d, ignore_errors=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", type=int, default=256)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        bench_reference(args)
+    else:
+        bench_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -177,8 +177,21 @@ int sdpg_get_vector(sdpg_solver *h, int which, void *out_ml);
 int sdpg_solver_timers(sdpg_solver *h, double *out8);
 /* Iteration table rows (9 doubles each: it, mu, thetaP, thetaD, objP, objD, alphaP, alphaD, beta). */
 int sdpg_solver_history(sdpg_solver *h, double *out, int cap);
+/* Multi-limb multiply-adds issued through the GEMM since the last counter reset. */
 long long sdpg_solver_gemm_macs(sdpg_solver *h);
 int sdpg_solver_reset_counters(sdpg_solver *h);
+/* enable: 1 on, 0 off, -1 unchanged.  out3 (may be NULL): digit-GEMM kernel milliseconds,
+ * launches and multi-limb MACs since the last counter reset (events on the solver's stream). */
+int sdpg_solver_gemm_profile(sdpg_solver *h, int enable, double *out3);
+/* Bytes copied host->device and device->host by this solver so far (setup included). */
+int sdpg_solver_io_bytes(sdpg_solver *h, long long *h2d, long long *d2h);
+
+/* ---- instrumentation (no reference counterpart) ---------------------------- */
+/* Total kernel launches made by the library in this process. */
+unsigned long long sdpg_launch_count(void);
+/* Measured throughput of signed 32x32->64 multiply-adds (IMAD.WIDE) on one GPU, the
+ * instruction the multi-limb GEMM is built from; the plain path's roofline denominator. */
+int sdpg_probe_imad_wide(int device, double *ops_per_second);
 /* Read data + param, solve, write the result file: `sdpa_gmp -ds data -o out -p param`
  * (main / pinpal, sdpa_main.cpp:43-461, 501-677).  Returns iterations; info12 as above. */
 int sdpg_solve_file(const char *data_path, const char *param_path, const char *out_path, int device,

@@ -104,6 +104,10 @@ def _setup(lib: ctypes.CDLL) -> ctypes.CDLL:
         "sdpg_solver_history": (i, [vp, c.POINTER(c.c_double), i]),
         "sdpg_solver_gemm_macs": (c.c_longlong, [vp]),
         "sdpg_solver_reset_counters": (i, [vp]),
+        "sdpg_solver_gemm_profile": (i, [vp, i, c.POINTER(c.c_double)]),
+        "sdpg_solver_io_bytes": (i, [vp, c.POINTER(ll), c.POINTER(ll)]),
+        "sdpg_launch_count": (c.c_ulonglong, []),
+        "sdpg_probe_imad_wide": (i, [i, c.POINTER(c.c_double)]),
         "sdpg_solve_file": (i, [c.c_char_p, c.c_char_p, c.c_char_p, i, c.POINTER(c.c_double)]),
     }
     for name, (res, args) in sig.items():
@@ -360,6 +364,27 @@ class Solver:
 
     def reset_counters(self) -> None:
         check(lib().sdpg_solver_reset_counters(self.h))
+
+    def gemm_profile(self, enable: int = -1) -> dict:
+        out = (ctypes.c_double * 3)()
+        check(lib().sdpg_solver_gemm_profile(self.h, enable, out))
+        return {"kernel_ms": out[0], "launches": int(out[1]), "macs": int(out[2])}
+
+    def io_bytes(self) -> tuple[int, int]:
+        a, b = ctypes.c_longlong(), ctypes.c_longlong()
+        check(lib().sdpg_solver_io_bytes(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+
+def launch_count() -> int:
+    return int(lib().sdpg_launch_count())
+
+
+def probe_imad_wide(device: int = 0) -> float:
+    """Measured IMAD.WIDE (signed 32x32->64 multiply-add) operations per second."""
+    out = ctypes.c_double()
+    check(lib().sdpg_probe_imad_wide(device, ctypes.byref(out)))
+    return out.value
 
 
 def solve_file(data_path: str, param_path: str | None = None, out_path: str | None = None,

@@ -1,0 +1,80 @@
+// C ABI: counters and the integer-pipe throughput probe used by the benchmark's
+// roofline (the plain multi-limb kernels are bound by 32x32->64 multiply-adds).
+#include "capi_util.cuh"
+#include "gemm.cuh"
+#include "sdpg.h"
+
+namespace sdpg {
+unsigned long long g_kernel_launches = 0;
+}
+
+using namespace sdpg;
+
+namespace {
+
+// 16 independent signed 32x32->64 multiply-add chains per thread (IMAD.WIDE), with a
+// data dependence between iterations so no multiply can be hoisted or folded.
+__global__ void imad_wide_probe_kernel(const int *in, long long *out, int iters) {
+    int x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = in[(threadIdx.x + 7 * k) & 255];
+    int y0 = in[(threadIdx.x * 3) & 255], y1 = in[(threadIdx.x * 5 + 1) & 255];
+    long long acc[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc[k] = k;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            acc[k] += (long long)x[k] * y0;
+            acc[k + 8] += (long long)x[k] * y1;
+        }
+        y0 = ((int)acc[3] & 0x7fff) ^ it;
+        y1 = ((int)(acc[12] >> 7) & 0x7fff) + it;
+    }
+    long long s = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) s ^= acc[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" {
+
+unsigned long long sdpg_launch_count(void) { return g_kernel_launches; }
+
+int sdpg_probe_imad_wide(int device, double *ops_per_second) {
+    return sdpg_guard([&] {
+        if (!ops_per_second) throw sdpg_error(SDPG_ERR_ARG, "null output");
+        SDPG_CUDA(cudaSetDevice(device));
+        int sms = 0;
+        SDPG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        const int blocks = sms * 8, threads = 256, iters = 8192;
+        DeviceBuffer in(256 * sizeof(int)), out((size_t)blocks * threads * sizeof(long long));
+        int h[256];
+        for (int i = 0; i < 256; ++i) h[i] = 1000003 * i + 17;
+        SDPG_CUDA(cudaMemcpy(in.p, h, sizeof h, cudaMemcpyHostToDevice));
+        cudaEvent_t a, b;
+        SDPG_CUDA(cudaEventCreate(&a));
+        SDPG_CUDA(cudaEventCreate(&b));
+        imad_wide_probe_kernel<<<blocks, threads>>>((const int *)in.p, (long long *)out.p, 256);  // warm-up
+        SDPG_CHECK_LAUNCH();
+        float best = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+            SDPG_CUDA(cudaEventRecord(a));
+            imad_wide_probe_kernel<<<blocks, threads>>>((const int *)in.p, (long long *)out.p, iters);
+            SDPG_CHECK_LAUNCH();
+            SDPG_CUDA(cudaEventRecord(b));
+            SDPG_CUDA(cudaEventSynchronize(b));
+            float ms = 0;
+            SDPG_CUDA(cudaEventElapsedTime(&ms, a, b));
+            if (ms < best) best = ms;
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        *ops_per_second = (double)blocks * threads * iters * 16.0 / (best * 1e-3);
+        return (int)SDPG_OK;
+    });
+}
+
+}  // extern "C"

@@ -372,6 +372,24 @@ long long sdpg_solver_gemm_macs(sdpg_solver *h) {
     return rc == SDPG_OK ? v : rc;
 }
 
+int sdpg_solver_gemm_profile(sdpg_solver *h, int enable, double *out3) {
+    return sdpg_guard([&] {
+        if (out3) S(h).gemm_profile(out3);
+        if (enable >= 0) S(h).set_gemm_profiling(enable != 0);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_solver_io_bytes(sdpg_solver *h, long long *h2d, long long *d2h) {
+    return sdpg_guard([&] {
+        long long a = 0, b = 0;
+        S(h).io_bytes(&a, &b);
+        if (h2d) *h2d = a;
+        if (d2h) *d2h = b;
+        return (int)SDPG_OK;
+    });
+}
+
 int sdpg_solver_reset_counters(sdpg_solver *h) {
     return sdpg_guard([&] {
         S(h).reset_counters();

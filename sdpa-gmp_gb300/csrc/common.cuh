@@ -26,7 +26,14 @@ struct sdpg_error : std::runtime_error {
                                      std::string(#call) + ": " + cudaGetErrorString(_e));       \
     } while (0)
 
-#define SDPG_CHECK_LAUNCH() SDPG_CUDA(cudaGetLastError())
+// Every kernel launch in the library is followed by SDPG_CHECK_LAUNCH(), which also
+// counts it (sdpg_launch_count reports the total).
+extern unsigned long long g_kernel_launches;
+#define SDPG_CHECK_LAUNCH()                 \
+    do {                                    \
+        ++::sdpg::g_kernel_launches;        \
+        SDPG_CUDA(cudaGetLastError());      \
+    } while (0)
 
 // Device scratch that only grows; one per problem handle (or per C-ABI call).
 struct Workspace {

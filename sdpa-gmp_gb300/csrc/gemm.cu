@@ -308,9 +308,11 @@ void ml_gemm_scratch(const GemmProblem<N> &p, void *scratch, cudaStream_t stream
     constexpr int threads = (T::BM / T::TM) * (T::BN / T::TN);
     const mlf<N> one = ml_one<N>();
     const int alpha_one = memcmp(&one, &p.alpha, sizeof(one)) == 0;
+    if (p.ev_before) SDPG_CUDA(cudaEventRecord(p.ev_before, stream));
     bfp_gemm_kernel<N, T::BM, T::BN, T::BK, T::TM, T::TN><<<grid, threads, 0, stream>>>(
         Aq, Bq, EA, EB, L.Mpad, L.Npad, L.Kpad, sAq, sBq, sEA, sEB, alpha_one, p);
     SDPG_CHECK_LAUNCH();
+    if (p.ev_after) SDPG_CUDA(cudaEventRecord(p.ev_after, stream));
 }
 
 template <int N>

@@ -47,6 +47,8 @@ struct GemmProblem {
     long long ldc, sc;
     mlf<N> alpha, beta;
     int lower_only;  // 1: only entries with i >= j are written (SYRK-style update)
+    // optional: events recorded immediately before / after the digit-GEMM kernel launch
+    cudaEvent_t ev_before = nullptr, ev_after = nullptr;
 };
 
 // Build operands from BLAS-style (trans, pointer, ld, batch stride) arguments.

@@ -59,6 +59,7 @@ class Solver final : public SolverBase {
     ~Solver() override {
         for (void *p : allocs_) cudaFree(p);
         for (auto &e : ev_) cudaEventDestroy(e);
+        for (auto &e : prof_ev_) cudaEventDestroy(e);
     }
 
     int limbs() const override { return N; }
@@ -74,6 +75,31 @@ class Solver final : public SolverBase {
     void reset_counters() override {
         gemm_macs_ = 0;
         tm_ = Timers();
+        collect_gemm_events();
+        prof_ms_ = 0;
+        prof_launches_ = 0;
+        prof_macs_ = 0;
+    }
+    void set_gemm_profiling(bool on) override { prof_on_ = on; }
+    void collect_gemm_events() {
+        if (prof_used_ == 0) return;
+        SDPG_CUDA(cudaStreamSynchronize(st_));
+        for (int i = 0; i < prof_used_; ++i) {
+            float ms = 0;
+            SDPG_CUDA(cudaEventElapsedTime(&ms, prof_ev_[2 * i], prof_ev_[2 * i + 1]));
+            prof_ms_ += ms;
+        }
+        prof_used_ = 0;
+    }
+    void gemm_profile(double *o) override {
+        collect_gemm_events();
+        o[0] = prof_ms_;
+        o[1] = (double)prof_launches_;
+        o[2] = (double)prof_macs_;
+    }
+    void io_bytes(long long *h2d, long long *d2h) const override {
+        *h2d = h2d_;
+        *d2h = d2h_;
     }
     void sync() override { SDPG_CUDA(cudaStreamSynchronize(st_)); }
 
@@ -312,15 +338,18 @@ class Solver final : public SolverBase {
     V *dalloc(size_t count) { return (V *)dalloc_raw(count * sizeof(V)); }
     template <class T>
     T *upload_new(const std::vector<T> &h) {
+        h2d_ += (long long)(h.size() * sizeof(T));
         T *d = (T *)dalloc_raw(h.size() * sizeof(T));
         if (!h.empty()) SDPG_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
         return d;
     }
     void upload(V *d, const V *h, size_t count) {
+        h2d_ += (long long)(count * sizeof(V));
         SDPG_CUDA(cudaMemcpy(d, h, count * sizeof(V), cudaMemcpyHostToDevice));
     }
     // read device scalar slots [0, cnt)
     std::vector<R> fetch(int cnt) {
+        d2h_ += (long long)cnt * (long long)sizeof(V);
         std::vector<V> h(cnt);
         SDPG_CUDA(cudaMemcpyAsync(h.data(), slot_, cnt * sizeof(V), cudaMemcpyDeviceToHost, st_));
         SDPG_CUDA(cudaStreamSynchronize(st_));
@@ -329,6 +358,7 @@ class Solver final : public SolverBase {
         return r;
     }
     R fetch1(const V *d) {
+        d2h_ += (long long)sizeof(V);
         V h;
         SDPG_CUDA(cudaMemcpyAsync(&h, d, sizeof(V), cudaMemcpyDeviceToHost, st_));
         SDPG_CUDA(cudaStreamSynchronize(st_));
@@ -353,7 +383,23 @@ class Solver final : public SolverBase {
         p.beta = beta.v;
         gemm(p);
     }
-    void gemm(const GemmProblem<N> &p) {
+    void gemm(const GemmProblem<N> &p0) {
+        GemmProblem<N> p = p0;
+        if (prof_on_) {
+            if (prof_used_ * 2 + 2 > (int)prof_ev_.size()) {
+                if (prof_used_ >= 4096) collect_gemm_events();
+                while (prof_used_ * 2 + 2 > (int)prof_ev_.size()) {
+                    cudaEvent_t e;
+                    SDPG_CUDA(cudaEventCreate(&e));
+                    prof_ev_.push_back(e);
+                }
+            }
+            p.ev_before = prof_ev_[2 * prof_used_];
+            p.ev_after = prof_ev_[2 * prof_used_ + 1];
+            ++prof_used_;
+            ++prof_launches_;
+            prof_macs_ += (long long)p.M * p.Nn * p.K * p.batch;
+        }
         const size_t mark = ws_.used;
         ml_gemm<N>(p, ws_, st_);
         ws_.used = mark;
@@ -490,6 +536,7 @@ class Solver final : public SolverBase {
                             }
                         long long *dxo = (long long *)ws_.carve(xo.size() * sizeof(long long));
                         long long *dyo = (long long *)ws_.carve(yo.size() * sizeof(long long));
+                        h2d_ += (long long)xo.size() * 16;
                         SDPG_CUDA(cudaMemcpyAsync(dxo, xo.data(), xo.size() * 8, cudaMemcpyHostToDevice, st_));
                         SDPG_CUDA(cudaMemcpyAsync(dyo, yo.data(), yo.size() * 8, cudaMemcpyHostToDevice, st_));
                         k_dot_batched<N>(nn, G, dxo, B.cons.dense, dyo, cnt * nd, P, ws_, st_);
@@ -507,6 +554,7 @@ class Solver final : public SolverBase {
         if (!corrector) {
             ml_potrf<N>(m_, B_, m_, info_, ws_, st_);
             int info = 0;
+            d2h_ += (long long)sizeof(int);
             SDPG_CUDA(cudaMemcpyAsync(&info, info_, sizeof(int), cudaMemcpyDeviceToHost, st_));
             SDPG_CUDA(cudaStreamSynchronize(st_));
             if (info != 0) return false;
@@ -565,6 +613,7 @@ class Solver final : public SolverBase {
         {
             const V one = ml_one<N>();
             std::vector<V> h(n, one);
+            h2d_ += (long long)n * (long long)sizeof(V);
             SDPG_CUDA(cudaMemcpyAsync(B.r, h.data(), n * sizeof(V), cudaMemcpyHostToDevice, st_));
             SDPG_CUDA(cudaMemsetAsync(B.q, 0, n * sizeof(V), st_));
             SDPG_CUDA(cudaStreamSynchronize(st_));
@@ -580,6 +629,7 @@ class Solver final : public SolverBase {
             const R rb = R(1) / beta;  // value = MONE / beta
             {
                 V *rbd = slot_ + 40;
+                h2d_ += (long long)sizeof(V);
                 SDPG_CUDA(cudaMemcpyAsync(rbd, &rb.v, sizeof(V), cudaMemcpyHostToDevice, st_));
                 k_lanczos_next<N>(n, B.r, rbd, B.q, B.qold, st_);  // qold = q; q = r / beta
             }
@@ -593,6 +643,7 @@ class Solver final : public SolverBase {
             }
             {
                 V *bd = slot_ + 41;
+                h2d_ += (long long)sizeof(V);
                 SDPG_CUDA(cudaMemcpyAsync(bd, &beta.v, sizeof(V), cudaMemcpyHostToDevice, st_));
                 k_lanczos_update<N>(n, B.w, B.q, B.qold, B.td + k, bd, B.r, st_);
             }
@@ -607,6 +658,7 @@ class Solver final : public SolverBase {
                 ws_.used = mark;
             }
             std::vector<V> h(5);
+            d2h_ += 3 * (long long)sizeof(V);
             SDPG_CUDA(cudaMemcpyAsync(h.data(), slot_ + 42, 3 * sizeof(V), cudaMemcpyDeviceToHost, st_));
             SDPG_CUDA(cudaStreamSynchronize(st_));
             if (eig) {
@@ -615,6 +667,7 @@ class Solver final : public SolverBase {
                 error = R(h[1]);
             }
             beta = rsqrt_(R(h[2]));
+            h2d_ += (long long)sizeof(V);
             SDPG_CUDA(cudaMemcpyAsync(B.te + k, &beta.v, sizeof(V), cudaMemcpyHostToDevice, st_));  // diagVec2[k]
             SDPG_CUDA(cudaStreamSynchronize(st_));
             ++k;
@@ -753,7 +806,8 @@ class Solver final : public SolverBase {
         k_copy<N>((long long)n * n, A, B.F, st_);
         ml_potrf<N>(n, B.F, n, info_, ws_, st_);
         int info = 0;
-        SDPG_CUDA(cudaMemcpyAsync(&info, info_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+        d2h_ += (long long)sizeof(int);
+            SDPG_CUDA(cudaMemcpyAsync(&info, info_, sizeof(int), cudaMemcpyDeviceToHost, st_));
         SDPG_CUDA(cudaStreamSynchronize(st_));
         if (info != 0) return false;
         k_zero_strict_upper<N>(n, B.F, st_);
@@ -1106,6 +1160,7 @@ class Solver final : public SolverBase {
     // The reference prints xVec = -y (IO::printLastInfo, Vector::display with scalar -1).
     void get_y(void *out, int form) const override {
         std::vector<V> h(m_);
+        d2h_ += (long long)m_ * (long long)sizeof(V);
         SDPG_CUDA(cudaMemcpy(h.data(), y_, m_ * sizeof(V), cudaMemcpyDeviceToHost));
         for (int i = 0; i < m_; ++i) {
             if (form == 0) ((double *)out)[i] = ml_to_double(ml_neg(h[i]));
@@ -1119,6 +1174,7 @@ class Solver final : public SolverBase {
         const V *srcs[] = {B.X, B.Z, B.Dx, B.Dz, B.Zinv, B.LX, B.LZ, B.C, B.Dres};
         if (which < 0 || which > 8) throw sdpg_error(SDPG_ERR_ARG, "bad matrix selector");
         const V *src = srcs[which];
+        d2h_ += (long long)(nn * sizeof(V));
         SDPG_CUDA(cudaMemcpy(h.data(), src, nn * sizeof(V), cudaMemcpyDeviceToHost));
         for (size_t i = 0; i < nn; ++i) {
             if (form == 0) ((double *)out)[i] = ml_to_double(h[i]);
@@ -1176,6 +1232,12 @@ class Solver final : public SolverBase {
     std::vector<cudaEvent_t> ev_;
     FILE *trace_ = nullptr;
     long long gemm_macs_ = 0;
+    bool prof_on_ = false;
+    std::vector<cudaEvent_t> prof_ev_;
+    int prof_used_ = 0;
+    double prof_ms_ = 0;
+    long long prof_launches_ = 0, prof_macs_ = 0;
+    mutable long long h2d_ = 0, d2h_ = 0;
 };
 
 }  // namespace

@@ -70,6 +70,12 @@ class SolverBase {
     virtual int block_size(int l) const = 0;
     virtual long long gemm_macs() const = 0;                // multi-limb MACs issued through the GEMM
     virtual void reset_counters() = 0;
+    // GEMM-kernel profiling: when on, every digit-GEMM launch is bracketed by CUDA events;
+    // out: [kernel milliseconds, launches, multi-limb MACs] since the last reset.
+    virtual void set_gemm_profiling(bool on) = 0;
+    virtual void gemm_profile(double *out3) = 0;
+    // bytes copied host->device and device->host since construction (setup included)
+    virtual void io_bytes(long long *h2d, long long *d2h) const = 0;
     virtual void sync() = 0;
 };
 
