@@ -116,23 +116,55 @@ __global__ void recip_diag_kernel(int n, const mlf<N> *L, int ldl, mlf<N> *rinv)
     if (i < n) rinv[i] = ml_recip(L[i + (long long)i * ldl]);
 }
 
-// x := L^{-T} L^{-1} x in one CTA (forward then backward substitution)
+// x := L^{-T} L^{-1} x in one CTA, blocked by NB: warp 0 solves each diagonal block
+// (one lane per row, pivots broadcast by shuffle), then every thread updates one of
+// the remaining rows with the block's NB solved entries.
 template <int N>
 __global__ void potrs_kernel(int n, const mlf<N> *L, int ldl, const mlf<N> *rinv, mlf<N> *x) {
-    for (int j = 0; j < n; ++j) {
-        if (threadIdx.x == 0) x[j] = ml_mul(x[j], rinv[j]);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // forward: L y = x
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        const int kb = min(NB, n - k0);
+        if (warp == 0) {
+            mlf<N> a = lane < kb ? x[k0 + lane] : ml_zero<N>();
+            for (int j = 0; j < kb; ++j) {
+                mlf<N> xj = ml_zero<N>();
+                if (lane == j) xj = ml_mul(a, rinv[k0 + j]);
+                xj = ml_shfl(xj, j);
+                if (lane == j) a = xj;
+                if (lane > j && lane < kb) a = ml_sub(a, ml_mul(L[(k0 + lane) + (long long)(k0 + j) * ldl], xj));
+            }
+            if (lane < kb) x[k0 + lane] = a;
+        }
         __syncthreads();
-        const mlf<N> xj = x[j];
-        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x)
-            x[i] = ml_sub(x[i], ml_mul(L[i + (long long)j * ldl], xj));
+        for (int i = k0 + kb + tid; i < n; i += blockDim.x) {
+            mlf<N> acc = ml_zero<N>();
+            for (int j = 0; j < kb; ++j) acc = ml_add(acc, ml_mul(L[i + (long long)(k0 + j) * ldl], x[k0 + j]));
+            x[i] = ml_sub(x[i], acc);
+        }
         __syncthreads();
     }
-    for (int j = n - 1; j >= 0; --j) {
-        if (threadIdx.x == 0) x[j] = ml_mul(x[j], rinv[j]);
+    // backward: L^T z = y
+    const int nblk = (n + NB - 1) / NB;
+    for (int bI = nblk - 1; bI >= 0; --bI) {
+        const int k0 = bI * NB, kb = min(NB, n - k0);
+        if (warp == 0) {
+            mlf<N> a = lane < kb ? x[k0 + lane] : ml_zero<N>();
+            for (int j = kb - 1; j >= 0; --j) {
+                mlf<N> zj = ml_zero<N>();
+                if (lane == j) zj = ml_mul(a, rinv[k0 + j]);
+                zj = ml_shfl(zj, j);
+                if (lane == j) a = zj;
+                if (lane < j) a = ml_sub(a, ml_mul(L[(k0 + j) + (long long)(k0 + lane) * ldl], zj));
+            }
+            if (lane < kb) x[k0 + lane] = a;
+        }
         __syncthreads();
-        const mlf<N> xj = x[j];
-        for (int i = threadIdx.x; i < j; i += blockDim.x)
-            x[i] = ml_sub(x[i], ml_mul(L[j + (long long)i * ldl], xj));
+        for (int i = tid; i < k0; i += blockDim.x) {
+            mlf<N> acc = ml_zero<N>();
+            for (int j = 0; j < kb; ++j) acc = ml_add(acc, ml_mul(L[(k0 + j) + (long long)i * ldl], x[k0 + j]));
+            x[i] = ml_sub(x[i], acc);
+        }
         __syncthreads();
     }
 }
@@ -167,7 +199,7 @@ void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t 
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int kb = min(NB, n - k0);
         mlf<N> *Akk = A + k0 + (long long)k0 * lda;
-        potf2_kernel<N><<<1, 256, 0, s>>>(Akk, lda, kb, k0, info, rinv);
+        potf2_kernel<N><<<1, 512, 0, s>>>(Akk, lda, kb, k0, info, rinv);
         SDPG_CHECK_LAUNCH();
         const int rows = n - k0 - kb;
         if (rows <= 0) break;

@@ -264,41 +264,91 @@ MLHD mlf<N> ml_add(const mlf<N> &a, const mlf<N> &b) {
 template <int N>
 MLHD mlf<N> ml_sub(const mlf<N> &a, const mlf<N> &b) { return ml_add(a, ml_neg(b)); }
 
-// --- multiplication -------------------------------------------------------------
+// --- multiplication -------------------------------------------------------------------
+//
+// Each mantissa is split into D radix-2^28 digits; a digit product is < 2^56, so
+// a column of <= D of them fits an unsigned 64-bit accumulator without carry
+// handling.  Every column is an independent chain of 32x32->64 multiply-adds
+// (short dependence chains, high instruction-level parallelism), followed by one
+// carry pass.  Columns below D-2 are dropped (their sum is below 2^-(32N-1) of the
+// product), then the top 32N bits are taken: the result is truncated like GMP's.
+
+template <int N>
+struct MulDigits {
+    static constexpr int D = (32 * N + 27) / 28;  // N=8 -> 10, N=16 -> 19
+    static constexpr int CK = D - 2;              // lowest kept product column
+    static constexpr int NCOL = 2 * D - 1 - CK;   // kept columns CK .. 2D-2
+    static constexpr int B0 = 28 * CK;            // bit weight of column CK
+    static constexpr int TOPREL = 64 * N - 1 - B0;  // product's top possible bit, relative to B0
+    static constexpr int LW = (28 * (NCOL + 1) + 31) / 32 + 2;
+};
+
+template <int N>
+MLHD void ml_digits28(const uint32_t (&m)[N], uint32_t (&d)[MulDigits<N>::D]) {
+    ML_UNROLL
+    for (int t = 0; t < MulDigits<N>::D; ++t) {
+        const int bit = 28 * t;
+        const int w = bit >> 5, r = bit & 31;
+        const uint32_t lo = (w < N) ? (m[w] >> r) : 0u;
+        const uint32_t hi = (r > 4 && w + 1 < N) ? (m[w + 1] << (32 - r)) : 0u;
+        d[t] = (lo | hi) & 0x0FFFFFFFu;
+    }
+}
+
+// 32 bits of W starting at compile-time bit offset `off`
+template <int L>
+MLHD uint32_t ml_bits32(const uint32_t (&W)[L], int off) {
+    const int w = off >> 5, r = off & 31;
+    const uint32_t lo = (w < L) ? (W[w] >> r) : 0u;
+    const uint32_t hi = (r != 0 && w + 1 < L) ? (W[w + 1] << (32 - r)) : 0u;
+    return lo | hi;
+}
 
 template <int N>
 MLHD mlf<N> ml_mul(const mlf<N> &a, const mlf<N> &b) {
     if (ml_is_zero(a) || ml_is_zero(b)) return ml_zero<N>();
-    // Columns N-2 .. 2N-1 of the 2N-limb product (lower columns dropped: truncation).
-    uint32_t r[N + 2];
-    uint64_t acc = 0;
-    uint32_t acc_hi = 0;
+    using G = MulDigits<N>;
+    uint32_t da[G::D], db[G::D];
+    ml_digits28<N>(a.m, da);
+    ml_digits28<N>(b.m, db);
+    uint64_t acc[G::NCOL + 1];
     ML_UNROLL
-    for (int c = N - 2; c <= 2 * N - 2; ++c) {
+    for (int c = 0; c <= G::NCOL; ++c) acc[c] = 0;
+    ML_UNROLL
+    for (int c = G::CK; c <= 2 * G::D - 2; ++c) {
         ML_UNROLL
-        for (int p = 0; p < N; ++p) {
+        for (int p = 0; p < G::D; ++p) {
             const int q = c - p;
-            if (q >= 0 && q < N) {
-                const uint64_t t = (uint64_t)a.m[p] * b.m[q];
-                acc += t;
-                acc_hi += (acc < t) ? 1u : 0u;
-            }
+            if (q >= 0 && q < G::D) acc[c - G::CK] += (uint64_t)da[p] * db[q];
         }
-        r[c - (N - 2)] = (uint32_t)acc;
-        acc = (acc >> 32) | ((uint64_t)acc_hi << 32);
-        acc_hi = 0;
     }
-    r[N + 1] = (uint32_t)acc;
+    ML_UNROLL
+    for (int c = 0; c < G::NCOL; ++c) {
+        acc[c + 1] += acc[c] >> 28;
+        acc[c] &= 0x0FFFFFFFull;
+    }
+    uint32_t W[G::LW];
+    ML_UNROLL
+    for (int w = 0; w < G::LW; ++w) W[w] = 0;
+    ML_UNROLL
+    for (int c = 0; c <= G::NCOL; ++c) {
+        const int bit = 28 * c;
+        const int w = bit >> 5, r = bit & 31;
+        W[w] |= (uint32_t)(acc[c] << r);
+        if (w + 1 < G::LW) W[w + 1] |= (uint32_t)(acc[c] >> (32 - r));
+    }
+    const bool top = (W[G::TOPREL >> 5] >> (G::TOPREL & 31)) & 1u;
+    constexpr int off = G::TOPREL + 1 - 32 * N;  // lowest mantissa bit when the top bit is set
     mlf<N> o;
     o.s = a.s ^ b.s;
-    if (r[N + 1] & 0x80000000u) {
+    if (top) {
         o.e = a.e + b.e;
         ML_UNROLL
-        for (int k = 0; k < N; ++k) o.m[k] = r[k + 2];
+        for (int k = 0; k < N; ++k) o.m[k] = ml_bits32<G::LW>(W, off + 32 * k);
     } else {
         o.e = a.e + b.e - 1;
         ML_UNROLL
-        for (int k = 0; k < N; ++k) o.m[k] = (r[k + 2] << 1) | (r[k + 1] >> 31);
+        for (int k = 0; k < N; ++k) o.m[k] = ml_bits32<G::LW>(W, off - 1 + 32 * k);
     }
     return o;
 }
@@ -405,6 +455,41 @@ struct ml_newton_steps {
                                  : (32 * N + 8 <= 800) ? 4 : 5;
 };
 
+// Precision conversions: keep the top M limbs (truncating) / extend with zero limbs.
+template <int M, int N>
+MLHD mlf<M> ml_narrow(const mlf<N> &a) {
+    mlf<M> r;
+    r.e = a.e;
+    r.s = a.s;
+    ML_UNROLL
+    for (int k = 0; k < M; ++k) r.m[k] = (N - M + k >= 0) ? a.m[N - M + k] : 0u;
+    return r;
+}
+template <int M, int N>
+MLHD mlf<M> ml_widen(const mlf<N> &a) {
+    mlf<M> r;
+    r.e = a.e;
+    r.s = a.s;
+    ML_UNROLL
+    for (int k = 0; k < M; ++k) r.m[k] = (k - (M - N) >= 0) ? a.m[k - (M - N)] : 0u;
+    return r;
+}
+
+// 1/bn for a mantissa bn in [1/2, 1): Newton steps at rising precision (N/2 first,
+// then one step at N doubles the correct bits), so only the last steps pay full cost.
+template <int N>
+MLHD mlf<N> ml_recip_mant(const mlf<N> &bn) {
+    const mlf<N> one = ml_one<N>();
+    mlf<N> x;
+    if constexpr (N <= 2) {
+        x = ml_from_double<N>(1.0 / ml_mant_double(bn));
+    } else {
+        x = ml_widen<N, N / 2>(ml_recip_mant<N / 2>(ml_narrow<N / 2, N>(bn)));
+    }
+    x = ml_add(x, ml_mul(x, ml_sub(one, ml_mul(bn, x))));
+    return x;
+}
+
 // 1/b
 template <int N>
 MLHD mlf<N> ml_recip(const mlf<N> &b) {
@@ -412,14 +497,9 @@ MLHD mlf<N> ml_recip(const mlf<N> &b) {
     mlf<N> bn = b;  // bn = mantissa in [1/2, 1)
     bn.e = 0;
     bn.s = 0;
-    const double md = ml_mant_double(bn);
-    mlf<N> x = ml_from_double<N>(1.0 / md);  // ~ 1/bn in (1, 2]
     const mlf<N> one = ml_one<N>();
-    ML_UNROLL
-    for (int it = 0; it < ml_newton_steps<N>::value; ++it) {
-        const mlf<N> t = ml_sub(one, ml_mul(bn, x));
-        x = ml_add(x, ml_mul(x, t));
-    }
+    mlf<N> x = ml_recip_mant<N>(bn);
+    x = ml_add(x, ml_mul(x, ml_sub(one, ml_mul(bn, x))));  // final step at full precision
     x.e -= b.e;
     x.s = b.s;
     return x;
@@ -436,23 +516,32 @@ MLHD mlf<N> ml_div(const mlf<N> &a, const mlf<N> &b) {
     return q;
 }
 
+// 1/sqrt(an) for an in [1/4, 1): Newton steps y += y (1 - an y^2) / 2 at rising precision
+template <int N>
+MLHD mlf<N> ml_rsqrt_mant(const mlf<N> &an) {
+    const mlf<N> one = ml_one<N>();
+    mlf<N> y;
+    if constexpr (N <= 2) {
+        y = ml_from_double<N>(1.0 / sqrt(ml_to_double(an)));
+    } else {
+        y = ml_widen<N, N / 2>(ml_rsqrt_mant<N / 2>(ml_narrow<N / 2, N>(an)));
+    }
+    const mlf<N> t = ml_sub(one, ml_mul(an, ml_mul(y, y)));
+    return ml_add(y, ml_ldexp(ml_mul(y, t), -1));
+}
+
 // 1/sqrt(a), a > 0
 template <int N>
 MLHD mlf<N> ml_rsqrt(const mlf<N> &a) {
     if (ml_is_zero(a) || a.s) return ml_zero<N>();
     // a = an * 2^(2k) with an in [1/4, 1)
-    int k = a.e >> 1;  // floor(e/2)
+    const int k = a.e >> 1;  // floor(e/2)
     mlf<N> an = a;
     an.e = a.e - 2 * k;  // 0 or 1
-    double ad = ml_mant_double(an) * (an.e == 1 ? 2.0 : 1.0);
-    mlf<N> y = ml_from_double<N>(1.0 / sqrt(ad));
+    mlf<N> y = ml_rsqrt_mant<N>(an);
     const mlf<N> one = ml_one<N>();
-    ML_UNROLL
-    for (int it = 0; it < ml_newton_steps<N>::value; ++it) {
-        // y += y * (1 - an*y^2) / 2
-        const mlf<N> t = ml_sub(one, ml_mul(an, ml_mul(y, y)));
-        y = ml_add(y, ml_ldexp(ml_mul(y, t), -1));
-    }
+    const mlf<N> t = ml_sub(one, ml_mul(an, ml_mul(y, y)));
+    y = ml_add(y, ml_ldexp(ml_mul(y, t), -1));  // final step at full precision
     y.e -= k;
     return y;
 }
