@@ -314,8 +314,52 @@ def bench_reference(args) -> None:
     shutil.rmtree(d, ignore_errors=True)
 
 
+def bench_gemm(args) -> None:
+    """Kernel mode: repeated n x n x n multi-limb GEMMs through sdpg_rgemm_device
+    (the profiling target of the digit-GEMM kernel); prints GMAC/s."""
+    import numpy as np
+    import torch
+    sdpg = importlib.import_module("sdpa-gmp_gb300")
+    lib = sdpg.lib()
+    n = args.gemm_n
+    limbs = 8 if args.precision <= 256 else 16
+    rng = np.random.default_rng(0)
+
+    def rnd(cnt):
+        h = rng.integers(0, 2**32, size=(cnt, limbs + 2), dtype=np.uint64).astype(np.uint32)
+        h[:, 0] = rng.integers(-5, 5, size=cnt).astype(np.int32).view(np.uint32)
+        h[:, 1] = rng.integers(0, 2, size=cnt).astype(np.uint32)
+        h[:, -1] |= np.uint32(0x80000000)
+        return torch.from_numpy(h.view(np.int32)).cuda()
+
+    A, B, C = rnd(n * n), rnd(n * n), rnd(n * n)
+    one = sdpg.ml_parse(["1"], limbs)
+    zero = sdpg.ml_parse(["0"], limbs)
+    st = torch.cuda.current_stream().cuda_stream
+
+    def run():
+        sdpg.check(lib.sdpg_rgemm_device(limbs, b"N", b"N", n, n, n, one.ctypes.data, A.data_ptr(), n,
+                                         B.data_ptr(), n, zero.ctypes.data, C.data_ptr(), n, st))
+
+    for _ in range(args.warmup):
+        run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    print(json.dumps({"kernel": "gemm", "n": n, "limbs": limbs, "ms_per_gemm": ms,
+                      "gmacs": n ** 3 / (ms * 1e-3) / 1e9}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--kernel", choices=["gemm"], default=None,
+                    help="kernel mode: time repeated multi-limb GEMMs instead of IPM iterations")
+    ap.add_argument("--gemm-n", type=int, default=500)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -326,7 +370,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.kernel == "gemm":
+        bench_gemm(args)
+    elif args.impl == "reference":
         bench_reference(args)
     else:
         bench_ours(args)
