@@ -83,6 +83,26 @@ int sdpg_rgemm_device(int limbs, char transa, char transb, int m, int n, int k, 
                       const void *A, int lda, const void *B, int ldb, const void *beta, void *C, int ldc,
                       void *stream);
 
+/* Size of the fixed device scratch behind sdpg_rgemm_device_noalloc (64 MiB). */
+#define SDPG_NOALLOC_SCRATCH_BYTES (64ull << 20)
+
+/* The same product as sdpg_rgemm_device, for callers that must not have the library
+ * allocate device memory: programs whose device memory is all held by their own pool
+ * allocator, or latency-critical loops where an allocation (which synchronises the
+ * device and can fail when memory is short) is not acceptable.  It has no counterpart
+ * in the reference.  Its scratch is one fixed device array of SDPG_NOALLOC_SCRATCH_BYTES
+ * that every GPU loading the library holds until the process exits; the call makes no
+ * cudaMalloc / cudaFree and no allocating library call.  The first call on a device
+ * looks up that array's device address (cudaGetSymbolAddress), so make it before any
+ * stream capture.  Products needing more scratch than the limit (about 880 x 880 x 880
+ * at 256 bits) return SDPG_ERR_TOO_LARGE without launching anything.  All calls share
+ * the one array: calls whose work can overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller.  Nothing in the array needs to
+ * start at zero; each call writes every scratch byte it reads. */
+int sdpg_rgemm_device_noalloc(int limbs, char transa, char transb, int m, int n, int k, const void *alpha,
+                              const void *A, int lda, const void *B, int ldb, const void *beta, void *C,
+                              int ldc, void *stream);
+
 
 /* ---- factorisations and eigenvalues (standalone, host buffers) ---------------- */
 
