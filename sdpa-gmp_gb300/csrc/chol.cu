@@ -138,9 +138,10 @@ __global__ void potrs_kernel(int n, const mlf<N> *L, int ldl, const mlf<N> *rinv
         }
         __syncthreads();
         for (int i = k0 + kb + tid; i < n; i += blockDim.x) {
-            mlf<N> acc = ml_zero<N>();
-            for (int j = 0; j < kb; ++j) acc = ml_add(acc, ml_mul(L[i + (long long)(k0 + j) * ldl], x[k0 + j]));
-            x[i] = ml_sub(x[i], acc);
+            mlf<N> acc[4] = {ml_zero<N>(), ml_zero<N>(), ml_zero<N>(), ml_zero<N>()};
+            for (int j = 0; j < kb; ++j)
+                acc[j & 3] = ml_add(acc[j & 3], ml_mul(L[i + (long long)(k0 + j) * ldl], x[k0 + j]));
+            x[i] = ml_sub(x[i], ml_add(ml_add(acc[0], acc[1]), ml_add(acc[2], acc[3])));
         }
         __syncthreads();
     }
@@ -161,9 +162,10 @@ __global__ void potrs_kernel(int n, const mlf<N> *L, int ldl, const mlf<N> *rinv
         }
         __syncthreads();
         for (int i = tid; i < k0; i += blockDim.x) {
-            mlf<N> acc = ml_zero<N>();
-            for (int j = 0; j < kb; ++j) acc = ml_add(acc, ml_mul(L[(k0 + j) + (long long)i * ldl], x[k0 + j]));
-            x[i] = ml_sub(x[i], acc);
+            mlf<N> acc[4] = {ml_zero<N>(), ml_zero<N>(), ml_zero<N>(), ml_zero<N>()};
+            for (int j = 0; j < kb; ++j)
+                acc[j & 3] = ml_add(acc[j & 3], ml_mul(L[(k0 + j) + (long long)i * ldl], x[k0 + j]));
+            x[i] = ml_sub(x[i], ml_add(ml_add(acc[0], acc[1]), ml_add(acc[2], acc[3])));
         }
         __syncthreads();
     }

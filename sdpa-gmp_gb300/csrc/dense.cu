@@ -36,6 +36,12 @@ __global__ void copy_kernel(long long n, const mlf<N> *x, mlf<N> *out) {
 }
 
 template <int N>
+__global__ void fill_kernel(long long n, mlf<N> *x, mlf<N> v) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) x[i] = v;
+}
+
+template <int N>
 __global__ void identity_kernel(int n, mlf<N> *A, mlf<N> v) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= (long long)n * n) return;
@@ -78,10 +84,15 @@ __global__ void dot_partial_kernel(long long n, const mlf<N> *x, const long long
                                    const long long *yoff, mlf<N> *partial) {
     const int b = blockIdx.y;
     const long long xo = xoff ? xoff[b] : 0, yo = yoff ? yoff[b] : 0;
-    mlf<N> acc = ml_zero<N>();
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        acc = ml_add(acc, ml_mul(x[xo + i], y[yo + i]));
-    acc = ml_block_sum(acc);
+    mlf<N> a0 = ml_zero<N>(), a1 = ml_zero<N>();
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; i + stride < n; i += 2 * stride) {
+        a0 = ml_add(a0, ml_mul(x[xo + i], y[yo + i]));
+        a1 = ml_add(a1, ml_mul(x[xo + i + stride], y[yo + i + stride]));
+    }
+    if (i < n) a0 = ml_add(a0, ml_mul(x[xo + i], y[yo + i]));
+    mlf<N> acc = ml_block_sum(ml_add(a0, a1));
     if (threadIdx.x == 0) partial[(long long)b * gridDim.x + blockIdx.x] = acc;
 }
 
@@ -275,6 +286,13 @@ void k_copy(long long n, const mlf<N> *x, mlf<N> *out, cudaStream_t s) {
 }
 
 template <int N>
+void k_fill(long long n, mlf<N> *x, const mlf<N> &v, cudaStream_t s) {
+    if (n <= 0) return;
+    fill_kernel<N><<<grid1(n), kThreads, 0, s>>>(n, x, v);
+    SDPG_CHECK_LAUNCH();
+}
+
+template <int N>
 void k_set_identity(int n, mlf<N> *A, const mlf<N> &v, cudaStream_t s) {
     identity_kernel<N><<<grid1((long long)n * n), kThreads, 0, s>>>(n, A, v);
     SDPG_CHECK_LAUNCH();
@@ -406,6 +424,7 @@ void k_schur_f1_dense_scatter(const BlockDev<N> &B, const int *owners, int cnt, 
     template void k_axpby<N>(long long, const mlf<N> &, const mlf<N> *, const mlf<N> &, const mlf<N> *,        \
                              mlf<N> *, cudaStream_t);                                                        \
     template void k_copy<N>(long long, const mlf<N> *, mlf<N> *, cudaStream_t);                              \
+    template void k_fill<N>(long long, mlf<N> *, const mlf<N> &, cudaStream_t);                              \
     template void k_set_identity<N>(int, mlf<N> *, const mlf<N> &, cudaStream_t);                            \
     template void k_symmetrize<N>(int, mlf<N> *, cudaStream_t);                                              \
     template void k_transpose<N>(int, const mlf<N> *, mlf<N> *, cudaStream_t);                               \

@@ -35,9 +35,14 @@ __global__ void matvec_t_kernel(int n, const mlf<N> *A, int tri, const mlf<N> *x
     const int lo = (tri == 1) ? o : 0;
     const int hi = (tri == 2) ? o + 1 : n;
     const mlf<N> *col = A + (long long)o * n;
-    mlf<N> acc = ml_zero<N>();
-    for (int i = lo + lane; i < hi; i += 32) acc = ml_add(acc, ml_mul(col[i], x[i]));
-    acc = ml_warp_sum(acc);
+    mlf<N> a0 = ml_zero<N>(), a1 = ml_zero<N>();
+    int i = lo + lane;
+    for (; i + 32 < hi; i += 64) {
+        a0 = ml_add(a0, ml_mul(col[i], x[i]));
+        a1 = ml_add(a1, ml_mul(col[i + 32], x[i + 32]));
+    }
+    if (i < hi) a0 = ml_add(a0, ml_mul(col[i], x[i]));
+    mlf<N> acc = ml_warp_sum(ml_add(a0, a1));
     if (lane == 0) y[o] = acc;
 }
 

@@ -123,7 +123,7 @@ __device__ __forceinline__ mlf<N> columns_to_mlf(long long (&acc)[NC], int escal
 }
 
 template <int N, int BM, int BN, int BK, int TM, int TN>
-__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+__global__ void __launch_bounds__((BM / TM) * (BN / TN), 2)
 bfp_gemm_kernel(const int *__restrict__ Aq, const int *__restrict__ Bq, const int *__restrict__ EA,
                 const int *__restrict__ EB, int Mpad, int Npad, int Kpad, long long sAq, long long sBq,
                 long long sEA, long long sEB, int alpha_one, GemmProblem<N> p) {
@@ -178,18 +178,20 @@ bfp_gemm_kernel(const int *__restrict__ Aq, const int *__restrict__ Bq, const in
 #pragma unroll
                 for (int c = 0; c < TN; ++c) bv[c][d] = Bs[d][kk][tx * TN + c];
             }
+            // digit-pair order: consecutive multiply-adds go to different column
+            // accumulators (and different outputs), so no two back-to-back IMAD.WIDE
+            // depend on each other
 #pragma unroll
-            for (int a = 0; a < TM; ++a)
+            for (int pp = 0; pp < D; ++pp)
 #pragma unroll
-                for (int c = 0; c < TN; ++c)
+                for (int qq = 0; qq < D; ++qq) {
+                    if (pp + qq < C0) continue;
 #pragma unroll
-                    for (int col = C0; col <= 2 * D - 2; ++col)
+                    for (int a = 0; a < TM; ++a)
 #pragma unroll
-                        for (int pp = 0; pp < D; ++pp) {
-                            const int qq = col - pp;
-                            if (qq >= 0 && qq < D)
-                                acc[a][c][col - C0] += (long long)av[a][pp] * (long long)bv[c][qq];
-                        }
+                        for (int c = 0; c < TN; ++c)
+                            acc[a][c][pp + qq - C0] += (long long)av[a][pp] * (long long)bv[c][qq];
+                }
         }
         since += BK;
         if (since >= CH) {

@@ -42,6 +42,8 @@ void k_axpby(long long n, const mlf<N> &a, const mlf<N> *x, const mlf<N> &b, con
 template <int N>
 void k_copy(long long n, const mlf<N> *x, mlf<N> *out, cudaStream_t s);
 template <int N>
+void k_fill(long long n, mlf<N> *x, const mlf<N> &v, cudaStream_t s);  // x[i] = v
+template <int N>
 void k_set_identity(int n, mlf<N> *A, const mlf<N> &v, cudaStream_t s);  // A = v*I
 template <int N>
 void k_symmetrize(int n, mlf<N> *A, cudaStream_t s);  // Lal::getSymmetrize, sdpa_linear.cpp:457-482

@@ -490,7 +490,8 @@ MLHD mlf<N> ml_recip_mant(const mlf<N> &bn) {
     return x;
 }
 
-// 1/b
+// 1/b.  The mantissa reciprocal at half precision seeds one cubic (Halley) step at
+// full precision: with t = 1 - bn x, x' = x (1 + t + t^2) has error O(t^3).
 template <int N>
 MLHD mlf<N> ml_recip(const mlf<N> &b) {
     if (ml_is_zero(b)) return ml_zero<N>();  // caller guards; no IEEE infinities in this format
@@ -498,8 +499,18 @@ MLHD mlf<N> ml_recip(const mlf<N> &b) {
     bn.e = 0;
     bn.s = 0;
     const mlf<N> one = ml_one<N>();
-    mlf<N> x = ml_recip_mant<N>(bn);
-    x = ml_add(x, ml_mul(x, ml_sub(one, ml_mul(bn, x))));  // final step at full precision
+    mlf<N> x;
+    if constexpr (N <= 2) {
+        x = ml_recip_mant<N>(bn);
+        x = ml_add(x, ml_mul(x, ml_sub(one, ml_mul(bn, x))));
+    } else {
+        x = ml_widen<N, N / 2>(ml_recip_mant<N / 2>(ml_narrow<N / 2, N>(bn)));
+        const mlf<N> t = ml_sub(one, ml_mul(bn, x));  // ~2^-(16N), needs full precision
+        constexpr int H = N / 2 + 1;                  // the correction needs ~16N bits
+        const mlf<H> th = ml_narrow<H, N>(t);
+        const mlf<H> corr = ml_mul(ml_narrow<H, N>(x), ml_add(th, ml_mul(th, th)));
+        x = ml_add(x, ml_widen<N, H>(corr));
+    }
     x.e -= b.e;
     x.s = b.s;
     return x;
@@ -530,7 +541,8 @@ MLHD mlf<N> ml_rsqrt_mant(const mlf<N> &an) {
     return ml_add(y, ml_ldexp(ml_mul(y, t), -1));
 }
 
-// 1/sqrt(a), a > 0
+// 1/sqrt(a), a > 0.  Half-precision seed, then one cubic (Halley) step at full
+// precision: t = 1 - an y^2, y' = y (1 + t/2 + 3t^2/8), error O(t^3).
 template <int N>
 MLHD mlf<N> ml_rsqrt(const mlf<N> &a) {
     if (ml_is_zero(a) || a.s) return ml_zero<N>();
@@ -538,10 +550,22 @@ MLHD mlf<N> ml_rsqrt(const mlf<N> &a) {
     const int k = a.e >> 1;  // floor(e/2)
     mlf<N> an = a;
     an.e = a.e - 2 * k;  // 0 or 1
-    mlf<N> y = ml_rsqrt_mant<N>(an);
     const mlf<N> one = ml_one<N>();
-    const mlf<N> t = ml_sub(one, ml_mul(an, ml_mul(y, y)));
-    y = ml_add(y, ml_ldexp(ml_mul(y, t), -1));  // final step at full precision
+    mlf<N> y;
+    if constexpr (N <= 2) {
+        y = ml_rsqrt_mant<N>(an);
+        const mlf<N> t = ml_sub(one, ml_mul(an, ml_mul(y, y)));
+        y = ml_add(y, ml_ldexp(ml_mul(y, t), -1));
+    } else {
+        y = ml_widen<N, N / 2>(ml_rsqrt_mant<N / 2>(ml_narrow<N / 2, N>(an)));
+        const mlf<N> t = ml_sub(one, ml_mul(an, ml_mul(y, y)));
+        constexpr int H = N / 2 + 1;
+        const mlf<H> th = ml_narrow<H, N>(t);
+        const mlf<H> t2 = ml_mul(th, th);
+        // t/2 + 3t^2/8 = t/2 + (t^2 + t^2/2)/4
+        const mlf<H> poly = ml_add(ml_ldexp(th, -1), ml_ldexp(ml_add(t2, ml_ldexp(t2, -1)), -2));
+        y = ml_add(y, ml_widen<N, H>(ml_mul(ml_narrow<H, N>(y), poly)));
+    }
     y.e -= k;
     return y;
 }

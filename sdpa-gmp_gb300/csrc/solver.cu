@@ -43,7 +43,9 @@ class Solver final : public SolverBase {
     struct Blk {
         int n = 0;
         V *C, *X, *Z, *Zinv, *LX, *LZ, *Dx, *Dz, *Rm, *XRDZ, *W1, *W2, *Dres, *Lt, *F;
-        V *q, *qold, *r, *w, *tmp, *td, *te;
+        // Lanczos vectors and tridiagonal storage, one set per side (0: X, 1: Z)
+        V *q[2], *qold[2], *r[2], *w[2], *tmp[2], *td[2], *te[2], *sl[2];
+        V *SW1 = nullptr, *SW2 = nullptr;  // Z-side work matrices of the small-block eigenvalue path
         BlockDev<N> cons;
         std::vector<int> f1_owners_h;
         int *f1_owners = nullptr;
@@ -57,6 +59,11 @@ class Solver final : public SolverBase {
         setup(P);
     }
     ~Solver() override {
+        if (st2_) cudaStreamSynchronize(st2_);
+        if (st2_) cudaStreamDestroy(st2_);
+        if (ev_fork_) cudaEventDestroy(ev_fork_);
+        if (ev_join_) cudaEventDestroy(ev_join_);
+        if (pinned_) cudaFreeHost(pinned_);
         for (void *p : allocs_) cudaFree(p);
         for (auto &e : ev_) cudaEventDestroy(e);
         for (auto &e : prof_ev_) cudaEventDestroy(e);
@@ -279,13 +286,20 @@ class Solver final : public SolverBase {
             B.f1_owners = upload_new(B.f1_owners_h);
             // Lanczos vectors; at most min(n, sqrt(n)+10) steps (sdpa_linear.cpp:43)
             B.lanczos_kmax = std::min(n, (int)sqrt((double)n) + 12) + 2;
-            B.q = dalloc(n);
-            B.qold = dalloc(n);
-            B.r = dalloc(n);
-            B.w = dalloc(n);
-            B.tmp = dalloc(n);
-            B.td = dalloc(std::max(B.lanczos_kmax, n) + 2);
-            B.te = dalloc(std::max(B.lanczos_kmax, n) + 2);
+            for (int side = 0; side < 2; ++side) {
+                B.q[side] = dalloc(n);
+                B.qold[side] = dalloc(n);
+                B.r[side] = dalloc(n);
+                B.w[side] = dalloc(n);
+                B.tmp[side] = dalloc(n);
+                B.td[side] = dalloc(std::max(B.lanczos_kmax, n) + 2);
+                B.te[side] = dalloc(std::max(B.lanczos_kmax, n) + 2);
+                B.sl[side] = dalloc(8);
+            }
+            if (n <= 20) {
+                B.SW1 = dalloc(nn);
+                B.SW2 = dalloc(nn);
+            }
             // workspace need
             max_ws = std::max(max_ws, gemm_bytes(n, n, n, 1));
             const int chunk = f1_chunk(B);
@@ -301,6 +315,13 @@ class Solver final : public SolverBase {
         }
         max_ws = std::max(max_ws, gemm_bytes(m_, m_, 32, 1));
         ws_.reserve(max_ws + (64u << 20));
+        ws2_.reserve(max_ws + (64u << 20));
+        SDPG_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
+        SDPG_CUDA(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
+        SDPG_CUDA(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
+        SDPG_CUDA(cudaMallocHost(&pinned_, kPinned * sizeof(V)));
+        info2_ = (int *)dalloc_raw(sizeof(int) * (4 * blk_.size() + 16));
+        info_all_ = (int *)dalloc_raw(sizeof(int) * (4 * blk_.size() + 16));
         ev_.resize(2);
         for (auto &e : ev_) SDPG_CUDA(cudaEventCreate(&e));
     }
@@ -369,6 +390,10 @@ class Solver final : public SolverBase {
 
     // C = alpha * op(A) * op(B) + beta * C on n x n blocks (Lal::multiply -> Rgemm)
     void mm(int n, V *C, const V *A, char ta, const V *Bm, char tb, const R &alpha = R(1), const R &beta = R(0)) {
+        mm_on(st_, ws_, n, C, A, ta, Bm, tb, alpha, beta);
+    }
+    void mm_on(cudaStream_t st, Workspace &ws, int n, V *C, const V *A, char ta, const V *Bm, char tb,
+               const R &alpha = R(1), const R &beta = R(0)) {
         GemmProblem<N> p{};
         p.M = n;
         p.Nn = n;
@@ -381,9 +406,10 @@ class Solver final : public SolverBase {
         p.sc = 0;
         p.alpha = alpha.v;
         p.beta = beta.v;
-        gemm(p);
+        gemm(p, st, ws);
     }
-    void gemm(const GemmProblem<N> &p0) {
+    void gemm(const GemmProblem<N> &p0) { gemm(p0, st_, ws_); }
+    void gemm(const GemmProblem<N> &p0, cudaStream_t st, Workspace &ws) {
         GemmProblem<N> p = p0;
         if (prof_on_) {
             if (prof_used_ * 2 + 2 > (int)prof_ev_.size()) {
@@ -400,9 +426,9 @@ class Solver final : public SolverBase {
             ++prof_launches_;
             prof_macs_ += (long long)p.M * p.Nn * p.K * p.batch;
         }
-        const size_t mark = ws_.used;
-        ml_gemm<N>(p, ws_, st_);
-        ws_.used = mark;
+        const size_t mark = ws.used;
+        ml_gemm<N>(p, ws, st);
+        ws.used = mark;
         gemm_macs_ += (long long)p.M * p.Nn * p.K * p.batch;
     }
     // ret = sum over blocks of A_l . B_l  (Lal::let(ret,'=',A,'.',B) on DenseLinearSpace)
@@ -604,96 +630,185 @@ class Solver final : public SolverBase {
 
     // ---------------------------------------------------------------- eigenvalues (sdpa_jordan.cpp, sdpa_linear.cpp)
 
-    // Lal::getMinEigen (Lanczos), sdpa_linear.cpp:27-124; L = invCholesky block, Xm = direction block
-    R lanczos_min(Blk &B, V *L, V *Xm) {
-        const int n = B.n;
-        R min(1.0e+51), min_old(1.0e+52), error(1.0e+10);
-        k_transpose<N>(n, L, B.Lt, st_);
-        // r = 1, q = 0
+    // One Lanczos run (Lal::getMinEigen, sdpa_linear.cpp:27-124) on L Xm L^T for one block
+    // and side; the host keeps the reference's loop control, the device does the rest.
+    struct Lz {
+        Blk *B;
+        int side, n, k, kk;
+        V *L, *Xm, *Lt;
+        cudaStream_t st;
+        Workspace *ws;
+        V *hp;  // 8 pinned slots: 0 rb, 1 beta, 2 te[k], 4 lambda, 5 z, 6 r.r
+        R min, min_old, error, beta, sq_n, sq_n9;
+        bool active, issued, eig;
+    };
+
+    void lanczos_issue(Lz &t) {
+        Blk &B = *t.B;
+        const int n = t.n, s = t.side;
+        V *sl = B.sl[s];
+        t.hp[0] = (R(1) / t.beta).v;  // value = MONE / beta
+        t.hp[1] = t.beta.v;
+        h2d_ += 2 * (long long)sizeof(V);
+        SDPG_CUDA(cudaMemcpyAsync(sl + 0, t.hp + 0, 2 * sizeof(V), cudaMemcpyHostToDevice, t.st));
+        k_lanczos_next<N>(n, B.r[s], sl + 0, B.q[s], B.qold[s], t.st);  // qold = q; q = r / beta
+        k_matvec<N>(n, t.L, 'T', 1, B.q[s], B.w[s], t.st);              // w = L^T q
+        k_matvec<N>(n, t.Xm, 'T', 0, B.w[s], B.tmp[s], t.st);           // tmp = X w (X symmetric)
+        k_matvec<N>(n, t.Lt, 'T', 2, B.tmp[s], B.w[s], t.st);           // w = L tmp
         {
-            const V one = ml_one<N>();
-            std::vector<V> h(n, one);
-            h2d_ += (long long)n * (long long)sizeof(V);
-            SDPG_CUDA(cudaMemcpyAsync(B.r, h.data(), n * sizeof(V), cudaMemcpyHostToDevice, st_));
-            SDPG_CUDA(cudaMemsetAsync(B.q, 0, n * sizeof(V), st_));
-            SDPG_CUDA(cudaStreamSynchronize(st_));
+            const size_t mark = t.ws->used;
+            k_dot<N>(n, B.q[s], B.w[s], B.td[s] + t.k, *t.ws, t.st);  // alpha = q . w -> diagVec[k]
+            t.ws->used = mark;
         }
-        R beta = rsqrt_(R(n));
-        const R sq_n = rsqrt_(R(n));
-        const R sq_n9 = rsqrt_(R(n) + R(9));
-        int k = 0, kk = 0;
-        while (k < n && R(k) < sq_n + R(10) && beta > R(1.0e-16) &&
-               (rabs(min - min_old) > R(1.0e-5) * rabs(min) + R(1.0e-8) ||
-                rabs(error * beta) > R(1.0e-2) * rabs(min) + R(1.0e-4))) {
-            if (k + 1 >= B.lanczos_kmax) break;
-            const R rb = R(1) / beta;  // value = MONE / beta
-            {
-                V *rbd = slot_ + 40;
-                h2d_ += (long long)sizeof(V);
-                SDPG_CUDA(cudaMemcpyAsync(rbd, &rb.v, sizeof(V), cudaMemcpyHostToDevice, st_));
-                k_lanczos_next<N>(n, B.r, rbd, B.q, B.qold, st_);  // qold = q; q = r / beta
-            }
-            k_matvec<N>(n, L, 'T', 1, B.q, B.w, st_);       // w = L^T q
-            k_matvec<N>(n, Xm, 'T', 0, B.w, B.tmp, st_);    // tmp = X w (X symmetric)
-            k_matvec<N>(n, B.Lt, 'T', 2, B.tmp, B.w, st_);  // w = L tmp
-            {
-                const size_t mark = ws_.used;
-                k_dot<N>(n, B.q, B.w, B.td + k, ws_, st_);  // alpha = q . w -> diagVec[k]
-                ws_.used = mark;
-            }
-            {
-                V *bd = slot_ + 41;
-                h2d_ += (long long)sizeof(V);
-                SDPG_CUDA(cudaMemcpyAsync(bd, &beta.v, sizeof(V), cudaMemcpyHostToDevice, st_));
-                k_lanczos_update<N>(n, B.w, B.q, B.qold, B.td + k, bd, B.r, st_);
-            }
-            const bool eig = R(kk) >= rsqrt_(R(k)) || k == n - 1 || R(k) > sq_n9;
-            if (eig) {
-                kk = 0;
-                k_tridiag_min<N>(k + 1, B.td, B.te, slot_ + 42, status_, st_);
-            }
-            {
-                const size_t mark = ws_.used;
-                k_dot<N>(n, B.r, B.r, slot_ + 44, ws_, st_);  // value = r . r
-                ws_.used = mark;
-            }
-            std::vector<V> h(5);
-            d2h_ += 3 * (long long)sizeof(V);
-            SDPG_CUDA(cudaMemcpyAsync(h.data(), slot_ + 42, 3 * sizeof(V), cudaMemcpyDeviceToHost, st_));
-            SDPG_CUDA(cudaStreamSynchronize(st_));
-            if (eig) {
-                min_old = min;
-                min = R(h[0]);
-                error = R(h[1]);
-            }
-            beta = rsqrt_(R(h[2]));
-            h2d_ += (long long)sizeof(V);
-            SDPG_CUDA(cudaMemcpyAsync(B.te + k, &beta.v, sizeof(V), cudaMemcpyHostToDevice, st_));  // diagVec2[k]
-            SDPG_CUDA(cudaStreamSynchronize(st_));
-            ++k;
-            ++kk;
+        k_lanczos_update<N>(n, B.w[s], B.q[s], B.qold[s], B.td[s] + t.k, sl + 1, B.r[s], t.st);
+        t.eig = R(t.kk) >= rsqrt_(R(t.k)) || t.k == n - 1 || R(t.k) > t.sq_n9;
+        if (t.eig) {
+            t.kk = 0;
+            k_tridiag_min<N>(t.k + 1, B.td[s], B.te[s], sl + 4, status_, t.st);
         }
-        return min - rabs(error * beta);
+        {
+            const size_t mark = t.ws->used;
+            k_dot<N>(n, B.r[s], B.r[s], sl + 6, *t.ws, t.st);  // value = r . r
+            t.ws->used = mark;
+        }
+        d2h_ += 3 * (long long)sizeof(V);
+        SDPG_CUDA(cudaMemcpyAsync(t.hp + 4, sl + 4, 3 * sizeof(V), cudaMemcpyDeviceToHost, t.st));
+        t.issued = true;
     }
 
-    // Lal::getMinEigenValue on L*X*L^T for blocks of size <= 20 (sdpa_jordan.cpp:63-68)
-    R small_min(Blk &B, V *L, V *Xm) {
+    void lanczos_finish_step(Lz &t) {
+        Blk &B = *t.B;
+        if (t.eig) {
+            t.min_old = t.min;
+            t.min = R(t.hp[4]);
+            t.error = R(t.hp[5]);
+        }
+        t.beta = rsqrt_(R(t.hp[6]));
+        t.hp[2] = t.beta.v;
+        h2d_ += (long long)sizeof(V);
+        SDPG_CUDA(cudaMemcpyAsync(B.te[t.side] + t.k, t.hp + 2, sizeof(V), cudaMemcpyHostToDevice, t.st));  // diagVec2[k]
+        ++t.k;
+        ++t.kk;
+        t.issued = false;
+    }
+
+    // all Lanczos runs advance in lockstep: one host synchronisation per step for all of them
+    void lanczos_all(std::vector<Lz> &T) {
+        if (8 * T.size() > (size_t)kPinned) throw sdpg_error(SDPG_ERR_TOO_LARGE, "too many Lanczos runs at once");
+        for (size_t i = 0; i < T.size(); ++i) {
+            Lz &t = T[i];
+            Blk &B = *t.B;
+            t.hp = pinned_ + 8 * i;
+            k_transpose<N>(t.n, t.L, t.Lt, t.st);
+            k_fill<N>(t.n, B.r[t.side], ml_one<N>(), t.st);
+            SDPG_CUDA(cudaMemsetAsync(B.q[t.side], 0, t.n * sizeof(V), t.st));
+            t.min = R(1.0e+51);
+            t.min_old = R(1.0e+52);
+            t.error = R(1.0e+10);
+            t.beta = rsqrt_(R(t.n));  // norm of r
+            t.sq_n = t.beta;
+            t.sq_n9 = rsqrt_(R(t.n) + R(9));
+            t.k = t.kk = 0;
+            t.active = true;
+            t.issued = false;
+        }
+        while (true) {
+            bool any = false;
+            for (Lz &t : T) {
+                if (!t.active) continue;
+                const bool go = t.k < t.n && R(t.k) < t.sq_n + R(10) && t.beta > R(1.0e-16) &&
+                                (rabs(t.min - t.min_old) > R(1.0e-5) * rabs(t.min) + R(1.0e-8) ||
+                                 rabs(t.error * t.beta) > R(1.0e-2) * rabs(t.min) + R(1.0e-4));
+                if (!go || t.k + 1 >= t.B->lanczos_kmax) {
+                    t.active = false;
+                    continue;
+                }
+                lanczos_issue(t);
+                any = true;
+            }
+            if (!any) break;
+            SDPG_CUDA(cudaStreamSynchronize(st_));
+            SDPG_CUDA(cudaStreamSynchronize(st2_));
+            for (Lz &t : T)
+                if (t.issued) lanczos_finish_step(t);
+        }
+        SDPG_CUDA(cudaStreamSynchronize(st_));
+        SDPG_CUDA(cudaStreamSynchronize(st2_));
+    }
+
+    // Lal::getMinEigenValue on L*X*L^T for blocks of size <= 20 (sdpa_jordan.cpp:63-68):
+    // enqueue only; the value lands in B.sl[side][4]
+    void small_min_issue(Blk &B, int side, V *L, V *Xm, cudaStream_t st, Workspace &ws) {
         const int n = B.n;
-        mm(n, B.W2, Xm, 'N', L, 'T');
-        mm(n, B.W1, L, 'N', B.W2, 'N');
-        k_tridiagonalize_small<N>(n, B.W1, B.td, B.te, st_);
-        k_tridiag_min<N>(n, B.td, B.te, slot_ + 42, status_, st_);
-        return fetch1(slot_ + 42);
+        V *w1 = side == 0 ? B.W1 : B.SW1;
+        V *w2 = side == 0 ? B.W2 : B.SW2;
+        mm_on(st, ws, n, w2, Xm, 'N', L, 'T');
+        mm_on(st, ws, n, w1, L, 'N', w2, 'N');
+        k_tridiagonalize_small<N>(n, w1, B.td[side], B.te[side], st);
+        k_tridiag_min<N>(n, B.td[side], B.te[side], B.sl[side] + 4, status_, st);
     }
 
-    // Jal::getMinEigen(lMat, xMat), sdpa_jordan.cpp:55-88
-    R getMinEigen(V *Blk::*L, V *Blk::*Xm) {
-        R mn(1.0E50);
+    // Jal::getMinEigen(L_X^-1, dX) and Jal::getMinEigen(L_Z^-1, dZ) (sdpa_jordan.cpp:55-88),
+    // both sides and all blocks at once: the X side on the main stream, the Z side on the
+    // second stream.
+    void min_eigen_both(R *minX, R *minZ) {
+        // the Z side reads dZ / L_Z^-1 written on the main stream
+        SDPG_CUDA(cudaEventRecord(ev_fork_, st_));
+        SDPG_CUDA(cudaStreamWaitEvent(st2_, ev_fork_, 0));
+        std::vector<Lz> T;
         for (auto &B : blk_) {
-            const R v = (B.n > 20) ? lanczos_min(B, B.*L, B.*Xm) : small_min(B, B.*L, B.*Xm);
-            if (v < mn) mn = v;
+            for (int side = 0; side < 2; ++side) {
+                V *L = side == 0 ? B.LX : B.LZ;
+                V *Xm = side == 0 ? B.Dx : B.Dz;
+                cudaStream_t st = side == 0 ? st_ : st2_;
+                Workspace &ws = side == 0 ? ws_ : ws2_;
+                if (B.n > 20) {
+                    Lz t{};
+                    t.B = &B;
+                    t.side = side;
+                    t.n = B.n;
+                    t.L = L;
+                    t.Xm = Xm;
+                    t.Lt = side == 0 ? B.Lt : B.F;
+                    t.st = st;
+                    t.ws = &ws;
+                    T.push_back(t);
+                } else {
+                    small_min_issue(B, side, L, Xm, st, ws);
+                }
+            }
         }
-        return mn;
+        lanczos_all(T);
+        *minX = R(1.0E50);
+        *minZ = R(1.0E50);
+        // small-block results
+        std::vector<V> h(2 * blk_.size());
+        for (size_t l = 0; l < blk_.size(); ++l)
+            if (blk_[l].n <= 20)
+                for (int side = 0; side < 2; ++side) {
+                    d2h_ += (long long)sizeof(V);
+                    SDPG_CUDA(cudaMemcpy(&h[2 * l + side], blk_[l].sl[side] + 4, sizeof(V), cudaMemcpyDeviceToHost));
+                }
+        size_t ti = 0;
+        for (size_t l = 0; l < blk_.size(); ++l) {
+            for (int side = 0; side < 2; ++side) {
+                R v;
+                if (blk_[l].n > 20) {
+                    const Lz &t = T[ti++];
+                    v = t.min - rabs(t.error * t.beta);
+                } else {
+                    v = R(h[2 * l + side]);
+                }
+                R &target = side == 0 ? *minX : *minZ;
+                if (v < target) target = v;
+            }
+        }
+    }
+
+    R getMinEigen(V *Blk::*L, V *Blk::*Xm) {
+        R mx, mz;
+        min_eigen_both(&mx, &mz);
+        return (L == &Blk::LX) ? mx : mz;
     }
 
     // ---------------------------------------------------------------- step length (sdpa_parts.cpp)
@@ -701,10 +816,10 @@ class Solver final : public SolverBase {
     // StepLength::computeStepLength, sdpa_parts.cpp:298-360
     void computeStepLength() {
         const R alphaBD(100.0);
-        const R minX = getMinEigen(&Blk::LX, &Blk::Dx);
+        R minX, minZ;
+        min_eigen_both(&minX, &minZ);
         if (-minX > R(1.0) / alphaBD) aP_ = -R(1.0) / minX;
         else aP_ = alphaBD;
-        const R minZ = getMinEigen(&Blk::LZ, &Blk::Dz);
         if (-minZ > R(1.0) / alphaBD) aD_ = -R(1.0) / minZ;
         else aD_ = alphaBD;
     }
@@ -800,30 +915,36 @@ class Solver final : public SolverBase {
 
     // ---------------------------------------------------------------- iterate update (sdpa_dataset.cpp)
 
-    // Jal::getInvChol / getInvCholAndInv (sdpa_jordan.cpp:123-171) for one block
-    bool inv_chol(Blk &B, V *A, V *Linv, V *Inv) {
+    // Jal::getInvChol / getInvCholAndInv (sdpa_jordan.cpp:123-171) for one block, enqueued
+    // on `st`: factor a copy of A (Lal::getCholesky), invert the factor, optionally form
+    // Inv = Linv^T Linv (Rtrmm).  A failed factorisation leaves its column in *info.
+    void inv_chol_issue(Blk &B, V *A, V *Fbuf, V *Linv, V *Inv, int *info, cudaStream_t st, Workspace &ws) {
         const int n = B.n;
-        k_copy<N>((long long)n * n, A, B.F, st_);
-        ml_potrf<N>(n, B.F, n, info_, ws_, st_);
-        int info = 0;
-        d2h_ += (long long)sizeof(int);
-            SDPG_CUDA(cudaMemcpyAsync(&info, info_, sizeof(int), cudaMemcpyDeviceToHost, st_));
-        SDPG_CUDA(cudaStreamSynchronize(st_));
-        if (info != 0) return false;
-        k_zero_strict_upper<N>(n, B.F, st_);
-        ml_trtri_lower<N>(n, B.F, n, Linv, ws_, st_);
-        if (Inv) mm(n, Inv, Linv, 'T', Linv, 'N');  // Rtrmm: Inv = Linv^T * Linv
-        return true;
+        k_copy<N>((long long)n * n, A, Fbuf, st);
+        ml_potrf<N>(n, Fbuf, n, info, ws, st);
+        k_zero_strict_upper<N>(n, Fbuf, st);
+        ml_trtri_lower<N>(n, Fbuf, n, Linv, ws, st);
+        if (Inv) mm_on(st, ws, n, Inv, Linv, 'T', Linv, 'N');
     }
 
-    // Solutions::computeInverse, sdpa_dataset.cpp:96-118
+    // Solutions::computeInverse, sdpa_dataset.cpp:96-118: the X and Z chains are
+    // independent and run concurrently (X on the main stream, Z on the second stream).
     bool computeInverse() {
-        bool ok = true;
-        for (auto &B : blk_)
-            if (!inv_chol(B, B.X, B.LX, nullptr)) ok = false;
-        for (auto &B : blk_)
-            if (!inv_chol(B, B.Z, B.LZ, B.Zinv)) ok = false;
-        return ok;
+        const size_t nb = blk_.size();
+        SDPG_CUDA(cudaEventRecord(ev_fork_, st_));
+        SDPG_CUDA(cudaStreamWaitEvent(st2_, ev_fork_, 0));
+        for (size_t l = 0; l < nb; ++l) inv_chol_issue(blk_[l], blk_[l].X, blk_[l].F, blk_[l].LX, nullptr, info_all_ + l, st_, ws_);
+        for (size_t l = 0; l < nb; ++l)
+            inv_chol_issue(blk_[l], blk_[l].Z, blk_[l].W2, blk_[l].LZ, blk_[l].Zinv, info_all_ + nb + l, st2_, ws2_);
+        SDPG_CUDA(cudaEventRecord(ev_join_, st2_));
+        SDPG_CUDA(cudaStreamWaitEvent(st_, ev_join_, 0));
+        std::vector<int> info(2 * nb);
+        d2h_ += (long long)(2 * nb * sizeof(int));
+        SDPG_CUDA(cudaMemcpyAsync(info.data(), info_all_, 2 * nb * sizeof(int), cudaMemcpyDeviceToHost, st_));
+        SDPG_CUDA(cudaStreamSynchronize(st_));
+        for (int v : info)
+            if (v != 0) return false;
+        return true;
     }
 
     // Solutions::update, sdpa_dataset.cpp:120-143
@@ -1216,7 +1337,12 @@ class Solver final : public SolverBase {
   private:
     Param par_;
     cudaStream_t st_;
-    Workspace ws_;
+    Workspace ws_, ws2_;  // ws2_ serves work issued on the second stream
+    cudaStream_t st2_ = nullptr;
+    cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
+    static constexpr int kPinned = 4096;
+    V *pinned_ = nullptr;  // page-locked staging for per-step scalars
+    int *info2_ = nullptr, *info_all_ = nullptr;
     std::vector<Blk> blk_;
     int m_ = 0, nDim_ = 0;
     std::vector<V> b_h_;
