@@ -110,62 +110,89 @@ __global__ void trtri_diag_kernel(const mlf<N> *L, int ldl, mlf<N> *Linv, int ld
     }
 }
 
+// Inverses of the NB x NB diagonal blocks of the lower-triangular L, packed:
+// Dinv[b] (ld NB, lower, zeros above) = L[bNB:, bNB:]^{-1} restricted to the block.
 template <int N>
-__global__ void recip_diag_kernel(int n, const mlf<N> *L, int ldl, mlf<N> *rinv) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) rinv[i] = ml_recip(L[i + (long long)i * ldl]);
-}
-
-// x := L^{-T} L^{-1} x in one CTA, blocked by NB: warp 0 solves each diagonal block
-// (one lane per row, pivots broadcast by shuffle), then every thread updates one of
-// the remaining rows with the block's NB solved entries.
-template <int N>
-__global__ void potrs_kernel(int n, const mlf<N> *L, int ldl, const mlf<N> *rinv, mlf<N> *x) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // forward: L y = x
-    for (int k0 = 0; k0 < n; k0 += NB) {
-        const int kb = min(NB, n - k0);
-        if (warp == 0) {
-            mlf<N> a = lane < kb ? x[k0 + lane] : ml_zero<N>();
-            for (int j = 0; j < kb; ++j) {
-                mlf<N> xj = ml_zero<N>();
-                if (lane == j) xj = ml_mul(a, rinv[k0 + j]);
-                xj = ml_shfl(xj, j);
-                if (lane == j) a = xj;
-                if (lane > j && lane < kb) a = ml_sub(a, ml_mul(L[(k0 + lane) + (long long)(k0 + j) * ldl], xj));
-            }
-            if (lane < kb) x[k0 + lane] = a;
+__global__ void trtri_diag_packed_kernel(const mlf<N> *L, int ldl, mlf<N> *Dinv, int n) {
+    const int b = blockIdx.x;
+    const int o = b * NB;
+    const int kb = min(NB, n - o);
+    const mlf<N> *T = L + o + (long long)o * ldl;
+    mlf<N> *X = Dinv + (long long)b * NB * NB;
+    __shared__ mlf<N> rv[NB];
+    if (threadIdx.x < kb) rv[threadIdx.x] = ml_recip(T[threadIdx.x + (long long)threadIdx.x * ldl]);
+    for (int q = threadIdx.x; q < NB * NB; q += blockDim.x) {
+        const int i = q % NB, c = q / NB;
+        X[i + NB * c] = (i == c && i < kb) ? ml_one<N>() : ml_zero<N>();
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; ++j) {
+        for (int c = threadIdx.x; c <= j; c += blockDim.x) X[j + NB * c] = ml_mul(X[j + NB * c], rv[j]);
+        __syncthreads();
+        const int rows = kb - j - 1, cols = j + 1;
+        for (int q = threadIdx.x; q < rows * cols; q += blockDim.x) {
+            const int i = j + 1 + q % rows, c = q / rows;
+            mlf<N> *x = X + i + NB * c;
+            *x = ml_sub(*x, ml_mul(T[i + (long long)j * ldl], X[j + NB * c]));
         }
         __syncthreads();
+    }
+}
+
+// sum_{j<cnt} a[j*stride] * y[j] with four independent accumulator chains
+template <int N>
+__device__ __forceinline__ mlf<N> dot_ld(const mlf<N> *a, long long stride, const mlf<N> *y, int cnt) {
+    mlf<N> a0 = ml_zero<N>(), a1 = ml_zero<N>(), a2 = ml_zero<N>(), a3 = ml_zero<N>();
+    int j = 0;
+    for (; j + 3 < cnt; j += 4) {
+        a0 = ml_add(a0, ml_mul(a[j * stride], y[j]));
+        a1 = ml_add(a1, ml_mul(a[(j + 1) * stride], y[j + 1]));
+        a2 = ml_add(a2, ml_mul(a[(j + 2) * stride], y[j + 2]));
+        a3 = ml_add(a3, ml_mul(a[(j + 3) * stride], y[j + 3]));
+    }
+    for (; j < cnt; ++j) a0 = ml_add(a0, ml_mul(a[j * stride], y[j]));
+    return ml_add(ml_add(a0, a1), ml_add(a2, a3));
+}
+
+// x := L^{-T} L^{-1} x in one CTA (512 threads at 256 bits, 256 at 512 bits), blocked by NB with the inverted
+// diagonal blocks: each block solve is a small matrix-vector product (one warp per
+// output, a lane per term, tree-summed), then every thread updates one remaining row.
+template <int N>
+__global__ void __launch_bounds__(N <= 8 ? 512 : 256) potrs_blocked_kernel(int n, const mlf<N> *L, int ldl, const mlf<N> *Dinv, mlf<N> *x) {
+    __shared__ mlf<N> ys[NB];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const int nblk = (n + NB - 1) / NB;
+    // forward: L y = x
+    for (int b = 0; b < nblk; ++b) {
+        const int k0 = b * NB, kb = min(NB, n - k0);
+        const mlf<N> *D = Dinv + (long long)b * NB * NB;
+        for (int w = warp; w < kb; w += nwarps) {
+            mlf<N> p = (lane <= w && lane < kb) ? ml_mul(D[w + NB * lane], x[k0 + lane]) : ml_zero<N>();
+            p = ml_warp_sum(p);
+            if (lane == 0) ys[w] = p;
+        }
+        __syncthreads();
+        if (tid < kb) x[k0 + tid] = ys[tid];
         for (int i = k0 + kb + tid; i < n; i += blockDim.x) {
-            mlf<N> acc[4] = {ml_zero<N>(), ml_zero<N>(), ml_zero<N>(), ml_zero<N>()};
-            for (int j = 0; j < kb; ++j)
-                acc[j & 3] = ml_add(acc[j & 3], ml_mul(L[i + (long long)(k0 + j) * ldl], x[k0 + j]));
-            x[i] = ml_sub(x[i], ml_add(ml_add(acc[0], acc[1]), ml_add(acc[2], acc[3])));
+            const mlf<N> *Li = L + i + (long long)k0 * ldl;
+            x[i] = ml_sub(x[i], dot_ld<N>(Li, ldl, ys, kb));
         }
         __syncthreads();
     }
     // backward: L^T z = y
-    const int nblk = (n + NB - 1) / NB;
-    for (int bI = nblk - 1; bI >= 0; --bI) {
-        const int k0 = bI * NB, kb = min(NB, n - k0);
-        if (warp == 0) {
-            mlf<N> a = lane < kb ? x[k0 + lane] : ml_zero<N>();
-            for (int j = kb - 1; j >= 0; --j) {
-                mlf<N> zj = ml_zero<N>();
-                if (lane == j) zj = ml_mul(a, rinv[k0 + j]);
-                zj = ml_shfl(zj, j);
-                if (lane == j) a = zj;
-                if (lane < j) a = ml_sub(a, ml_mul(L[(k0 + j) + (long long)(k0 + lane) * ldl], zj));
-            }
-            if (lane < kb) x[k0 + lane] = a;
+    for (int b = nblk - 1; b >= 0; --b) {
+        const int k0 = b * NB, kb = min(NB, n - k0);
+        const mlf<N> *D = Dinv + (long long)b * NB * NB;
+        for (int w = warp; w < kb; w += nwarps) {
+            mlf<N> p = (lane >= w && lane < kb) ? ml_mul(D[lane + NB * w], x[k0 + lane]) : ml_zero<N>();
+            p = ml_warp_sum(p);
+            if (lane == 0) ys[w] = p;
         }
         __syncthreads();
+        if (tid < kb) x[k0 + tid] = ys[tid];
         for (int i = tid; i < k0; i += blockDim.x) {
-            mlf<N> acc[4] = {ml_zero<N>(), ml_zero<N>(), ml_zero<N>(), ml_zero<N>()};
-            for (int j = 0; j < kb; ++j)
-                acc[j & 3] = ml_add(acc[j & 3], ml_mul(L[(k0 + j) + (long long)i * ldl], x[k0 + j]));
-            x[i] = ml_sub(x[i], ml_add(ml_add(acc[0], acc[1]), ml_add(acc[2], acc[3])));
+            const mlf<N> *Li = L + k0 + (long long)i * ldl;
+            x[i] = ml_sub(x[i], dot_ld<N>(Li, 1, ys, kb));
         }
         __syncthreads();
     }
@@ -250,20 +277,38 @@ void ml_trtri_lower(int n, const mlf<N> *L, int ldl, mlf<N> *Linv, Workspace &ws
 }
 
 template <int N>
+size_t ml_potrs_prepare_bytes(int n) {
+    return (size_t)ceil_div(n, NB) * NB * NB * sizeof(mlf<N>);
+}
+
+template <int N>
+void ml_potrs_prepare(int n, const mlf<N> *L, int ldl, mlf<N> *Dinv, cudaStream_t s) {
+    trtri_diag_packed_kernel<N><<<ceil_div(n, NB), 256, 0, s>>>(L, ldl, Dinv, n);
+    SDPG_CHECK_LAUNCH();
+}
+
+template <int N>
+void ml_potrs_solve(int n, const mlf<N> *L, int ldl, const mlf<N> *Dinv, mlf<N> *x, cudaStream_t s) {
+    potrs_blocked_kernel<N><<<1, N <= 8 ? 512 : 256, 0, s>>>(n, L, ldl, Dinv, x);
+    SDPG_CHECK_LAUNCH();
+}
+
+template <int N>
 void ml_potrs(int n, const mlf<N> *L, int ldl, mlf<N> *x, Workspace &ws, cudaStream_t s) {
     const size_t mark = ws.used;
-    mlf<N> *rinv = (mlf<N> *)ws.carve((size_t)n * sizeof(mlf<N>));
-    recip_diag_kernel<N><<<ceil_div(n, 128), 128, 0, s>>>(n, L, ldl, rinv);
-    SDPG_CHECK_LAUNCH();
-    potrs_kernel<N><<<1, 512, 0, s>>>(n, L, ldl, rinv, x);
-    SDPG_CHECK_LAUNCH();
+    mlf<N> *Dinv = (mlf<N> *)ws.carve(ml_potrs_prepare_bytes<N>(n));
+    ml_potrs_prepare<N>(n, L, ldl, Dinv, s);
+    ml_potrs_solve<N>(n, L, ldl, Dinv, x, s);
     ws.used = mark;
 }
 
 #define SDPG_INST_CHOL(N)                                                                       \
     template void ml_potrf<N>(int, mlf<N> *, int, int *, Workspace &, cudaStream_t);            \
     template void ml_trtri_lower<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t); \
-    template void ml_potrs<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t);
+    template void ml_potrs<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t);             \
+    template size_t ml_potrs_prepare_bytes<N>(int);                                                        \
+    template void ml_potrs_prepare<N>(int, const mlf<N> *, int, mlf<N> *, cudaStream_t);                    \
+    template void ml_potrs_solve<N>(int, const mlf<N> *, int, const mlf<N> *, mlf<N> *, cudaStream_t);
 SDPG_INST_CHOL(8)
 SDPG_INST_CHOL(16)
 

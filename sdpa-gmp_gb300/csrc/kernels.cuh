@@ -102,6 +102,14 @@ void ml_trtri_lower(int n, const mlf<N> *L, int ldl, mlf<N> *Linv, Workspace &ws
 // x = (L L^T)^{-1} x (two Rtrsv, Lal::solveSystems sdpa_linear.cpp:683-695)
 template <int N>
 void ml_potrs(int n, const mlf<N> *L, int ldl, mlf<N> *x, Workspace &ws, cudaStream_t s);
+// the same in two parts: invert the NB x NB diagonal blocks once per factor (Dinv holds
+// ml_potrs_prepare_bytes), then solve any number of right-hand sides with them
+template <int N>
+size_t ml_potrs_prepare_bytes(int n);
+template <int N>
+void ml_potrs_prepare(int n, const mlf<N> *L, int ldl, mlf<N> *Dinv, cudaStream_t s);
+template <int N>
+void ml_potrs_solve(int n, const mlf<N> *L, int ldl, const mlf<N> *Dinv, mlf<N> *x, cudaStream_t s);
 
 // ---- eigenvalues (eig.cu) ---------------------------------------------------------
 // y = op(A) x for a dense n x n A (op: 'N' plain, 'T' transpose; A lower-triangular

@@ -137,6 +137,7 @@ class Solver final : public SolverBase {
         g_ = dalloc(m_);
         p_ = dalloc(m_);
         B_ = dalloc((size_t)m_ * m_);
+        Bdinv_ = (V *)dalloc_raw(ml_potrs_prepare_bytes<N>(m_));
         upload(b_, bh.data(), m_);
         b_h_ = bh;
         info_ = (int *)dalloc_raw(64);
@@ -584,9 +585,10 @@ class Solver final : public SolverBase {
             SDPG_CUDA(cudaMemcpyAsync(&info, info_, sizeof(int), cudaMemcpyDeviceToHost, st_));
             SDPG_CUDA(cudaStreamSynchronize(st_));
             if (info != 0) return false;
+            ml_potrs_prepare<N>(m_, B_, m_, Bdinv_, st_);
         }
         k_copy<N>(m_, g_, Dy_, st_);
-        ml_potrs<N>(m_, B_, m_, Dy_, ws_, st_);
+        ml_potrs_solve<N>(m_, B_, m_, Bdinv_, Dy_, st_);
         return true;
     }
 
@@ -1346,6 +1348,7 @@ class Solver final : public SolverBase {
     std::vector<Blk> blk_;
     int m_ = 0, nDim_ = 0;
     std::vector<V> b_h_;
+    V *Bdinv_ = nullptr;  // inverted 32 x 32 diagonal blocks of the Schur factor
     V *b_ = nullptr, *y_ = nullptr, *Dy_ = nullptr, *g_ = nullptr, *p_ = nullptr, *B_ = nullptr, *slot_ = nullptr;
     int *info_ = nullptr, *status_ = nullptr;
     R muInit_, muCur_, thP_, thD_, aP_, aD_, betaV_, rho_, etaP_, etaD_, objP_, objD_, normP_, normD_;
