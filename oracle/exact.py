@@ -190,3 +190,100 @@ def max_rel_err(got: np.ndarray, exact, scale) -> float:
             continue
         worst = max(worst, d / s)
     return float(worst)
+
+
+# ---------------------------------------------------------------- factorisations and eigenvalues
+
+
+def matmul(A, B, m: int, n: int, k: int, lda: int, ldb: int, a_lower: bool = False,
+           b_lower: bool = False) -> list[tuple[int, int]]:
+    """Exact column-major m x n product of (m x k) A and (k x n) B; a triangular flag
+    skips the structural zeros (used to form L L^T, L X and L (L^T x) residuals of
+    Rpotrf, Rtrsm and Rtrsv, mplapack/Rpotrf.cpp, Rtrsm.cpp, Rtrsv.cpp)."""
+    out = []
+    for j in range(n):
+        for i in range(m):
+            lo, hi = 0, k
+            if a_lower:
+                hi = min(hi, i + 1)
+            if b_lower:
+                lo = max(lo, j)
+            out.append(dy_sum(dy_mul(A[i + t * lda], B[t + j * ldb]) for t in range(lo, hi)))
+    return out
+
+
+def max_abs(vals) -> Fraction:
+    return max((abs(to_fraction(v)) for v in vals), default=Fraction(0))
+
+
+def _to_int_scale(vals):
+    """Common exponent x and integers v_i with vals_i = v_i * 2**x."""
+    nz = [v for v in vals if v[0] != 0]
+    x = min((v[1] for v in nz), default=0)
+    return [(v[0] << (v[1] - x)) if v[0] else 0 for v in vals], x
+
+
+def count_below_tridiag(d, e, sigma: Fraction) -> int:
+    """Number of eigenvalues of tridiag(e, d, e) below sigma: sign changes of the
+    leading principal minors of T - sigma I (Sturm sequence), exact in rationals.
+    Restates the bisection count behind Rsteqr's ordering, mplapack/Rsteqr.cpp."""
+    p_prev, p = Fraction(1), to_fraction(d[0]) - sigma
+    changes = 1 if p < 0 else 0
+    if p == 0:
+        raise ValueError("sigma is an eigenvalue of a leading block")
+    for i in range(1, len(d)):
+        ei = to_fraction(e[i - 1])
+        p_prev, p = p, (to_fraction(d[i]) - sigma) * p - ei * ei * p_prev
+        if p == 0:
+            raise ValueError("sigma is an eigenvalue of a leading block")
+        if (p < 0) != (p_prev < 0):
+            changes += 1
+    return changes
+
+
+def tridiag_last_component_sq(d, e, lam: Fraction) -> Fraction:
+    """z_k^2 = p_{k-1}(lam) / p_k'(lam) for the unit eigenvector of tridiag(e, d, e)
+    belonging to the simple eigenvalue lam (p_i the leading minors of lam I - T)."""
+    k = len(d)
+    p_prev, p = Fraction(1), lam - to_fraction(d[0])
+    dp_prev, dp = Fraction(0), Fraction(1)
+    for i in range(1, k):
+        ei2 = to_fraction(e[i - 1]) ** 2
+        a = lam - to_fraction(d[i])
+        p_new = a * p - ei2 * p_prev
+        dp_new = p + a * dp - ei2 * dp_prev
+        p_prev, p, dp_prev, dp = p, p_new, dp, dp_new
+    return p_prev / dp
+
+
+def count_below_dense(A, n: int, sigma: Fraction) -> int:
+    """Number of eigenvalues of the symmetric n x n A (column-major, full storage)
+    below sigma, from the signs of the leading principal minors of A - sigma I
+    computed by fraction-free (Bareiss) elimination.  The reference obtains the
+    eigenvalues from Rsyev (mplapack/Rsyev.cpp); inertia pins the smallest one."""
+    num, den = sigma.numerator, sigma.denominator
+    if den & (den - 1):
+        raise ValueError("sigma must be dyadic")
+    vals, x = _to_int_scale(list(A))
+    sh = den.bit_length() - 1
+    t = max(-x, sh)  # M = (A - sigma I) * 2^t is integral
+    M = [[vals[i + j * n] << (x + t) for j in range(n)] for i in range(n)]
+    s_int = num << (t - sh)
+    for i in range(n):
+        M[i][i] -= s_int
+    prev = 1
+    changes = 0
+    sign_prev = 1
+    for k in range(n):
+        piv = M[k][k]
+        if piv == 0:
+            raise ValueError("zero leading minor")
+        sgn = 1 if piv > 0 else -1
+        if sgn != sign_prev:
+            changes += 1
+        sign_prev = sgn
+        for i in range(k + 1, n):
+            for j in range(k + 1, n):
+                M[i][j] = (M[i][j] * piv - M[i][k] * M[k][j]) // prev
+        prev = piv
+    return changes

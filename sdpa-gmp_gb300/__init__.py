@@ -200,6 +200,52 @@ def rgemm(transa: str, transb: str, m: int, n: int, k: int, alpha: np.ndarray, A
     return C
 
 
+def rpotrf(A: np.ndarray, n: int, lda: int) -> tuple[np.ndarray, int]:
+    """Lower Cholesky in place on a copy (Rpotrf "Lower"); returns (factor, info)."""
+    limbs = A.shape[1] - 2
+    A = np.array(A, copy=True, order="C")
+    info = ctypes.c_int(0)
+    check(lib().sdpg_rpotrf(limbs, n, A.ctypes.data, lda, ctypes.byref(info)))
+    return A, info.value
+
+
+def inv_lower(L: np.ndarray, n: int, ldl: int) -> np.ndarray:
+    """L^{-1} (n x n, ld n) of a lower-triangular L."""
+    limbs = L.shape[1] - 2
+    L = np.ascontiguousarray(L)
+    out = ml_empty(n * n, limbs)
+    check(lib().sdpg_inv_lower(limbs, n, L.ctypes.data, ldl, out.ctypes.data))
+    return out
+
+
+def solve_systems(L: np.ndarray, n: int, ldl: int, x: np.ndarray) -> np.ndarray:
+    """(L L^T)^{-1} x."""
+    limbs = L.shape[1] - 2
+    L = np.ascontiguousarray(L)
+    x = np.array(x, copy=True, order="C")
+    check(lib().sdpg_solve_systems(limbs, n, L.ctypes.data, ldl, x.ctypes.data))
+    return x
+
+
+def tridiag_min(d: np.ndarray, e: np.ndarray) -> np.ndarray:
+    """Smallest eigenvalue of tridiag(e, d, e) and the last component of its eigenvector."""
+    limbs = d.shape[1] - 2
+    d = np.ascontiguousarray(d)
+    e = np.ascontiguousarray(e if len(e) else ml_empty(1, limbs))
+    out = ml_empty(2, limbs)
+    check(lib().sdpg_tridiag_min(limbs, d.shape[0], d.ctypes.data, e.ctypes.data, out.ctypes.data))
+    return out
+
+
+def sym_min_eigen(A: np.ndarray, n: int) -> np.ndarray:
+    """Smallest eigenvalue of a dense symmetric n x n (n <= 64)."""
+    limbs = A.shape[1] - 2
+    A = np.ascontiguousarray(A)
+    out = ml_empty(2, limbs)
+    check(lib().sdpg_sym_min_eigen(limbs, n, A.ctypes.data, out.ctypes.data))
+    return out[:1]
+
+
 PHASES = ["noINFO", "pFEAS", "dFEAS", "pdFEAS", "pdINF", "pFEAS_dINF", "pINF_dFEAS", "pdOPT", "pUNBD",
           "dUNBD"]
 INFO_KEYS = ["phase", "iteration", "objValPrimal", "objValDual", "mu", "relative gap", "p.feas.error",

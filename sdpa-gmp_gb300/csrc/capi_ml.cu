@@ -251,12 +251,7 @@ int sdpg_inv_lower(int limbs, int n, const void *L, int ldl, void *Linv) {
             int rc = with_device_copy(limbs, (size_t)ldl * n, L, false, nullptr, [&](void *dL) {
                 Workspace &ws = thread_workspace();
                 ws.reset();
-                GemmProblem<N> p{};
-                p.M = 32;
-                p.Nn = n;
-                p.K = n;
-                p.batch = 1;
-                ws.reserve(2 * gemm_workspace_bytes<N>(p) + (size_t)32 * n * sizeof(mlf<N>) + (1 << 20));
+                ws.reserve(ml_trtri_workspace_bytes<N>(n) + (1 << 20));
                 ml_trtri_lower<N>(n, (const mlf<N> *)dL, ldl, (mlf<N> *)dout.p, ws, nullptr);
                 return (int)SDPG_OK;
             });

@@ -245,34 +245,107 @@ void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t 
     ws.used = mark;
 }
 
+namespace {
+
+template <int N>
+__global__ void pad_lower_kernel(int n, int P, const mlf<N> *L, int ldl, mlf<N> *Lp) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= (long long)P * P) return;
+    const int i = (int)(q % P), j = (int)(q / P);
+    mlf<N> v = ml_zero<N>();
+    if (i < n && j < n) {
+        if (i >= j) v = L[i + (long long)j * ldl];
+    } else if (i == j) {
+        v = ml_one<N>();
+    }
+    Lp[q] = v;
+}
+
+template <int N>
+__global__ void unpad_kernel(int n, int P, const mlf<N> *Xp, mlf<N> *X) {
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= (long long)n * n) return;
+    const int i = (int)(q % n), j = (int)(q / n);
+    X[q] = Xp[i + (long long)j * P];
+}
+
+inline int trtri_pad(int n) {
+    int P = NB;
+    while (P < n) P *= 2;
+    return P;
+}
+
+}  // namespace
+
+template <int N>
+size_t ml_trtri_workspace_bytes(int n) {
+    const int P = trtri_pad(n);
+    const size_t pp = (size_t)P * P;
+    GemmProblem<N> g{};
+    g.M = P / 2;
+    g.Nn = P / 2;
+    g.K = P / 2;
+    g.batch = 1;
+    // padded L and X, the per-level W, and the scratch of the top level's GEMM (a level with
+    // node size b quantises P*b/4 entries per operand, so the top level is the largest),
+    // with slack for alignment
+    return 2 * pp * sizeof(mlf<N>) + pp / 2 * sizeof(mlf<N>) + 2 * gemm_workspace_bytes<N>(g) + (64u << 10);
+}
+
+// Linv = L^{-1}: pad L to P = 32 * 2^k with an identity tail, invert the 32 x 32 diagonal
+// blocks in parallel, then for node sizes b = 64, 128, ..., P form every node's
+// off-diagonal block X21 = -X22 (L21 X11) with one batched GEMM pair per level.
 template <int N>
 void ml_trtri_lower(int n, const mlf<N> *L, int ldl, mlf<N> *Linv, Workspace &ws, cudaStream_t s) {
-    // Linv assumed n x n with leading dimension n
-    SDPG_CUDA(cudaMemsetAsync(Linv, 0, (size_t)n * n * sizeof(mlf<N>), s));
-    const int nb = ceil_div(n, NB);
-    trtri_diag_kernel<N><<<nb, 256, 0, s>>>(L, ldl, Linv, n, n);
-    SDPG_CHECK_LAUNCH();
+    const int P = trtri_pad(n);
     const size_t mark = ws.used;
-    mlf<N> *W = (mlf<N> *)ws.carve((size_t)NB * n * sizeof(mlf<N>));
+    const long long pp = (long long)P * P;
+    mlf<N> *Lp = (mlf<N> *)ws.carve(pp * sizeof(mlf<N>));
+    mlf<N> *Xp = (mlf<N> *)ws.carve(pp * sizeof(mlf<N>));
+    mlf<N> *W = (mlf<N> *)ws.carve(pp / 2 * sizeof(mlf<N>));
+    pad_lower_kernel<N><<<ceil_div(pp, 256), 256, 0, s>>>(n, P, L, ldl, Lp);
+    SDPG_CHECK_LAUNCH();
+    SDPG_CUDA(cudaMemsetAsync(Xp, 0, pp * sizeof(mlf<N>), s));
+    trtri_diag_kernel<N><<<P / NB, 256, 0, s>>>(Lp, P, Xp, P, P);
+    SDPG_CHECK_LAUNCH();
     const mlf<N> one = ml_one<N>(), zero = ml_zero<N>(), mone = ml_from_int<N>(-1);
-    for (int ib = 1; ib < nb; ++ib) {
-        const int i0 = ib * NB, kb = min(NB, n - i0);
-        // W (kb x i0) = L[i0:i0+kb, 0:i0] * Linv[0:i0, 0:i0]
+    for (int b = 2 * NB; b <= P; b *= 2) {
+        const int h = b / 2, nodes = P / b;
+        const long long node_stride = (long long)b * (1 + P);
+        // W_t = L21 X11  (h x h x h), batched over nodes
+        GemmProblem<N> p{};
+        p.M = h;
+        p.Nn = h;
+        p.K = h;
+        p.batch = nodes;
+        p.A = operand_A<N>('N', Lp + h, P, node_stride);
+        p.B = operand_B<N>('N', Xp, P, node_stride);
+        p.C = W;
+        p.ldc = h;
+        p.sc = (long long)h * h;
+        p.alpha = one;
+        p.beta = zero;
+        p.lower_only = 0;
         {
-            GemmProblem<N> p = gemm_nn<N>(kb, i0, i0, one, L + i0, ldl, 'N', Linv, n, 'N', zero, W, kb);
             const size_t m2 = ws.used;
             ml_gemm<N>(p, ws, s);
             ws.used = m2;
         }
-        // Linv[i0:i0+kb, 0:i0] = -Linv[i0:, i0:] (kb x kb) * W
+        // X21 = -X22 W_t
+        p.A = operand_A<N>('N', Xp + h + (long long)h * P, P, node_stride);
+        p.B = operand_B<N>('N', W, h, (long long)h * h);
+        p.C = Xp + h;
+        p.ldc = P;
+        p.sc = node_stride;
+        p.alpha = mone;
         {
-            GemmProblem<N> p = gemm_nn<N>(kb, i0, kb, mone, Linv + i0 + (long long)i0 * n, n, 'N', W, kb, 'N', zero,
-                                          Linv + i0, n);
             const size_t m2 = ws.used;
             ml_gemm<N>(p, ws, s);
             ws.used = m2;
         }
     }
+    unpad_kernel<N><<<ceil_div((long long)n * n, 256), 256, 0, s>>>(n, P, Xp, Linv);
+    SDPG_CHECK_LAUNCH();
     ws.used = mark;
 }
 
@@ -305,6 +378,7 @@ void ml_potrs(int n, const mlf<N> *L, int ldl, mlf<N> *x, Workspace &ws, cudaStr
 #define SDPG_INST_CHOL(N)                                                                       \
     template void ml_potrf<N>(int, mlf<N> *, int, int *, Workspace &, cudaStream_t);            \
     template void ml_trtri_lower<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t); \
+    template size_t ml_trtri_workspace_bytes<N>(int);                                                       \
     template void ml_potrs<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t);             \
     template size_t ml_potrs_prepare_bytes<N>(int);                                                        \
     template void ml_potrs_prepare<N>(int, const mlf<N> *, int, mlf<N> *, cudaStream_t);                    \

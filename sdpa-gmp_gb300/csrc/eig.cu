@@ -17,6 +17,8 @@
 // p_{k-1}(lambda) / p_k'(lambda).
 #include <float.h>
 
+#include <climits>
+
 #include "kernels.cuh"
 #include "mlwarp.cuh"
 
@@ -145,9 +147,14 @@ __global__ void tridiag_min_kernel(int k, const mlf<N> *d, const mlf<N> *e, mlf<
         else a = mid;
     }
     mlf<N> lam = ml_from_double<N>(0.5 * (a + b));
+    // Newton on the characteristic polynomial.  Converged when the step is below
+    // 2^-(32N+2) of the matrix scale S = max(|lo|, |hi|) (the Gershgorin bound), or
+    // once steps stop shrinking (the rounding floor of the recurrence is reached).
+    const int scale_e = ml_from_double<N>(fmax(fabs(lo), fabs(hi))).e;
     mlf<N> pk, dpk, pkm1;
     int st = 2;  // not converged
-    for (int it = 0; it < 12; ++it) {
+    int prev_e = INT_MAX;
+    for (int it = 0; it < 16; ++it) {
         charpoly<N>(k, d, e, lam, &pk, &dpk, &pkm1);
         if (ml_is_zero(pk)) {
             st = 0;
@@ -156,12 +163,13 @@ __global__ void tridiag_min_kernel(int k, const mlf<N> *d, const mlf<N> *e, mlf<
         if (ml_is_zero(dpk)) break;
         const mlf<N> delta = ml_div(pk, dpk);
         lam = ml_sub(lam, delta);
-        // converged when |delta| < 2^-(32N+4) * max(|lam|, tiny)
-        if (ml_is_zero(delta) || (!ml_is_zero(lam) && delta.e < lam.e - (32 * N + 4))) {
+        if (ml_is_zero(delta) || delta.e < scale_e - (32 * N + 2) ||
+            (!ml_is_zero(lam) && delta.e < lam.e - (32 * N + 2)) || (it >= 2 && delta.e > prev_e - 2)) {
             st = 0;
             charpoly<N>(k, d, e, lam, &pk, &dpk, &pkm1);
             break;
         }
+        prev_e = delta.e;
     }
     out[0] = lam;
     // z^2 = p_{k-1}(lam) / p_k'(lam)  (>= 0 at a simple root)

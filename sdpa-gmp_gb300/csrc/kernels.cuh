@@ -99,6 +99,9 @@ void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t 
 // Linv's strict upper triangle is set to zero.
 template <int N>
 void ml_trtri_lower(int n, const mlf<N> *L, int ldl, mlf<N> *Linv, Workspace &ws, cudaStream_t s);
+// workspace bytes ml_trtri_lower carves (beyond ws.used)
+template <int N>
+size_t ml_trtri_workspace_bytes(int n);
 // x = (L L^T)^{-1} x (two Rtrsv, Lal::solveSystems sdpa_linear.cpp:683-695)
 template <int N>
 void ml_potrs(int n, const mlf<N> *L, int ldl, mlf<N> *x, Workspace &ws, cudaStream_t s);

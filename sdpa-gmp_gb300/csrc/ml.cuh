@@ -475,6 +475,51 @@ MLHD mlf<M> ml_widen(const mlf<N> &a) {
     return r;
 }
 
+// Double-double seeds (about 106 correct bits) for the reciprocal and the inverse
+// square root of a mantissa, from one Newton step carried out in double-double
+// arithmetic with fused multiply-adds (error-free products).  The value is returned
+// as hi + lo.
+MLHD void ml_dd_two_prod(double a, double b, double *p, double *e) {
+    *p = a * b;
+    *e = fma(a, b, -*p);
+}
+
+template <int N>
+MLHD void ml_dd_of(const mlf<N> &a, double *hi, double *lo) {
+    // top 106 bits of the mantissa as an exact double-double (exponent dropped: a in [1/2,1) or [1/4,1))
+    const uint64_t t0 = ((uint64_t)a.m[N - 1] << 32) | a.m[N - 2];
+    const uint64_t t1 = ((uint64_t)a.m[N - 3] << 32) | (N >= 4 ? a.m[N - 4] : 0u);
+    const double h = ldexp((double)(t0 >> 11), a.e - 53);
+    const double l = ldexp((double)(((t0 & 0x7ffull) << 42) | (t1 >> 22)), a.e - 106);
+    *hi = h + l;
+    *lo = l - (*hi - h);
+}
+
+// 1/x for x = xh + xl in [1/2, 1): ~106 bits
+MLHD void ml_dd_recip(double xh, double xl, double *rh, double *rl) {
+    const double r0 = 1.0 / xh;
+    double p, e;
+    ml_dd_two_prod(xh, r0, &p, &e);
+    // t = 1 - x r0 (exact to ~2^-106 thanks to the error-free product)
+    const double t = ((1.0 - p) - e) - xl * r0;
+    *rh = r0;
+    *rl = r0 * t;
+}
+
+// 1/sqrt(x) for x = xh + xl in [1/4, 1): ~106 bits
+MLHD void ml_dd_rsqrt(double xh, double xl, double *rh, double *rl) {
+    const double y0 = 1.0 / sqrt(xh);
+    double s, se, p, pe;
+    ml_dd_two_prod(y0, y0, &s, &se);      // y0^2 = s + se exactly
+    ml_dd_two_prod(xh, s, &p, &pe);       // xh * s exactly
+    const double t = ((1.0 - p) - pe) - (xh * se + xl * s);  // 1 - x y0^2
+    *rh = y0;
+    *rl = 0.5 * y0 * t;
+}
+
+template <int N>
+MLHD mlf<N> ml_from_dd(double hi, double lo) { return ml_add(ml_from_double<N>(hi), ml_from_double<N>(lo)); }
+
 // 1/bn for a mantissa bn in [1/2, 1): Newton steps at rising precision (N/2 first,
 // then one step at N doubles the correct bits), so only the last steps pay full cost.
 template <int N>
@@ -504,9 +549,16 @@ MLHD mlf<N> ml_recip(const mlf<N> &b) {
         x = ml_recip_mant<N>(bn);
         x = ml_add(x, ml_mul(x, ml_sub(one, ml_mul(bn, x))));
     } else {
-        x = ml_widen<N, N / 2>(ml_recip_mant<N / 2>(ml_narrow<N / 2, N>(bn)));
-        const mlf<N> t = ml_sub(one, ml_mul(bn, x));  // ~2^-(16N), needs full precision
-        constexpr int H = N / 2 + 1;                  // the correction needs ~16N bits
+        if constexpr (N <= 8) {
+            double h, l, rh, rl;
+            ml_dd_of<N>(bn, &h, &l);
+            ml_dd_recip(h, l, &rh, &rl);
+            x = ml_from_dd<N>(rh, rl);  // ~106 bits; one cubic step gives > 300
+        } else {
+            x = ml_widen<N, N / 2>(ml_recip<N / 2>(ml_narrow<N / 2, N>(bn)));  // > 300 bits at N/2 = 8
+        }
+        const mlf<N> t = ml_sub(one, ml_mul(bn, x));
+        constexpr int H = N / 2 + 1;
         const mlf<H> th = ml_narrow<H, N>(t);
         const mlf<H> corr = ml_mul(ml_narrow<H, N>(x), ml_add(th, ml_mul(th, th)));
         x = ml_add(x, ml_widen<N, H>(corr));
@@ -557,7 +609,14 @@ MLHD mlf<N> ml_rsqrt(const mlf<N> &a) {
         const mlf<N> t = ml_sub(one, ml_mul(an, ml_mul(y, y)));
         y = ml_add(y, ml_ldexp(ml_mul(y, t), -1));
     } else {
-        y = ml_widen<N, N / 2>(ml_rsqrt_mant<N / 2>(ml_narrow<N / 2, N>(an)));
+        if constexpr (N <= 8) {
+            double h, l, rh, rl;
+            ml_dd_of<N>(an, &h, &l);
+            ml_dd_rsqrt(h, l, &rh, &rl);
+            y = ml_from_dd<N>(rh, rl);  // ~106 bits; one cubic step gives > 300
+        } else {
+            y = ml_widen<N, N / 2>(ml_rsqrt<N / 2>(ml_narrow<N / 2, N>(an)));  // > 300 bits at N/2 = 8
+        }
         const mlf<N> t = ml_sub(one, ml_mul(an, ml_mul(y, y)));
         constexpr int H = N / 2 + 1;
         const mlf<H> th = ml_narrow<H, N>(t);

@@ -313,6 +313,7 @@ class Solver final : public SolverBase {
                 }
             }
             max_ws = std::max(max_ws, gemm_bytes(32, n, n, 1) + 32 * (size_t)n * sizeof(V));
+            max_ws = std::max(max_ws, ml_trtri_workspace_bytes<N>(n));
         }
         max_ws = std::max(max_ws, gemm_bytes(m_, m_, 32, 1));
         ws_.reserve(max_ws + (64u << 20));
