@@ -271,8 +271,13 @@ int sdpg_solve_systems(int limbs, int n, const void *L, int ldl, void *x) {
             int rc = with_device_copy(limbs, (size_t)ldl * n, L, false, nullptr, [&](void *dL) {
                 Workspace &ws = thread_workspace();
                 ws.reset();
-                ws.reserve((size_t)n * sizeof(mlf<N>) + (1 << 20));
-                ml_potrs<N>(n, (const mlf<N> *)dL, ldl, (mlf<N> *)dx.p, ws, nullptr);
+                ws.reserve(ml_potrs_prepare_bytes<N>(n) + (1 << 20));
+                mlf<N> *Dinv = (mlf<N> *)ws.carve(ml_potrs_prepare_bytes<N>(n));
+                ml_potrs_prepare<N>(n, (const mlf<N> *)dL, ldl, Dinv, nullptr);
+                ml_potrs_solve<N>(n, (const mlf<N> *)dL, ldl, Dinv, (mlf<N> *)dx.p, nullptr);
+                int st = 0;
+                SDPG_CUDA(cudaMemcpy(&st, ml_potrs_status<N>(n, Dinv), sizeof(int), cudaMemcpyDeviceToHost));
+                if (st != 0) throw sdpg_error(SDPG_ERR_TIMEOUT, "triangular solve: a bounded wait timed out");
                 return (int)SDPG_OK;
             });
             SDPG_CUDA(cudaMemcpy(x, dx.p, (size_t)n * sizeof(mlf<N>), cudaMemcpyDeviceToHost));

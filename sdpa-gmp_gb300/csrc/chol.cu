@@ -16,65 +16,92 @@ namespace {
 
 constexpr int NB = 32;
 
-// Factor the kb x kb diagonal block at A (ld lda) in place; rinv[j] = 1/L[j][j].
+// Factor the kb x kb diagonal block at A (ld lda) in place; rinv[j] = 1/L[j][j] and
+// Lsc (ld NB) = diag(rinv) L, the row-scaled factor the panel solve uses.
 // info: 0, or (col0 + j + 1) for the first non-positive pivot.
+//
+// Division-free elimination.  One thread per lower-triangle entry keeps it in
+// registers.  Step j updates every entry right of column j as
+//     s_it <- (p_j s_it - s_ij s_tj) * 2^-e_j,     p_j = s_jj in [2^(e_j-1), 2^e_j),
+// so S^(j) = c_j T^(j) where T^(j) is the usual Schur complement and
+// c_{j+1} = c_j p_j 2^-e_j.  No square root or reciprocal sits on the pivot chain
+// (one multiply-subtract and one barrier per step); at the end every column is
+// normalised at once with L[i][j] = s_ij / sqrt(c_j p_j).
+constexpr int kPotf2Threads = ((NB * (NB + 1) / 2 + 31) / 32) * 32;
+
 template <int N>
-__global__ void potf2_kernel(mlf<N> *A, int lda, int kb, int col0, int *info, mlf<N> *rinv) {
-    __shared__ int bad;
+__global__ void __launch_bounds__(kPotf2Threads, 1)
+    potf2_kernel(mlf<N> *A, int lda, int kb, int col0, int *info, mlf<N> *rinv, mlf<N> *Lsc) {
+    __shared__ mlf<N> col[2][NB];  // column j of S^(j), double-buffered across steps
+    __shared__ mlf<N> cs[NB];      // c_j
+    __shared__ mlf<N> pv[NB];      // p_j
+    __shared__ mlf<N> rs[NB];      // 1/sqrt(c_j p_j)
+    __shared__ mlf<N> ri[NB];      // 1/L[j][j] = c_j / sqrt(c_j p_j)
     if (*info != 0) return;
-    if (threadIdx.x == 0) bad = 0;
+    // entries numbered column by column (column t holds rows t..NB-1), so the entries
+    // still active at step j (t > j) are the highest-numbered threads and whole warps
+    // drop out as the factorisation proceeds
+    const int q = threadIdx.x;
+    int t = 0;
+    while (t + 1 < NB && NB * (t + 1) - (t + 1) * t / 2 <= q) ++t;
+    const int i = t + (q - (NB * t - t * (t - 1) / 2));  // entry (i, t), t <= i
+    const bool mine = q < NB * (NB + 1) / 2 && i < kb;
+    mlf<N> a = mine ? A[i + (long long)t * lda] : ml_zero<N>();
+    if (mine && t == 0) col[0][i] = a;
     __syncthreads();
+    mlf<N> c = ml_one<N>();  // thread 0 (entry (0,0), idle after step 0) carries c_j
+    int bad = 0;
     for (int j = 0; j < kb; ++j) {
-        if (threadIdx.x == 0) {
-            const mlf<N> d = A[j + (long long)j * lda];
-            if (ml_sign(d) <= 0) {
-                bad = col0 + j + 1;
-            } else {
-                const mlf<N> r = ml_rsqrt(d);
-                A[j + (long long)j * lda] = ml_mul(d, r);  // sqrt(d)
-                rinv[j] = r;
-            }
+        const mlf<N> p = col[j & 1][j];
+        if (ml_sign(p) <= 0) {
+            bad = col0 + j + 1;
+            break;
         }
-        __syncthreads();
-        if (bad) break;
-        const mlf<N> r = rinv[j];
-        for (int i = j + 1 + threadIdx.x; i < kb; i += blockDim.x)
-            A[i + (long long)j * lda] = ml_mul(A[i + (long long)j * lda], r);
-        __syncthreads();
-        // trailing lower triangle of the block: A[i,t] -= L[i,j] L[t,j], j < t <= i < kb
-        const int w = kb - j - 1;
-        const int cnt = w * (w + 1) / 2;
-        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
-            // q -> (ii, tt) with 0 <= tt <= ii < w
-            int ii = (int)((sqrtf(8.0f * q + 1.0f) - 1.0f) * 0.5f);
-            while (ii * (ii + 1) / 2 > q) --ii;
-            while ((ii + 1) * (ii + 2) / 2 <= q) ++ii;
-            const int tt = q - ii * (ii + 1) / 2;
-            const int i = j + 1 + ii, t = j + 1 + tt;
-            mlf<N> *a = A + i + (long long)t * lda;
-            *a = ml_sub(*a, ml_mul(A[i + (long long)j * lda], A[t + (long long)j * lda]));
+        if (q == 0) {
+            cs[j] = c;
+            c = ml_mul(c, ml_ldexp(p, -p.e));
+        }
+        if (mine && t > j) {
+            const mlf<N> u = ml_sub(ml_mul(p, a), ml_mul(col[j & 1][i], col[j & 1][t]));
+            a = ml_ldexp(u, -p.e);
+            if (t == j + 1) col[(j + 1) & 1][i] = a;
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0 && bad) *info = bad;
+    if (bad) {
+        if (q == 0) *info = bad;
+        return;
+    }
+    if (mine && i == t) pv[t] = a;
+    __syncthreads();
+    if (q < kb) {
+        const mlf<N> r = ml_rsqrt(ml_mul(cs[q], pv[q]));
+        rs[q] = r;
+        ri[q] = ml_mul(cs[q], r);
+    }
+    __syncthreads();
+    if (mine) {
+        a = ml_mul(a, rs[t]);
+        A[i + (long long)t * lda] = a;
+        if (i > t) Lsc[i + NB * t] = ml_mul(a, ri[i]);
+    }
+    if (q < kb) rinv[q] = ri[q];
 }
 
-// Rows below the diagonal block: solve x * L11^T = a for each row (one warp per row).
-// L11 at Ld (ld lda, kb x kb lower), rows at R (ld lda), nrows rows.
+// Rows below the diagonal block: solve x L11^T = a for each row, one warp per row.
+// With a~ = a / diag(L11) and Lsc = diag(L11)^-1 L11 (unit lower), x_j = a~_j -
+// sum_{t<j} Lsc[j][t] x_t: each step is a broadcast and one multiply-subtract.
 template <int N>
-__global__ void panel_trsm_kernel(const mlf<N> *Ld, mlf<N> *R, int lda, int kb, int nrows, const int *info,
+__global__ void panel_trsm_kernel(const mlf<N> *Lsc, mlf<N> *R, int lda, int kb, int nrows, const int *info,
                                   const mlf<N> *rinv) {
     if (*info != 0) return;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= nrows) return;
     mlf<N> *row = R + warp;  // element t at row[t * lda]
-    mlf<N> a = lane < kb ? row[(long long)lane * lda] : ml_zero<N>();
-    for (int j = 0; j < kb; ++j) {
-        mlf<N> xj = ml_zero<N>();
-        if (lane == j) xj = ml_mul(a, rinv[j]);
-        xj = ml_shfl(xj, j);
-        if (lane == j) a = xj;
-        if (lane > j && lane < kb) a = ml_sub(a, ml_mul(xj, Ld[lane + (long long)j * lda]));
+    mlf<N> a = lane < kb ? ml_mul(row[(long long)lane * lda], rinv[lane]) : ml_zero<N>();
+    for (int j = 0; j + 1 < kb; ++j) {
+        const mlf<N> xj = ml_shfl(a, j);
+        if (lane > j && lane < kb) a = ml_sub(a, ml_mul(xj, Lsc[lane + NB * j]));
     }
     if (lane < kb) row[(long long)lane * lda] = a;
 }
@@ -139,62 +166,138 @@ __global__ void trtri_diag_packed_kernel(const mlf<N> *L, int ldl, mlf<N> *Dinv,
     }
 }
 
-// sum_{j<cnt} a[j*stride] * y[j] with four independent accumulator chains
+// Triangular solves as a wavefront over 32-row blocks, one CTA per block.  A CTA
+// draws a ticket at start (so every CTA it waits on has already started and is
+// resident), takes the contribution of each earlier block as soon as that block's
+// solution is published, and publishes its own after the diagonal solve with the
+// inverted diagonal block.  Only the last contribution and the diagonal solve are
+// on the critical path.  Every wait is bounded: on time-out the CTA records
+// status 1 and leaves (the result is then invalid and the caller reports it).
+//
+// sync (ints, zeroed before each launch): [0] ticket counter, [1 + b] block b done.
+constexpr int kTrsvThreads = 256;
+
 template <int N>
-__device__ __forceinline__ mlf<N> dot_ld(const mlf<N> *a, long long stride, const mlf<N> *y, int cnt) {
-    mlf<N> a0 = ml_zero<N>(), a1 = ml_zero<N>(), a2 = ml_zero<N>(), a3 = ml_zero<N>();
-    int j = 0;
-    for (; j + 3 < cnt; j += 4) {
-        a0 = ml_add(a0, ml_mul(a[j * stride], y[j]));
-        a1 = ml_add(a1, ml_mul(a[(j + 1) * stride], y[j + 1]));
-        a2 = ml_add(a2, ml_mul(a[(j + 2) * stride], y[j + 2]));
-        a3 = ml_add(a3, ml_mul(a[(j + 3) * stride], y[j + 3]));
-    }
-    for (; j < cnt; ++j) a0 = ml_add(a0, ml_mul(a[j * stride], y[j]));
-    return ml_add(ml_add(a0, a1), ml_add(a2, a3));
+__device__ __forceinline__ mlf<N> ml_load_cg(const mlf<N> *p) {
+    mlf<N> r;
+    const unsigned *w = reinterpret_cast<const unsigned *>(p);
+    unsigned *o = reinterpret_cast<unsigned *>(&r);
+#pragma unroll
+    for (int k = 0; k < N + 2; ++k) o[k] = __ldcg(w + k);
+    return r;
 }
 
-// x := L^{-T} L^{-1} x in one CTA (512 threads at 256 bits, 256 at 512 bits), blocked by NB with the inverted
-// diagonal blocks: each block solve is a small matrix-vector product (one warp per
-// output, a lane per term, tree-summed), then every thread updates one remaining row.
+constexpr int kTrsvWarps = kTrsvThreads / 32;
+constexpr long long kSpinLimit = 1ll << 24;
+
+__device__ __forceinline__ bool wait_flag(const int *flag, int *status) {
+    long long spins = 0;
+    while (*(volatile const int *)flag == 0) {
+        if (++spins > kSpinLimit || *(volatile int *)status != 0) {
+            atomicExch(status, 1);
+            return false;
+        }
+        __nanosleep(32);
+    }
+    __threadfence();
+    return true;
+}
+
+// rows r0 + i (i = lane) of the block: sum over this warp's terms t = warp, warp + 8, ...
+// of A[(r0 + i) + (c0 + t) lda] * xs[t] (t < kc), into part[warp][lane]
 template <int N>
-__global__ void __launch_bounds__(N <= 8 ? 512 : 256) potrs_blocked_kernel(int n, const mlf<N> *L, int ldl, const mlf<N> *Dinv, mlf<N> *x) {
-    __shared__ mlf<N> ys[NB];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+__device__ __forceinline__ void block_matvec_part(const mlf<N> *A, long long lda, int r0, int kb, int c0, int kc,
+                                                  const mlf<N> *xs, mlf<N> (*part)[NB], bool lower_t_le_i,
+                                                  bool upper_t_ge_i) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    mlf<N> s0 = ml_zero<N>(), s1 = ml_zero<N>();
+    if (lane < kb) {
+        int q = 0;
+        for (int t = warp; t < kc; t += kTrsvWarps, ++q) {
+            if (lower_t_le_i && t > lane) continue;
+            if (upper_t_ge_i && t < lane) continue;
+            const mlf<N> v = ml_mul(A[(r0 + lane) + (long long)(c0 + t) * lda], xs[t]);
+            if (q & 1) s1 = ml_add(s1, v);
+            else s0 = ml_add(s0, v);
+        }
+    }
+    part[warp][lane] = ml_add(s0, s1);
+}
+
+template <int N>
+__device__ __forceinline__ mlf<N> sum_parts(mlf<N> (*part)[NB], int lane) {
+    const mlf<N> a = ml_add(ml_add(part[0][lane], part[1][lane]), ml_add(part[2][lane], part[3][lane]));
+    const mlf<N> b = ml_add(ml_add(part[4][lane], part[5][lane]), ml_add(part[6][lane], part[7][lane]));
+    return ml_add(a, b);
+}
+
+// backward == 0: x := L^{-1} x (A = L, ld ldl); backward == 1: x := L^{-T} x (A = LT, ld n)
+template <int N>
+__global__ void __launch_bounds__(kTrsvThreads)
+    trsv_wavefront_kernel(int n, const mlf<N> *A, long long lda, const mlf<N> *Dinv, mlf<N> *x, int *sync, int *status,
+                          int backward) {
+    __shared__ int tk, abort_;
+    __shared__ mlf<N> xs[NB];
+    __shared__ mlf<N> part[kTrsvWarps][NB];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nblk = (n + NB - 1) / NB;
-    // forward: L y = x
-    for (int b = 0; b < nblk; ++b) {
-        const int k0 = b * NB, kb = min(NB, n - k0);
-        const mlf<N> *D = Dinv + (long long)b * NB * NB;
-        for (int w = warp; w < kb; w += nwarps) {
-            mlf<N> p = (lane <= w && lane < kb) ? ml_mul(D[w + NB * lane], x[k0 + lane]) : ml_zero<N>();
-            p = ml_warp_sum(p);
-            if (lane == 0) ys[w] = p;
-        }
+    if (tid == 0) {
+        tk = atomicAdd(&sync[0], 1);
+        abort_ = 0;
+    }
+    __syncthreads();
+    if (tk >= nblk) return;
+    const int b = backward ? nblk - 1 - tk : tk;
+    const int r0 = b * NB, kb = min(NB, n - r0);
+    mlf<N> acc = ml_zero<N>();  // warp 0, lane i: running sum for row r0 + i
+    for (int q = 0; q < tk; ++q) {
+        const int c = backward ? nblk - 1 - q : q;
+        const int c0 = c * NB, kc = min(NB, n - c0);
+        if (tid == 0 && !wait_flag(&sync[1 + c], status)) abort_ = 1;
         __syncthreads();
-        if (tid < kb) x[k0 + tid] = ys[tid];
-        for (int i = k0 + kb + tid; i < n; i += blockDim.x) {
-            const mlf<N> *Li = L + i + (long long)k0 * ldl;
-            x[i] = ml_sub(x[i], dot_ld<N>(Li, ldl, ys, kb));
-        }
+        if (abort_) return;
+        if (tid < kc) xs[tid] = ml_load_cg(x + c0 + tid);  // from L2: written by another CTA
+        __syncthreads();
+        block_matvec_part<N>(A, lda, r0, kb, c0, kc, xs, part, false, false);
+        __syncthreads();
+        if (warp == 0) acc = ml_add(acc, sum_parts<N>(part, lane));
         __syncthreads();
     }
-    // backward: L^T z = y
-    for (int b = nblk - 1; b >= 0; --b) {
-        const int k0 = b * NB, kb = min(NB, n - k0);
-        const mlf<N> *D = Dinv + (long long)b * NB * NB;
-        for (int w = warp; w < kb; w += nwarps) {
-            mlf<N> p = (lane >= w && lane < kb) ? ml_mul(D[lane + NB * w], x[k0 + lane]) : ml_zero<N>();
-            p = ml_warp_sum(p);
-            if (lane == 0) ys[w] = p;
+    if (warp == 0 && lane < kb) xs[lane] = ml_sub(x[r0 + lane], acc);
+    __syncthreads();
+    // diagonal: y = Dinv_b rhs (forward) or Dinv_b^T rhs (backward); Dinv_b[i][t] at D[i + NB t]
+    const mlf<N> *D = Dinv + (long long)b * NB * NB;
+    if (backward) {
+        // (Dinv^T)[i][t] = D[t + NB i], t >= i: lanes over i read with stride NB (a 32 x 32 block, cached)
+        mlf<N> s0 = ml_zero<N>(), s1 = ml_zero<N>();
+        if (lane < kb) {
+            int q = 0;
+            for (int t = warp; t < kb; t += kTrsvWarps, ++q) {
+                if (t < lane) continue;
+                const mlf<N> v = ml_mul(D[t + NB * lane], xs[t]);
+                if (q & 1) s1 = ml_add(s1, v);
+                else s0 = ml_add(s0, v);
+            }
         }
-        __syncthreads();
-        if (tid < kb) x[k0 + tid] = ys[tid];
-        for (int i = tid; i < k0; i += blockDim.x) {
-            const mlf<N> *Li = L + k0 + (long long)i * ldl;
-            x[i] = ml_sub(x[i], dot_ld<N>(Li, 1, ys, kb));
-        }
-        __syncthreads();
+        part[warp][lane] = ml_add(s0, s1);
+    } else {
+        block_matvec_part<N>(D, NB, 0, kb, 0, kb, xs, part, true, false);
+    }
+    __syncthreads();
+    if (warp == 0 && lane < kb) x[r0 + lane] = sum_parts<N>(part, lane);
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicExch(&sync[1 + b], 1);
+}
+
+// LT (ld n) = L^T for the lower-triangular n x n L (ld ldl): LT[j + i n] = L[i + j ldl], i >= j
+template <int N>
+__global__ void transpose_lower_kernel(int n, const mlf<N> *L, int ldl, mlf<N> *LT) {
+    const int j0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
+    if (j0 > i0 + 31) return;  // tile entirely above the diagonal of L: LT entries unused
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int i = i0 + threadIdx.x, j = j0 + r;  // read L[i][j] coalesced along i
+        if (i < n && j < n && i >= j) LT[j + (long long)i * n] = L[i + (long long)j * ldl];
     }
 }
 
@@ -224,16 +327,17 @@ void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t 
     SDPG_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
     const size_t mark = ws.used;
     mlf<N> *rinv = (mlf<N> *)ws.carve(NB * sizeof(mlf<N>));
+    mlf<N> *Lsc = (mlf<N> *)ws.carve(NB * NB * sizeof(mlf<N>));
     const mlf<N> mone = ml_from_int<N>(-1), one = ml_one<N>();
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int kb = min(NB, n - k0);
         mlf<N> *Akk = A + k0 + (long long)k0 * lda;
-        potf2_kernel<N><<<1, 512, 0, s>>>(Akk, lda, kb, k0, info, rinv);
+        potf2_kernel<N><<<1, kPotf2Threads, 0, s>>>(Akk, lda, kb, k0, info, rinv, Lsc);
         SDPG_CHECK_LAUNCH();
         const int rows = n - k0 - kb;
         if (rows <= 0) break;
         mlf<N> *A21 = A + (k0 + kb) + (long long)k0 * lda;
-        panel_trsm_kernel<N><<<ceil_div((long long)rows * 32, 256), 256, 0, s>>>(Akk, A21, lda, kb, rows, info, rinv);
+        panel_trsm_kernel<N><<<ceil_div((long long)rows * 32, 256), 256, 0, s>>>(Lsc, A21, lda, kb, rows, info, rinv);
         SDPG_CHECK_LAUNCH();
         GemmProblem<N> p = gemm_nn<N>(rows, rows, kb, mone, A21, lda, 'N', A21, lda, 'T', one,
                                       A + (k0 + kb) + (long long)(k0 + kb) * lda, lda);
@@ -349,21 +453,42 @@ void ml_trtri_lower(int n, const mlf<N> *L, int ldl, mlf<N> *Linv, Workspace &ws
     ws.used = mark;
 }
 
+// prepared data: the packed inverted diagonal blocks, the transposed factor (ld n),
+// then the wavefront synchronisation words and a status word
 template <int N>
 size_t ml_potrs_prepare_bytes(int n) {
-    return (size_t)ceil_div(n, NB) * NB * NB * sizeof(mlf<N>);
+    const size_t nblk = ceil_div(n, NB);
+    return (nblk * NB * NB + (size_t)n * n) * sizeof(mlf<N>) + (2 * (nblk + 1) + 1) * sizeof(int) + 256;
 }
 
 template <int N>
 void ml_potrs_prepare(int n, const mlf<N> *L, int ldl, mlf<N> *Dinv, cudaStream_t s) {
     trtri_diag_packed_kernel<N><<<ceil_div(n, NB), 256, 0, s>>>(L, ldl, Dinv, n);
     SDPG_CHECK_LAUNCH();
+    mlf<N> *LT = Dinv + (size_t)ceil_div(n, NB) * NB * NB;
+    transpose_lower_kernel<N><<<dim3(ceil_div(n, 32), ceil_div(n, 32)), dim3(32, 8), 0, s>>>(n, L, ldl, LT);
+    SDPG_CHECK_LAUNCH();
 }
 
 template <int N>
 void ml_potrs_solve(int n, const mlf<N> *L, int ldl, const mlf<N> *Dinv, mlf<N> *x, cudaStream_t s) {
-    potrs_blocked_kernel<N><<<1, N <= 8 ? 512 : 256, 0, s>>>(n, L, ldl, Dinv, x);
+    const int nblk = ceil_div(n, NB);
+    const mlf<N> *LT = Dinv + (size_t)nblk * NB * NB;
+    int *sync = (int *)(((uintptr_t)(LT + (size_t)n * n) + 255) & ~(uintptr_t)255);
+    int *status = sync + 2 * (nblk + 1);
+    SDPG_CUDA(cudaMemsetAsync(sync, 0, (2 * (nblk + 1) + 1) * sizeof(int), s));
+    trsv_wavefront_kernel<N><<<nblk, kTrsvThreads, 0, s>>>(n, L, ldl, Dinv, x, sync, status, 0);
     SDPG_CHECK_LAUNCH();
+    trsv_wavefront_kernel<N><<<nblk, kTrsvThreads, 0, s>>>(n, LT, n, Dinv, x, sync + nblk + 1, status, 1);
+    SDPG_CHECK_LAUNCH();
+}
+
+template <int N>
+int *ml_potrs_status(int n, mlf<N> *Dinv) {
+    const int nblk = ceil_div(n, NB);
+    const mlf<N> *LT = Dinv + (size_t)nblk * NB * NB;
+    int *sync = (int *)(((uintptr_t)(LT + (size_t)n * n) + 255) & ~(uintptr_t)255);
+    return sync + 2 * (nblk + 1);
 }
 
 template <int N>
@@ -382,7 +507,8 @@ void ml_potrs(int n, const mlf<N> *L, int ldl, mlf<N> *x, Workspace &ws, cudaStr
     template void ml_potrs<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t);             \
     template size_t ml_potrs_prepare_bytes<N>(int);                                                        \
     template void ml_potrs_prepare<N>(int, const mlf<N> *, int, mlf<N> *, cudaStream_t);                    \
-    template void ml_potrs_solve<N>(int, const mlf<N> *, int, const mlf<N> *, mlf<N> *, cudaStream_t);
+    template void ml_potrs_solve<N>(int, const mlf<N> *, int, const mlf<N> *, mlf<N> *, cudaStream_t);        \
+    template int *ml_potrs_status<N>(int, mlf<N> *);
 SDPG_INST_CHOL(8)
 SDPG_INST_CHOL(16)
 

@@ -79,29 +79,42 @@ __global__ void lanczos_next_kernel(int n, const mlf<N> *r, const mlf<N> *rbeta,
     q[i] = ml_mul(r[i], *rbeta);
 }
 
-__device__ int sturm_count_d(int k, const double *d, const double *e2, double x) {
+// Number of eigenvalues of the (scaled, single-precision) tridiagonal below x: the
+// negative pivots of the LDL^T factorisation of T - x I (Sturm sequence).
+__device__ int sturm_count_f(int k, const float *d, const float *e2, float x) {
     int cnt = 0;
-    double q = d[0] - x;
-    if (q < 0) ++cnt;
+    float q = d[0] - x;
+    cnt += q < 0.0f;
     for (int i = 1; i < k; ++i) {
-        if (q == 0.0) q = -DBL_EPSILON * (fabs(d[i - 1]) + 1e-300);
-        q = d[i] - x - e2[i - 1] / q;
-        if (q < 0) ++cnt;
+        if (q == 0.0f) q = -1e-30f;
+        q = (d[i] - x) - e2[i - 1] / q;
+        cnt += q < 0.0f;
     }
     return cnt;
 }
 
-// p_k(lam) and p_k'(lam), p_{k-1}(lam) by the monic three-term recurrence
+// a * 2^-E as a float (0 below the float range); E is at least a's exponent
 template <int N>
-__device__ void charpoly(int k, const mlf<N> *d, const mlf<N> *e, const mlf<N> &lam, mlf<N> *pk, mlf<N> *dpk,
-                         mlf<N> *pkm1) {
-    mlf<N> p_prev = ml_one<N>(), p_cur = ml_sub(lam, d[0]);
-    mlf<N> dp_prev = ml_zero<N>(), dp_cur = ml_one<N>();
+__device__ float ml_to_float_scaled(const mlf<N> &a, int E) {
+    if (ml_is_zero(a)) return 0.0f;
+    const int ex = a.e - E;
+    if (ex < -120) return 0.0f;
+    const float f = ldexpf((float)(a.m[N - 1] >> 8) * 5.9604644775390625e-8f, ex);
+    return a.s ? -f : f;
+}
+
+// p_k(lam), p_k'(lam) and p_{k-1}(lam) of det(lam I - T) at M limbs, from d, e held at N limbs
+template <int M, int N>
+__device__ void charpoly_at(int k, const mlf<N> *d, const mlf<N> *e, const mlf<M> &lam, mlf<M> *pk, mlf<M> *dpk,
+                            mlf<M> *pkm1) {
+    mlf<M> p_prev = ml_one<M>(), p_cur = ml_sub(lam, ml_narrow<M, N>(d[0]));
+    mlf<M> dp_prev = ml_zero<M>(), dp_cur = ml_one<M>();
     for (int i = 1; i < k; ++i) {
-        const mlf<N> a = ml_sub(lam, d[i]);
-        const mlf<N> b2 = ml_mul(e[i - 1], e[i - 1]);
-        const mlf<N> p_new = ml_sub(ml_mul(a, p_cur), ml_mul(b2, p_prev));
-        const mlf<N> dp_new = ml_sub(ml_add(p_cur, ml_mul(a, dp_cur)), ml_mul(b2, dp_prev));
+        const mlf<M> a = ml_sub(lam, ml_narrow<M, N>(d[i]));
+        const mlf<M> ei = ml_narrow<M, N>(e[i - 1]);
+        const mlf<M> b2 = ml_mul(ei, ei);
+        const mlf<M> p_new = ml_sub(ml_mul(a, p_cur), ml_mul(b2, p_prev));
+        const mlf<M> dp_new = ml_sub(ml_add(p_cur, ml_mul(a, dp_cur)), ml_mul(b2, dp_prev));
         p_prev = p_cur;
         p_cur = p_new;
         dp_prev = dp_cur;
@@ -112,71 +125,136 @@ __device__ void charpoly(int k, const mlf<N> *d, const mlf<N> *e, const mlf<N> &
     *pkm1 = p_prev;
 }
 
+// Newton on det(lam I - T) at M limbs until the step is below 2^-tol of the scale
+// 2^scale_e (at most maxit evaluations).  Returns 1 when that tolerance was met.
+template <int M, int N>
+__device__ int newton_level(int k, const mlf<N> *d, const mlf<N> *e, mlf<M> &lam, int scale_e, int tol, int maxit,
+                            mlf<M> *pkm1, mlf<M> *dpk) {
+    int prev_e = INT_MAX;
+    for (int it = 0; it < maxit; ++it) {
+        mlf<M> pk;
+        charpoly_at<M, N>(k, d, e, lam, &pk, dpk, pkm1);
+        if (ml_is_zero(pk)) return 1;
+        if (ml_is_zero(*dpk)) return 0;
+        const mlf<M> delta = ml_div(pk, *dpk);
+        lam = ml_sub(lam, delta);
+        if (ml_is_zero(delta) || delta.e < scale_e - tol) return 1;
+        // steps that no longer shrink fourfold: the rounding floor of the recurrence
+        if (delta.e > prev_e - 2) return 1;
+        prev_e = delta.e;
+    }
+    return 0;
+}
+
+// Smallest eigenvalue of tridiag(e, d, e): a 32-way single-precision multisection of
+// the Gershgorin interval on the Sturm count (one point per lane) down to about 20
+// bits, then Newton's method on the characteristic polynomial from the left end of
+// the bracket at 2, 4, ... limbs up to full precision (from the left of the smallest
+// root of a real-rooted polynomial, Newton increases monotonically towards it).
+// out[1] = |z_k| = sqrt(p_{k-1}(lam) / p_k'(lam)).
 template <int N>
 __global__ void tridiag_min_kernel(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *status) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    __shared__ float df[kMaxTri], e2f[kMaxTri];
+    __shared__ float bounds[2];
+    const int lane = threadIdx.x;
     if (k <= 0 || k > kMaxTri) {
-        *status = 1;
+        if (lane == 0) *status = 1;
         return;
     }
     if (k == 1) {
-        out[0] = d[0];
-        out[1] = ml_one<N>();
-        *status = 0;
+        if (lane == 0) {
+            out[0] = d[0];
+            out[1] = ml_one<N>();
+            *status = 0;
+        }
         return;
     }
-    double dd[kMaxTri], e2[kMaxTri];
-    double lo = 0, hi = 0;
-    for (int i = 0; i < k; ++i) {
-        dd[i] = ml_to_double(d[i]);
-        const double ea = (i > 0 ? fabs(ml_to_double(e[i - 1])) : 0.0) + (i + 1 < k ? fabs(ml_to_double(e[i])) : 0.0);
-        if (i + 1 < k) {
-            const double ev = ml_to_double(e[i]);
-            e2[i] = ev * ev;
-        }
-        const double l = dd[i] - ea, h = dd[i] + ea;
-        if (i == 0 || l < lo) lo = l;
-        if (i == 0 || h > hi) hi = h;
+    // common scale 2^E: the largest exponent among the entries
+    int E = INT_MIN;
+    for (int i = lane; i < k; i += 32) {
+        if (!ml_is_zero(d[i])) E = max(E, d[i].e);
+        if (i + 1 < k && !ml_is_zero(e[i])) E = max(E, e[i].e);
     }
-    // bisection for the smallest eigenvalue: count(x) >= 1 means x above it
-    double a = lo - 1e-300 - fabs(lo) * 1e-15, b = hi + fabs(hi) * 1e-15 + 1e-300;
-    for (int it = 0; it < 200; ++it) {
-        const double mid = 0.5 * (a + b);
-        if (mid <= a || mid >= b) break;
-        if (sturm_count_d(k, dd, e2, mid) >= 1) b = mid;
-        else a = mid;
+    for (int o = 16; o > 0; o >>= 1) E = max(E, __shfl_xor_sync(0xffffffffu, E, o));
+    if (E == INT_MIN) {  // the zero matrix
+        if (lane == 0) {
+            out[0] = ml_zero<N>();
+            out[1] = ml_one<N>();
+            *status = 0;
+        }
+        return;
     }
-    mlf<N> lam = ml_from_double<N>(0.5 * (a + b));
-    // Newton on the characteristic polynomial.  Converged when the step is below
-    // 2^-(32N+2) of the matrix scale S = max(|lo|, |hi|) (the Gershgorin bound), or
-    // once steps stop shrinking (the rounding floor of the recurrence is reached).
-    const int scale_e = ml_from_double<N>(fmax(fabs(lo), fabs(hi))).e;
-    mlf<N> pk, dpk, pkm1;
-    int st = 2;  // not converged
-    int prev_e = INT_MAX;
-    for (int it = 0; it < 16; ++it) {
-        charpoly<N>(k, d, e, lam, &pk, &dpk, &pkm1);
-        if (ml_is_zero(pk)) {
-            st = 0;
-            break;
+    float lo = 3.4e38f, hi = -3.4e38f;
+    for (int i = lane; i < k; i += 32) {
+        const float di = ml_to_float_scaled(d[i], E);
+        const float em = i > 0 ? fabsf(ml_to_float_scaled(e[i - 1], E)) : 0.0f;
+        const float ep = i + 1 < k ? fabsf(ml_to_float_scaled(e[i], E)) : 0.0f;
+        df[i] = di;
+        if (i + 1 < k) e2f[i] = ep * ep;
+        lo = fminf(lo, di - em - ep);
+        hi = fmaxf(hi, di + em + ep);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    __syncwarp();
+    // widen slightly: the float Gershgorin bounds are rounded
+    const float span = fmaxf(hi - lo, 1e-30f);
+    lo -= 1e-6f * span + 1e-30f;
+    hi += 1e-6f * span + 1e-30f;
+    const float scale = fmaxf(fabsf(lo), fabsf(hi));  // matrix scale for the stopping rules
+    for (int round = 0; round < 8; ++round) {
+        const float w = hi - lo;
+        if (w <= 1e-6f * fmaxf(fmaxf(fabsf(lo), fabsf(hi)), 1e-30f)) break;
+        const float x = lo + w * (float)(lane + 1) * (1.0f / 33.0f);
+        const unsigned ball = __ballot_sync(0xffffffffu, sturm_count_f(k, df, e2f, x) >= 1);
+        const int first = ball ? __ffs(ball) - 1 : 32;  // first point with an eigenvalue below it
+        const float xlo = __shfl_sync(0xffffffffu, x, first > 0 ? first - 1 : 0);
+        const float xhi = __shfl_sync(0xffffffffu, x, first < 32 ? first : 31);
+        if (first == 32) lo = xhi;
+        else {
+            hi = xhi;
+            if (first > 0) lo = xlo;
         }
-        if (ml_is_zero(dpk)) break;
-        const mlf<N> delta = ml_div(pk, dpk);
-        lam = ml_sub(lam, delta);
-        if (ml_is_zero(delta) || delta.e < scale_e - (32 * N + 2) ||
-            (!ml_is_zero(lam) && delta.e < lam.e - (32 * N + 2)) || (it >= 2 && delta.e > prev_e - 2)) {
-            st = 0;
-            charpoly<N>(k, d, e, lam, &pk, &dpk, &pkm1);
-            break;
+    }
+    if (lane == 0) {
+        bounds[0] = lo;
+        bounds[1] = hi;
+    }
+    __syncwarp();
+    if (lane != 0) return;
+    const int scale_e = E + ilogbf(scale) + 1;
+    mlf<2> l2 = ml_ldexp(ml_from_float<2>(bounds[0]), E);
+    mlf<N> lam, pkm1, dpk;
+    int ok;
+    {
+        mlf<2> a, b;
+        newton_level<2, N>(k, d, e, l2, scale_e, 50, 8, &a, &b);
+    }
+    if constexpr (N <= 4) {
+        lam = ml_widen<N, 2>(l2);
+        ok = newton_level<N, N>(k, d, e, lam, scale_e, 32 * N - 4, 8, &pkm1, &dpk);
+    } else {
+        mlf<4> l4 = ml_widen<4, 2>(l2);
+        {
+            mlf<4> a, b;
+            newton_level<4, N>(k, d, e, l4, scale_e, 110, 6, &a, &b);
         }
-        prev_e = delta.e;
+        if constexpr (N <= 8) {
+            lam = ml_widen<N, 4>(l4);
+        } else {
+            mlf<8> l8 = ml_widen<8, 4>(l4);
+            mlf<8> a, b;
+            newton_level<8, N>(k, d, e, l8, scale_e, 230, 6, &a, &b);
+            lam = ml_widen<N, 8>(l8);
+        }
+        ok = newton_level<N, N>(k, d, e, lam, scale_e, 32 * N - 4, 8, &pkm1, &dpk);
     }
     out[0] = lam;
-    // z^2 = p_{k-1}(lam) / p_k'(lam)  (>= 0 at a simple root)
-    mlf<N> z2 = ml_is_zero(dpk) ? ml_zero<N>() : ml_div(pkm1, dpk);
-    z2 = ml_abs(z2);
+    const mlf<N> z2 = ml_is_zero(dpk) ? ml_zero<N>() : ml_abs(ml_div(pkm1, dpk));
     out[1] = ml_sqrt(z2);
-    *status = st;
+    *status = ok ? 0 : 2;
 }
 
 // Householder reduction of the symmetric n x n A (lower triangle used) to tridiagonal form.

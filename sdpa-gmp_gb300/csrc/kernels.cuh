@@ -113,6 +113,10 @@ template <int N>
 void ml_potrs_prepare(int n, const mlf<N> *L, int ldl, mlf<N> *Dinv, cudaStream_t s);
 template <int N>
 void ml_potrs_solve(int n, const mlf<N> *L, int ldl, const mlf<N> *Dinv, mlf<N> *x, cudaStream_t s);
+// device word inside the prepared data that a solve sets to 1 if one of its bounded
+// waits timed out (the solution is then invalid); reset by every solve
+template <int N>
+int *ml_potrs_status(int n, mlf<N> *Dinv);
 
 // ---- eigenvalues (eig.cu) ---------------------------------------------------------
 // y = op(A) x for a dense n x n A (op: 'N' plain, 'T' transpose; A lower-triangular

@@ -436,24 +436,10 @@ MLHD double ml_to_double(const mlf<N> &a) {
     return a.s ? -v : v;
 }
 
-// Mantissa as a double in [0.5, 1) (exponent dropped); used to seed Newton iterations.
-template <int N>
-MLHD double ml_mant_double(const mlf<N> &a) {
-    const uint64_t top = ((uint64_t)a.m[N - 1] << 32) | a.m[N - 2];
-    return (double)(top >> 11) * 0x1p-53;
-}
-
 template <int N>
 MLHD mlf<N> ml_one() { return ml_from_int<N>(1); }
 
 // --- division and square root (Newton-Raphson on the mantissa) -------------------
-
-template <int N>
-struct ml_newton_steps {
-    // bits doubled per step from a 50-bit seed until >= 32N + 8
-    static constexpr int value = (32 * N + 8 <= 100) ? 1 : (32 * N + 8 <= 200) ? 2 : (32 * N + 8 <= 400) ? 3
-                                 : (32 * N + 8 <= 800) ? 4 : 5;
-};
 
 // Precision conversions: keep the top M limbs (truncating) / extend with zero limbs.
 template <int M, int N>
@@ -475,50 +461,41 @@ MLHD mlf<M> ml_widen(const mlf<N> &a) {
     return r;
 }
 
-// Double-double seeds (about 106 correct bits) for the reciprocal and the inverse
-// square root of a mantissa, from one Newton step carried out in double-double
-// arithmetic with fused multiply-adds (error-free products).  The value is returned
-// as hi + lo.
-MLHD void ml_dd_two_prod(double a, double b, double *p, double *e) {
-    *p = a * b;
-    *e = fma(a, b, -*p);
+// Single-precision seeds.  The FP32 units give a 22-24 bit start in a few dozen
+// cycles (FP64 is far slower on this part), and Newton steps carried out in the
+// multi-limb format at rising precision take it from there.
+template <int N>
+MLHD mlf<N> ml_from_float_pos(float x) {  // x > 0, finite and normal
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    mlf<N> r = ml_zero<N>();
+    r.m[N - 1] = ((u & 0x7fffffu) | 0x800000u) << 8;
+    r.e = (int)((u >> 23) & 0xff) - 126;
+    return r;
 }
 
 template <int N>
-MLHD void ml_dd_of(const mlf<N> &a, double *hi, double *lo) {
-    // top 106 bits of the mantissa as an exact double-double (exponent dropped: a in [1/2,1) or [1/4,1))
-    const uint64_t t0 = ((uint64_t)a.m[N - 1] << 32) | a.m[N - 2];
-    const uint64_t t1 = ((uint64_t)a.m[N - 3] << 32) | (N >= 4 ? a.m[N - 4] : 0u);
-    const double h = ldexp((double)(t0 >> 11), a.e - 53);
-    const double l = ldexp((double)(((t0 & 0x7ffull) << 42) | (t1 >> 22)), a.e - 106);
-    *hi = h + l;
-    *lo = l - (*hi - h);
+MLHD mlf<N> ml_from_float(float x) {  // finite x; subnormals become zero
+    if (!(fabsf(x) >= 1.17549435e-38f)) return ml_zero<N>();
+    mlf<N> r = ml_from_float_pos<N>(fabsf(x));
+    r.s = x < 0.0f ? 1u : 0u;
+    return r;
 }
 
-// 1/x for x = xh + xl in [1/2, 1): ~106 bits
-MLHD void ml_dd_recip(double xh, double xl, double *rh, double *rl) {
-    const double r0 = 1.0 / xh;
-    double p, e;
-    ml_dd_two_prod(xh, r0, &p, &e);
-    // t = 1 - x r0 (exact to ~2^-106 thanks to the error-free product)
-    const double t = ((1.0 - p) - e) - xl * r0;
-    *rh = r0;
-    *rl = r0 * t;
-}
-
-// 1/sqrt(x) for x = xh + xl in [1/4, 1): ~106 bits
-MLHD void ml_dd_rsqrt(double xh, double xl, double *rh, double *rl) {
-    const double y0 = 1.0 / sqrt(xh);
-    double s, se, p, pe;
-    ml_dd_two_prod(y0, y0, &s, &se);      // y0^2 = s + se exactly
-    ml_dd_two_prod(xh, s, &p, &pe);       // xh * s exactly
-    const double t = ((1.0 - p) - pe) - (xh * se + xl * s);  // 1 - x y0^2
-    *rh = y0;
-    *rl = 0.5 * y0 * t;
-}
-
+// top 24 bits of the mantissa scaled by 2^e, as a float (e is 0 or 1 here)
 template <int N>
-MLHD mlf<N> ml_from_dd(double hi, double lo) { return ml_add(ml_from_double<N>(hi), ml_from_double<N>(lo)); }
+MLHD float ml_mant_float(const mlf<N> &a) {
+    const float f = (float)(a.m[N - 1] >> 8) * 5.9604644775390625e-8f;  // 2^-24
+    return a.e > 0 ? 2.0f * f : f;
+}
+
+MLHD float ml_rsqrt_float(float f) {
+#ifdef __CUDA_ARCH__
+    return rsqrtf(f);
+#else
+    return 1.0f / sqrtf(f);
+#endif
+}
 
 // 1/bn for a mantissa bn in [1/2, 1): Newton steps at rising precision (N/2 first,
 // then one step at N doubles the correct bits), so only the last steps pay full cost.
@@ -527,7 +504,8 @@ MLHD mlf<N> ml_recip_mant(const mlf<N> &bn) {
     const mlf<N> one = ml_one<N>();
     mlf<N> x;
     if constexpr (N <= 2) {
-        x = ml_from_double<N>(1.0 / ml_mant_double(bn));
+        x = ml_from_float_pos<N>(1.0f / ml_mant_float(bn));  // ~23 bits
+        x = ml_add(x, ml_mul(x, ml_sub(one, ml_mul(bn, x))));
     } else {
         x = ml_widen<N, N / 2>(ml_recip_mant<N / 2>(ml_narrow<N / 2, N>(bn)));
     }
@@ -549,14 +527,8 @@ MLHD mlf<N> ml_recip(const mlf<N> &b) {
         x = ml_recip_mant<N>(bn);
         x = ml_add(x, ml_mul(x, ml_sub(one, ml_mul(bn, x))));
     } else {
-        if constexpr (N <= 8) {
-            double h, l, rh, rl;
-            ml_dd_of<N>(bn, &h, &l);
-            ml_dd_recip(h, l, &rh, &rl);
-            x = ml_from_dd<N>(rh, rl);  // ~106 bits; one cubic step gives > 300
-        } else {
-            x = ml_widen<N, N / 2>(ml_recip<N / 2>(ml_narrow<N / 2, N>(bn)));  // > 300 bits at N/2 = 8
-        }
+        // N/2 limbs seed: about 62 bits at N/2 = 2, 124 at 4, 248 at 8
+        x = ml_widen<N, N / 2>(ml_recip_mant<N / 2>(ml_narrow<N / 2, N>(bn)));
         const mlf<N> t = ml_sub(one, ml_mul(bn, x));
         constexpr int H = N / 2 + 1;
         const mlf<H> th = ml_narrow<H, N>(t);
@@ -585,7 +557,9 @@ MLHD mlf<N> ml_rsqrt_mant(const mlf<N> &an) {
     const mlf<N> one = ml_one<N>();
     mlf<N> y;
     if constexpr (N <= 2) {
-        y = ml_from_double<N>(1.0 / sqrt(ml_to_double(an)));
+        y = ml_from_float_pos<N>(ml_rsqrt_float(ml_mant_float(an)));  // ~22 bits
+        const mlf<N> t = ml_sub(one, ml_mul(an, ml_mul(y, y)));
+        y = ml_add(y, ml_ldexp(ml_mul(y, t), -1));
     } else {
         y = ml_widen<N, N / 2>(ml_rsqrt_mant<N / 2>(ml_narrow<N / 2, N>(an)));
     }
@@ -609,14 +583,8 @@ MLHD mlf<N> ml_rsqrt(const mlf<N> &a) {
         const mlf<N> t = ml_sub(one, ml_mul(an, ml_mul(y, y)));
         y = ml_add(y, ml_ldexp(ml_mul(y, t), -1));
     } else {
-        if constexpr (N <= 8) {
-            double h, l, rh, rl;
-            ml_dd_of<N>(an, &h, &l);
-            ml_dd_rsqrt(h, l, &rh, &rl);
-            y = ml_from_dd<N>(rh, rl);  // ~106 bits; one cubic step gives > 300
-        } else {
-            y = ml_widen<N, N / 2>(ml_rsqrt<N / 2>(ml_narrow<N / 2, N>(an)));  // > 300 bits at N/2 = 8
-        }
+        // N/2 limbs seed: about 62 bits at N/2 = 2, 124 at 4, 248 at 8
+        y = ml_widen<N, N / 2>(ml_rsqrt_mant<N / 2>(ml_narrow<N / 2, N>(an)));
         const mlf<N> t = ml_sub(one, ml_mul(an, ml_mul(y, y)));
         constexpr int H = N / 2 + 1;
         const mlf<H> th = ml_narrow<H, N>(t);

@@ -162,7 +162,7 @@ inline void ml_decimal_digits(const mlf<N> &a, int ndig, std::string *digits, lo
     M.trim();
     const long e2 = (long)a.e - 32 * N;
     // estimate decimal exponent
-    const double l10 = log10(ml_mant_double(a)) + (double)a.e * 0.30102999566398119521;
+    const double l10 = log10((double)((((uint64_t)a.m[N - 1] << 32) | a.m[N - 2]) >> 11) * 0x1p-53) + (double)a.e * 0.30102999566398119521;
     long E = (long)floor(l10);
     for (int attempt = 0; attempt < 4; ++attempt) {
         // R = floor(|a| * 10^(ndig-1-E))

@@ -1155,6 +1155,13 @@ class Solver final : public SolverBase {
         if (phase_ == pdFEAS && (betaV_ > R(5) || objP_ < objD_)) return stop();
         newton(1);
         step_length(1);
+        {
+            // the Schur solves' bounded waits (step_length has synchronised the streams)
+            int st = 0;
+            d2h_ += (long long)sizeof(int);
+            SDPG_CUDA(cudaMemcpy(&st, ml_potrs_status<N>(m_, Bdinv_), sizeof(int), cudaMemcpyDeviceToHost));
+            if (st != 0) throw sdpg_error(SDPG_ERR_TIMEOUT, "Schur triangular solve: a bounded wait timed out");
+        }
         record_iteration();
         print_iteration(out);
         trace_line();
