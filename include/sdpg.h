@@ -209,6 +209,14 @@ int sdpg_solver_io_bytes(sdpg_solver *h, long long *h2d, long long *d2h);
 /* ---- instrumentation (no reference counterpart) ---------------------------- */
 /* Total kernel launches made by the library in this process. */
 unsigned long long sdpg_launch_count(void);
+/* GEMM method for 256-bit products: 0 (default) the residue-number-system path on the
+ * tcgen05 tensor cores wherever it applies (K <= 1024, not tiny), 1 the integer digit
+ * GEMM everywhere, 2 the residue path for every product with K <= 1024 (tests).
+ * Returns the previous method.  Both paths meet the same error bound. */
+int sdpg_set_gemm_method(int method);
+/* *flag = non-zero if a tensor-core GEMM kernel on `device` ever gave up a bounded wait
+ * (its results are then invalid); solvers check it every iteration. */
+int sdpg_tensor_error(int device, int *flag);
 /* Measured throughput of signed 32x32->64 multiply-adds (IMAD.WIDE) on one GPU, the
  * instruction the multi-limb GEMM is built from; the plain path's roofline denominator. */
 int sdpg_probe_imad_wide(int device, double *ops_per_second);

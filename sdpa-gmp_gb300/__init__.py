@@ -107,6 +107,8 @@ def _setup(lib: ctypes.CDLL) -> ctypes.CDLL:
         "sdpg_solver_gemm_profile": (i, [vp, i, c.POINTER(c.c_double)]),
         "sdpg_solver_io_bytes": (i, [vp, c.POINTER(ll), c.POINTER(ll)]),
         "sdpg_launch_count": (c.c_ulonglong, []),
+        "sdpg_set_gemm_method": (i, [i]),
+        "sdpg_tensor_error": (i, [i, c.POINTER(i)]),
         "sdpg_probe_imad_wide": (i, [i, c.POINTER(c.c_double)]),
         "sdpg_solve_file": (i, [c.c_char_p, c.c_char_p, c.c_char_p, i, c.POINTER(c.c_double)]),
     }
@@ -420,6 +422,18 @@ class Solver:
         a, b = ctypes.c_longlong(), ctypes.c_longlong()
         check(lib().sdpg_solver_io_bytes(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+
+def set_gemm_method(method: int) -> int:
+    """0: tensor-core residue path for 256-bit GEMMs where it applies; 1: digit GEMM only;
+    2: residue path for every 256-bit GEMM with K <= 1024.  Returns the previous method."""
+    return check(lib().sdpg_set_gemm_method(method))
+
+
+def tensor_error(device: int = 0) -> int:
+    flag = ctypes.c_int(0)
+    check(lib().sdpg_tensor_error(device, ctypes.byref(flag)))
+    return flag.value
 
 
 def launch_count() -> int:

@@ -70,7 +70,7 @@ extern "C" int sdpg_rgemm_device_noalloc(int limbs, char transa, char transb, in
             memcpy(&p.beta, beta, sizeof(mlf<N>));
             p.lower_only = 0;
             if (m == 0 || n == 0) return (int)SDPG_OK;
-            const size_t need = gemm_workspace_bytes<N>(p);
+            const size_t need = gemm_bfp_workspace_bytes<N>(p);
             if (need > (size_t)SDPG_NOALLOC_SCRATCH_BYTES)
                 throw sdpg_error(SDPG_ERR_TOO_LARGE,
                                  "sdpg_rgemm_device_noalloc: this product needs " + std::to_string(need) +

@@ -43,6 +43,24 @@ extern "C" {
 
 unsigned long long sdpg_launch_count(void) { return g_kernel_launches; }
 
+int sdpg_set_gemm_method(int method) {
+    return sdpg_guard([&] {
+        if (method < 0 || method > 2) throw sdpg_error(SDPG_ERR_ARG, "method must be 0, 1 or 2");
+        const int old = g_gemm_method;
+        g_gemm_method = method;
+        return old;
+    });
+}
+
+int sdpg_tensor_error(int device, int *flag) {
+    return sdpg_guard([&] {
+        if (!flag) throw sdpg_error(SDPG_ERR_ARG, "null output");
+        SDPG_CUDA(cudaSetDevice(device));
+        SDPG_CUDA(cudaMemcpy(flag, crt_error_word(), sizeof(int), cudaMemcpyDeviceToHost));
+        return (int)SDPG_OK;
+    });
+}
+
 int sdpg_probe_imad_wide(int device, double *ops_per_second) {
     return sdpg_guard([&] {
         if (!ops_per_second) throw sdpg_error(SDPG_ERR_ARG, "null output");

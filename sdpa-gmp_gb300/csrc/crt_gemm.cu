@@ -1,0 +1,328 @@
+// Residue-number-system (Chinese remainder) multi-limb GEMM on the tensor cores, for
+// 256-bit operands.
+//
+//   1. Exponents: EA_i = max_k exponent(op(A)[i,k]), EB_j likewise over op(B)[:,j].
+//   2. Residues: each entry becomes the integer X = trunc(x 2^(R - E)), |X| < 2^R with
+//      R = 276, and is stored as its balanced residues modulo L = 70 primes below 512
+//      (fp16, exact), K contiguous.
+//   3. Tensor cores (tc_gemm.cu): for each prime, S = A_l B_l^T exactly in fp32, then
+//      y_l = (S mod m_l) (M / m_l)^-1 mod m_l.
+//   4. Reconstruction: the exact sum V = sum_k X_ik X_kj satisfies
+//      V / M = sum_l y_l / m_l (mod 1) with |V / M| < 2^-6, so V / M is the centred
+//      fractional part of that sum, formed in 320-bit fixed point; then
+//      C = alpha V 2^(EA_i + EB_j - 2R) + beta C.
+//
+// The only rounding is the truncation of the inputs to R bits (relative 2^-276 of
+// the row / column maximum) and the final conversion to 256 bits, so the error obeys
+// the same normwise bound as the digit GEMM in gemm.cu.
+#include <mutex>
+
+#include "crt_tables.h"
+#include "gemm.cuh"
+#include "tc_gemm.cuh"
+
+namespace sdpg {
+
+namespace {
+
+__constant__ int c_moduli[kCrtL];
+__constant__ int c_pow16[kCrtL][kCrtPowChunks];
+__constant__ uint32_t c_inv[kCrtL][kCrtInvWords];
+__constant__ uint32_t c_mtot[8];
+__device__ int d_moduli[kCrtL];
+__device__ int d_cfac[kCrtL];
+__device__ int d_error;
+
+struct CrtDevice {
+    int *moduli = nullptr, *cfac = nullptr, *error = nullptr;
+};
+
+// Per device: upload the tables once and look up the global-memory copies' addresses.
+CrtDevice crt_device() {
+    static std::mutex mu;
+    static CrtDevice cache[64];
+    static bool ready[64] = {};
+    int dev = 0;
+    SDPG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) throw sdpg_error(SDPG_ERR_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ready[dev]) {
+        SDPG_CUDA(cudaMemcpyToSymbol(c_moduli, kCrtModuli, sizeof(kCrtModuli)));
+        SDPG_CUDA(cudaMemcpyToSymbol(c_pow16, kCrtPow16, sizeof(kCrtPow16)));
+        SDPG_CUDA(cudaMemcpyToSymbol(c_inv, kCrtInv, sizeof(kCrtInv)));
+        SDPG_CUDA(cudaMemcpyToSymbol(c_mtot, kCrtMtotMant, sizeof(kCrtMtotMant)));
+        SDPG_CUDA(cudaMemcpyToSymbol(d_moduli, kCrtModuli, sizeof(kCrtModuli)));
+        SDPG_CUDA(cudaMemcpyToSymbol(d_cfac, kCrtCfac, sizeof(kCrtCfac)));
+        CrtDevice c;
+        SDPG_CUDA(cudaGetSymbolAddress((void **)&c.moduli, d_moduli));
+        SDPG_CUDA(cudaGetSymbolAddress((void **)&c.cfac, d_cfac));
+        SDPG_CUDA(cudaGetSymbolAddress((void **)&c.error, d_error));
+        cache[dev] = c;
+        ready[dev] = true;
+    }
+    return cache[dev];
+}
+
+constexpr int kExpWarps = 8;
+
+template <int N>
+__global__ void crt_exp_kernel(Operand<N> X, int O, int K, int Opad, int *E) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int o = blockIdx.x * kExpWarps + warp;
+    const int b = blockIdx.y;
+    if (o >= Opad) return;
+    int emax = INT_MIN;
+    if (o < O) {
+        const mlf<N> *base = X.X + b * X.sb + o * X.so;
+        for (int k = lane; k < K; k += 32) {
+            const mlf<N> *v = base + k * X.sk;
+            if (v->m[N - 1] != 0) emax = max(emax, v->e);
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, off));
+    if (lane == 0) E[(long long)b * Opad + o] = (emax == INT_MIN) ? 0 : emax;
+}
+
+// Residues of op(X)[o,k] scaled to an integer below 2^R: Q[(b L + l)][o][k], padded
+// entries zero.  Threads run along k so that each modulus plane is written in
+// contiguous 64-byte rows.
+template <int N>
+__global__ void __launch_bounds__(256)
+    crt_residue_kernel(Operand<N> X, int O, int K, int Opad, int Kpad, const int *E, __half *Q) {
+    constexpr int R = kCrtR;
+    constexpr int LB = 10;
+    const int k = blockIdx.x * 32 + threadIdx.x;
+    const int o = blockIdx.y * 8 + threadIdx.y;
+    const int b = blockIdx.z;
+    if (o >= Opad || k >= Kpad) return;
+    uint32_t chunk[kCrtPowChunks];
+#pragma unroll
+    for (int c = 0; c < kCrtPowChunks; ++c) chunk[c] = 0;
+    bool neg = false;
+    if (o < O && k < K) {
+        const mlf<N> v = X.X[b * X.sb + o * X.so + k * X.sk];
+        if (v.m[N - 1] != 0) {
+            const int s = v.e - E[(long long)b * Opad + o] + R - 32 * N;  // integer = M * 2^s
+            if (s > -32 * N) {
+                uint32_t T[LB];
+#pragma unroll
+                for (int w = 0; w < LB; ++w) T[w] = (w < N) ? v.m[w] : 0u;
+                if (s >= 0) {
+                    ml_limb_shl<LB>(T, s >> 5);
+                    ml_bit_shl<LB>(T, s & 31);
+                } else {
+                    ml_limb_shr<LB>(T, (-s) >> 5);
+                    ml_bit_shr<LB>(T, (-s) & 31);
+                }
+#pragma unroll
+                for (int c = 0; c < kCrtPowChunks; ++c) chunk[c] = (T[c >> 1] >> (16 * (c & 1))) & 0xFFFFu;
+                neg = v.s != 0;
+            }
+        }
+    }
+    __half *q = Q + ((long long)b * kCrtL * Opad + o) * Kpad + k;
+    const long long plane = (long long)Opad * Kpad;
+#pragma unroll 2
+    for (int l = 0; l < kCrtL; ++l) {
+        const int m = c_moduli[l];
+        int acc = 0;  // < 18 * 65535 * 511 < 2^31
+#pragma unroll
+        for (int c = 0; c < kCrtPowChunks; ++c) acc += (int)chunk[c] * c_pow16[l][c];
+        int r = acc - (int)((float)acc * (1.0f / (float)m)) * m;
+        if (r < 0) r += m;
+        if (r >= m) r -= m;
+        if (2 * r > m) r -= m;  // balanced: |r| <= (m - 1) / 2
+        if (neg) r = -r;
+        q[l * plane] = __int2half_rn(r);
+    }
+}
+
+// V / M as the centred fractional part of sum_l y_l / m_l (320-bit fixed point), then
+// C = alpha V 2^(EA + EB - 2R) + beta C.  Threads run along j (contiguous y loads).
+template <int N>
+__global__ void __launch_bounds__(128)
+    crt_reconstruct_kernel(const uint16_t *Y, int Mpad, int Npad, const int *EA, const int *EB, long long sEA,
+                           long long sEB, int b0, int alpha_one, GemmProblem<N> p) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    const int bl = blockIdx.z;
+    if (i >= p.M || j >= p.Nn || (p.lower_only && i < j)) return;
+    const uint16_t *y = Y + ((long long)bl * kCrtL * Mpad + i) * Npad + j;
+    const long long plane = (long long)Mpad * Npad;
+    unsigned long long acc[kCrtInvWords];
+#pragma unroll
+    for (int w = 0; w < kCrtInvWords; ++w) acc[w] = 0;
+#pragma unroll 2
+    for (int l = 0; l < kCrtL; ++l) {
+        const uint32_t yl = y[l * plane];
+#pragma unroll
+        for (int w = 0; w < kCrtInvWords; ++w) acc[w] += (unsigned long long)yl * c_inv[l][w];
+    }
+    uint32_t W[kCrtInvWords];
+    unsigned long long carry = 0;
+#pragma unroll
+    for (int w = 0; w < kCrtInvWords; ++w) {
+        const unsigned long long t = acc[w] + carry;
+        W[w] = (uint32_t)t;
+        carry = t >> 32;
+    }
+    // the integer part (carry out of the top word) is dropped: fractional part in [0, 1)
+    const uint32_t neg = W[kCrtInvWords - 1] >> 31;
+    if (neg) {  // f >= 1/2: V / M = f - 1 < 0; magnitude 2^320 - f
+        unsigned long long c = 1;
+#pragma unroll
+        for (int w = 0; w < kCrtInvWords; ++w) {
+            const unsigned long long t = (unsigned long long)(~W[w]) + c;
+            W[w] = (uint32_t)t;
+            c = t >> 32;
+        }
+    }
+    const mlf<N> frac = ml_pack<N, kCrtInvWords>(W, 0, neg);  // |V| / M
+    mlf<N> Mt;
+    Mt.e = kCrtMtotExp;
+    Mt.s = 0;
+#pragma unroll
+    for (int w = 0; w < N; ++w) Mt.m[w] = c_mtot[w];
+    mlf<N> v = ml_mul(frac, Mt);
+    const int bg = b0 + bl;
+    v = ml_ldexp(v, EA[bl * sEA + i] + EB[bl * sEB + j] - 2 * kCrtR);
+    if (!alpha_one) v = ml_mul(v, p.alpha);
+    mlf<N> *cp = p.C + bg * p.sc + i + (long long)j * p.ldc;
+    if (!ml_is_zero(p.beta)) v = ml_add(v, ml_mul(p.beta, *cp));
+    *cp = v;
+}
+
+struct CrtLayout {
+    int Mpad, Npad, Kpad, G, groups;
+    size_t ea, eb, qa, qb, y;
+    size_t total() const { return ea + eb + qa + qb + y + 6 * 256; }
+};
+
+constexpr size_t kCrtBudget = (size_t)384 << 20;  // scratch per pass; larger batches run in groups
+
+template <int N>
+CrtLayout crt_layout(const GemmProblem<N> &p) {
+    CrtLayout L;
+    L.Mpad = (int)round_up(p.M, kTcBM);
+    L.Npad = (int)round_up(p.Nn, kTcBN);
+    L.Kpad = (int)round_up(p.K, kTcBK);
+    const bool ab = p.A.sb != 0, bb = p.B.sb != 0;
+    const size_t qa1 = (size_t)kCrtL * L.Mpad * L.Kpad * 2, qb1 = (size_t)kCrtL * L.Npad * L.Kpad * 2;
+    const size_t y1 = (size_t)kCrtL * L.Mpad * L.Npad * 2;
+    const size_t per = (ab ? qa1 + L.Mpad * 4 : 0) + (bb ? qb1 + L.Npad * 4 : 0) + y1;
+    const size_t fixed = (ab ? 0 : qa1 + L.Mpad * 4) + (bb ? 0 : qb1 + L.Npad * 4);
+    size_t G = kCrtBudget > fixed + per ? (kCrtBudget - fixed) / per : 1;
+    if (G < 1) G = 1;
+    if (G > (size_t)p.batch) G = p.batch;
+    L.G = (int)G;
+    L.groups = (p.batch + L.G - 1) / L.G;
+    L.ea = (size_t)(ab ? G : 1) * L.Mpad * 4;
+    L.eb = (size_t)(bb ? G : 1) * L.Npad * 4;
+    L.qa = (ab ? G : 1) * qa1;
+    L.qb = (bb ? G : 1) * qb1;
+    L.y = G * y1;
+    return L;
+}
+
+inline char *align256(char *p) { return (char *)(((uintptr_t)p + 255) & ~(uintptr_t)255); }
+
+}  // namespace
+
+// 0: tensor-core residue path where it applies and the product is not tiny;
+// 1: digit GEMM only; 2: residue path for every 256-bit product with K <= 1024
+int g_gemm_method = 0;
+
+template <int N>
+bool crt_gemm_applies(const GemmProblem<N> &p) {
+    if constexpr (N != 8) {
+        return false;
+    } else {
+        if (g_gemm_method == 1 || p.K <= 0 || p.K > kTcMaxK || p.M <= 0 || p.Nn <= 0) return false;
+        return g_gemm_method == 2 || (double)p.M * p.Nn * p.K * p.batch >= (double)(1 << 21);
+    }
+}
+
+template <int N>
+size_t crt_gemm_workspace_bytes(const GemmProblem<N> &p) {
+    return crt_layout<N>(p).total();
+}
+
+template <int N>
+void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
+    if constexpr (N != 8) {
+        throw sdpg_error(SDPG_ERR_ARG, "residue GEMM path is for 256-bit operands");
+    } else {
+        const CrtLayout L = crt_layout<N>(p);
+        const CrtDevice dev = crt_device();
+        char *cur = align256((char *)scratch);
+        int *EA = (int *)cur;
+        cur = align256(cur + L.ea);
+        int *EB = (int *)cur;
+        cur = align256(cur + L.eb);
+        __half *QA = (__half *)cur;
+        cur = align256(cur + L.qa);
+        __half *QB = (__half *)cur;
+        cur = align256(cur + L.qb);
+        uint16_t *Y = (uint16_t *)cur;
+        const bool ab = p.A.sb != 0, bb = p.B.sb != 0;
+        const mlf<N> one = ml_one<N>();
+        const int alpha_one = memcmp(&one, &p.alpha, sizeof(one)) == 0;
+        for (int g = 0; g < L.groups; ++g) {
+            const int b0 = g * L.G;
+            const int G = min(L.G, p.batch - b0);
+            const int gA = ab ? G : 1, gB = bb ? G : 1;
+            if (g == 0 || ab) {
+                Operand<N> A = p.A;
+                A.X += (long long)b0 * A.sb;
+                crt_exp_kernel<N><<<dim3(ceil_div(L.Mpad, kExpWarps), gA), 32 * kExpWarps, 0, s>>>(A, p.M, p.K, L.Mpad, EA);
+                SDPG_CHECK_LAUNCH();
+                crt_residue_kernel<N><<<dim3(L.Kpad / 32, L.Mpad / 8, gA), dim3(32, 8), 0, s>>>(A, p.M, p.K, L.Mpad,
+                                                                                            L.Kpad, EA, QA);
+                SDPG_CHECK_LAUNCH();
+            }
+            if (g == 0 || bb) {
+                Operand<N> B = p.B;
+                B.X += (long long)b0 * B.sb;
+                crt_exp_kernel<N><<<dim3(ceil_div(L.Npad, kExpWarps), gB), 32 * kExpWarps, 0, s>>>(B, p.Nn, p.K, L.Npad, EB);
+                SDPG_CHECK_LAUNCH();
+                crt_residue_kernel<N><<<dim3(L.Kpad / 32, L.Npad / 8, gB), dim3(32, 8), 0, s>>>(B, p.Nn, p.K, L.Npad,
+                                                                                            L.Kpad, EB, QB);
+                SDPG_CHECK_LAUNCH();
+            }
+            TcModGemm t{};
+            t.A = QA;
+            t.B = QB;
+            t.Y = Y;
+            t.L = kCrtL;
+            t.batch = G;
+            t.a_batched = ab;
+            t.b_batched = bb;
+            t.Mpad = L.Mpad;
+            t.Npad = L.Npad;
+            t.Kpad = L.Kpad;
+            t.lower_only = p.lower_only;
+            t.moduli = dev.moduli;
+            t.cfac = dev.cfac;
+            t.error = dev.error;
+            if (p.ev_before) SDPG_CUDA(cudaEventRecord(p.ev_before, s));
+            tc_modgemm(t, s);
+            if (p.ev_after) SDPG_CUDA(cudaEventRecord(p.ev_after, s));
+            crt_reconstruct_kernel<N><<<dim3(ceil_div(p.Nn, 128), p.M, G), 128, 0, s>>>(
+                Y, L.Mpad, L.Npad, EA, EB, ab ? L.Mpad : 0, bb ? L.Npad : 0, b0, alpha_one, p);
+            SDPG_CHECK_LAUNCH();
+        }
+    }
+}
+
+// device word set by the tensor-core kernel when one of its bounded waits timed out
+int *crt_error_word() { return crt_device().error; }
+
+template bool crt_gemm_applies<8>(const GemmProblem<8> &);
+template bool crt_gemm_applies<16>(const GemmProblem<16> &);
+template size_t crt_gemm_workspace_bytes<8>(const GemmProblem<8> &);
+template size_t crt_gemm_workspace_bytes<16>(const GemmProblem<16> &);
+template void crt_gemm<8>(const GemmProblem<8> &, void *, cudaStream_t);
+template void crt_gemm<16>(const GemmProblem<16> &, void *, cudaStream_t);
+
+}  // namespace sdpg

@@ -265,8 +265,13 @@ inline char *align256(char *p) { return (char *)(((uintptr_t)p + 255) & ~(uintpt
 }  // namespace
 
 template <int N>
-size_t gemm_workspace_bytes(const GemmProblem<N> &p) {
+size_t gemm_bfp_workspace_bytes(const GemmProblem<N> &p) {
     return gemm_layout<N>(p).total();
+}
+
+template <int N>
+size_t gemm_workspace_bytes(const GemmProblem<N> &p) {
+    return crt_gemm_applies<N>(p) ? crt_gemm_workspace_bytes<N>(p) : gemm_bfp_workspace_bytes<N>(p);
 }
 
 template <int N>
@@ -319,13 +324,19 @@ void ml_gemm_scratch(const GemmProblem<N> &p, void *scratch, cudaStream_t stream
 
 template <int N>
 void ml_gemm(const GemmProblem<N> &p, Workspace &ws, cudaStream_t stream) {
-    const size_t need = gemm_workspace_bytes(p);
-    void *s = ws.carve(need);
+    if (p.M <= 0 || p.Nn <= 0 || p.batch <= 0) return;
+    if (crt_gemm_applies<N>(p)) {
+        void *s = ws.carve(crt_gemm_workspace_bytes<N>(p));
+        crt_gemm<N>(p, s, stream);
+        return;
+    }
+    void *s = ws.carve(gemm_bfp_workspace_bytes<N>(p));
     ml_gemm_scratch(p, s, stream);
 }
 
 #define SDPG_INST_GEMM(N)                                                                  \
     template size_t gemm_workspace_bytes<N>(const GemmProblem<N> &);                        \
+    template size_t gemm_bfp_workspace_bytes<N>(const GemmProblem<N> &);                    \
     template void ml_gemm_scratch<N>(const GemmProblem<N> &, void *, cudaStream_t);        \
     template void ml_gemm<N>(const GemmProblem<N> &, Workspace &, cudaStream_t);
 SDPG_INST_GEMM(8)

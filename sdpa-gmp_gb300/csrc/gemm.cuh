@@ -65,17 +65,33 @@ inline Operand<N> operand_B(char trans, const mlf<N> *B, long long ldb, long lon
     return Operand<N>{B, 1, ldb, sB};
 }
 
-// Workspace bytes ml_gemm needs for this problem.
+// Workspace bytes ml_gemm needs for this problem (for whichever method it selects).
 template <int N>
 size_t gemm_workspace_bytes(const GemmProblem<N> &p);
 
-// Runs the quantisers and the digit GEMM on `stream`; scratch is carved from ws
-// (which must already hold gemm_workspace_bytes(p) beyond ws.used).
+// Runs the GEMM on `stream`; scratch is carved from ws (which must already hold
+// gemm_workspace_bytes(p) beyond ws.used).  256-bit products with K <= 1024 that are
+// not tiny go through the residue-number-system path on the tensor cores
+// (crt_gemm.cu); everything else through the digit GEMM below.
 template <int N>
 void ml_gemm(const GemmProblem<N> &p, Workspace &ws, cudaStream_t stream);
 
-// Same, with caller-provided scratch of at least gemm_workspace_bytes(p) bytes.
+// The digit GEMM alone, with caller-provided scratch of at least
+// gemm_bfp_workspace_bytes(p) bytes.
+template <int N>
+size_t gemm_bfp_workspace_bytes(const GemmProblem<N> &p);
 template <int N>
 void ml_gemm_scratch(const GemmProblem<N> &p, void *scratch, cudaStream_t stream);
+
+// Residue-number-system path (crt_gemm.cu).
+extern int g_gemm_method;  // 0: residue path where it applies, 1: digit GEMM only, 2: residue path always
+template <int N>
+bool crt_gemm_applies(const GemmProblem<N> &p);
+template <int N>
+size_t crt_gemm_workspace_bytes(const GemmProblem<N> &p);
+template <int N>
+void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t stream);
+// device word that the tensor-core kernel sets when a bounded wait timed out
+int *crt_error_word();
 
 }  // namespace sdpg

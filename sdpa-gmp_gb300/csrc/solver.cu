@@ -1161,6 +1161,11 @@ class Solver final : public SolverBase {
             d2h_ += (long long)sizeof(int);
             SDPG_CUDA(cudaMemcpy(&st, ml_potrs_status<N>(m_, Bdinv_), sizeof(int), cudaMemcpyDeviceToHost));
             if (st != 0) throw sdpg_error(SDPG_ERR_TIMEOUT, "Schur triangular solve: a bounded wait timed out");
+            if (N == 8 && g_gemm_method == 0) {
+                d2h_ += (long long)sizeof(int);
+                SDPG_CUDA(cudaMemcpy(&st, crt_error_word(), sizeof(int), cudaMemcpyDeviceToHost));
+                if (st != 0) throw sdpg_error(SDPG_ERR_TIMEOUT, "tensor-core GEMM: a bounded wait timed out");
+            }
         }
         record_iteration();
         print_iteration(out);

@@ -1,0 +1,336 @@
+// tcgen05 modular GEMM: TMA loads of 128 x 64 fp16 tiles (128-byte swizzle) into a
+// three-stage shared-memory ring, one thread issuing tcgen05.mma (M = N = 128,
+// K = 16) into fp32 accumulators in tensor memory, and a four-warp epilogue that
+// reads the accumulators with tcgen05.ld and reduces them modulo the tile's prime.
+//
+// Every wait on an mbarrier is bounded by a cycle budget; on time-out the kernel
+// records an error, lets the copies and products it issued finish (again with a
+// bound), frees its tensor memory and returns.
+#include <cuda.h>
+
+#include <mutex>
+
+#include "tc_gemm.cuh"
+
+namespace sdpg {
+
+namespace {
+
+constexpr int kStages = 3;
+constexpr int kTileBytes = kTcBM * kTcBK * 2;  // 16 KB, A and B tiles alike (BM == BN)
+constexpr int kStageBytes = 2 * kTileBytes;
+constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 256;
+constexpr long long kWaitCycles = 1ll << 31;  // about one second at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// false if the phase with the given parity has not completed within the budget
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > kWaitCycles) return false;
+    return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];" ::"r"(dst),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "setp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+        "}\n" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+// thread t of the warp receives 32 consecutive 32-bit columns of tensor-memory lane (base lane + t)
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Shared-memory matrix descriptor for a K-major tile written by TMA with the 128-byte
+// swizzle: rows of 128 bytes, 8-row groups 1024 bytes apart.  The start address of
+// the kk-th K = 16 slice is the tile base plus 32 kk bytes.
+__device__ __forceinline__ uint64_t sw128_kmajor_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);  // start address >> 4
+    d |= (uint64_t)1 << 16;                   // leading-dimension byte offset (unused with this swizzle)
+    d |= (uint64_t)(1024 >> 4) << 32;         // stride-dimension byte offset: one 8-row group
+    d |= (uint64_t)1 << 46;                   // descriptor version
+    d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor, kind::f16: fp32 accumulator, fp16 A and B, both K-major, M x N.
+constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(kTcBN >> 3) << 17) |
+                            ((uint32_t)(kTcBM >> 4) << 24);
+
+__device__ __forceinline__ int mod_of_float(float S, int m, float inv_m) {
+    // S is an integer-valued float, |S| < 2^24: S - m floor(S/m), corrected by one step
+    const float q = floorf(S * inv_m);
+    int r = (int)fmaf(-q, (float)m, S);
+    if (r < 0) r += m;
+    if (r >= m) r -= m;
+    return r;
+}
+
+__device__ __forceinline__ int mulmod(int a, int b, int m, float inv_m) {
+    const int p = a * b;  // < 2^18
+    int q = (int)((float)p * inv_m);
+    int r = p - q * m;
+    if (r < 0) r += m;
+    if (r >= m) r -= m;
+    return r;
+}
+
+__global__ void __launch_bounds__(128, 1)
+    tc_modgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcModGemm p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
+    uint64_t *full = bars;                 // kStages
+    uint64_t *empty = bars + kStages;      // kStages
+    uint64_t *done = bars + 2 * kStages;   // 1
+    uint32_t *tmem_slot = (uint32_t *)(bars + 2 * kStages + 1);
+    __shared__ int abort_flag;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n0 = blockIdx.x * kTcBN, m0 = blockIdx.y * kTcBM;
+    if (p.lower_only && n0 > m0 + kTcBM - 1) return;  // whole tile above the diagonal
+    const int z = blockIdx.z;
+    const int b = z / p.L, l = z - b * p.L;
+    const int arow = ((p.a_batched ? b : 0) * p.L + l) * p.Mpad + m0;
+    const int brow = ((p.b_batched ? b : 0) * p.L + l) * p.Npad + n0;
+    const int nk = p.Kpad / kTcBK;
+    const int nacc = (p.Kpad + kTcKChunk - 1) / kTcKChunk;
+    const uint32_t ncols = nacc <= 1 ? 128u : nacc <= 2 ? 256u : 512u;
+
+    if (threadIdx.x == 0) {
+        abort_flag = 0;
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        mbar_init(smem_u32(done), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) {
+        tmem_alloc(smem_u32(tmem_slot), ncols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (threadIdx.x == 0) {
+        // producer: TMA into the stage ring
+        int issued = 0;
+        bool ok = true;
+        for (int kb = 0; kb < nk; ++kb) {
+            const int s = kb % kStages;
+            if (kb >= kStages && !mbar_wait(smem_u32(&empty[s]), ((kb / kStages) - 1) & 1)) {
+                ok = false;
+                break;
+            }
+            const uint32_t fb = smem_u32(&full[s]);
+            mbar_expect_tx(fb, kStageBytes);
+            uint8_t *st = smem + s * kStageBytes;
+            tma_load_2d(smem_u32(st), &tmA, kb * kTcBK, arow, fb);
+            tma_load_2d(smem_u32(st + kTileBytes), &tmB, kb * kTcBK, brow, fb);
+            ++issued;
+        }
+        if (!ok) {
+            atomicExch(p.error, 1);
+            abort_flag = 1;
+            // let the copies already issued land before the CTA goes away
+            for (int kb = (issued > kStages ? issued - kStages : 0); kb < issued; ++kb)
+                mbar_wait(smem_u32(&full[kb % kStages]), (kb / kStages) & 1);
+        }
+    } else if (threadIdx.x == 32) {
+        // MMA issuer
+        bool ok = true;
+        for (int kb = 0; kb < nk; ++kb) {
+            const int s = kb % kStages;
+            if (!mbar_wait(smem_u32(&full[s]), (kb / kStages) & 1)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const int acc = (kb * kTcBK) / kTcKChunk;
+            const bool first = (kb * kTcBK) % kTcKChunk == 0;
+            const uint32_t dt = tmem + (uint32_t)(acc * kTcBN);
+            uint8_t *st = smem + s * kStageBytes;
+            const uint64_t ad = sw128_kmajor_desc(smem_u32(st));
+            const uint64_t bd = sw128_kmajor_desc(smem_u32(st + kTileBytes));
+#pragma unroll
+            for (int kk = 0; kk < kTcBK / 16; ++kk)
+                tc_mma(dt, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), kIdesc, (first && kk == 0) ? 0u : 1u);
+            tc_commit(smem_u32(&empty[s]));
+        }
+        if (!ok) {
+            atomicExch(p.error, 2);
+            abort_flag = 1;
+        }
+        tc_commit(smem_u32(done));  // arrives once every product issued above has completed
+    }
+    __syncwarp();
+    if (!mbar_wait(smem_u32(done), 0)) {
+        atomicExch(p.error, 3);
+        abort_flag = 1;
+    }
+    __syncthreads();
+    tc_fence_after();
+
+    if (!abort_flag) {
+        const int m = p.moduli[l], c = p.cfac[l];
+        const float inv_m = 1.0f / (float)m;
+        const int row = warp * 32 + lane;
+        uint16_t *yrow = p.Y + ((size_t)z * p.Mpad + m0 + row) * p.Npad + n0;
+#pragma unroll 1
+        for (int cb = 0; cb < kTcBN / 32; ++cb) {
+            int r[32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) r[q] = 0;
+#pragma unroll 1
+            for (int a = 0; a < nacc; ++a) {
+                uint32_t v[32];
+                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * kTcBN + cb * 32), v);
+                tmem_ld_wait();
+#pragma unroll
+                for (int q = 0; q < 32; ++q) r[q] += mod_of_float(__uint_as_float(v[q]), m, inv_m);
+            }
+            uint32_t packed[16];
+#pragma unroll
+            for (int q = 0; q < 32; q += 2) {
+                int y0 = r[q] % m, y1 = r[q + 1] % m;
+                y0 = mulmod(y0, c, m, inv_m);
+                y1 = mulmod(y1, c, m, inv_m);
+                packed[q / 2] = (uint32_t)y0 | ((uint32_t)y1 << 16);
+            }
+            uint4 *dst = reinterpret_cast<uint4 *>(yrow + cb * 32);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, ncols);
+    }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = [] {
+        void *ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        SDPG_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !ptr)
+            throw sdpg_error(SDPG_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        return (EncodeTiledFn)ptr;
+    }();
+    return fn;
+}
+
+// 2D fp16 map over `rows` rows of `cols` (contiguous) elements, box 64 x 128, 128-byte swizzle
+CUtensorMap make_map(const __half *base, long long rows, int cols) {
+    CUtensorMap m;
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)kTcBM};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, (void *)base, dims, strides, box, estr,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw sdpg_error(SDPG_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return m;
+}
+
+}  // namespace
+
+void tc_modgemm(const TcModGemm &p, cudaStream_t s) {
+    if (p.Mpad % kTcBM || p.Npad % kTcBN || p.Kpad % kTcBK || p.Kpad <= 0 || p.Kpad > kTcMaxK || p.L <= 0 ||
+        p.batch <= 0)
+        throw sdpg_error(SDPG_ERR_ARG, "tc_modgemm: unsupported shape");
+    if (((uintptr_t)p.A | (uintptr_t)p.B | (uintptr_t)p.Y) & 15)
+        throw sdpg_error(SDPG_ERR_ARG, "tc_modgemm: operands must be 16-byte aligned");
+    static std::once_flag attr_once;
+    std::call_once(attr_once, [] {
+        SDPG_CUDA(cudaFuncSetAttribute(tc_modgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    });
+    const long long arows = (long long)(p.a_batched ? p.batch : 1) * p.L * p.Mpad;
+    const long long brows = (long long)(p.b_batched ? p.batch : 1) * p.L * p.Npad;
+    const CUtensorMap ma = make_map(p.A, arows, p.Kpad);
+    const CUtensorMap mb = make_map(p.B, brows, p.Kpad);
+    dim3 grid(p.Npad / kTcBN, p.Mpad / kTcBM, p.batch * p.L);
+    tc_modgemm_kernel<<<grid, 128, kSmemBytes, s>>>(ma, mb, p);
+    SDPG_CHECK_LAUNCH();
+}
+
+}  // namespace sdpg

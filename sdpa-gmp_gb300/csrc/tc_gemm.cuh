@@ -1,0 +1,42 @@
+// Exact modular GEMMs on the fifth-generation tensor cores (tcgen05).
+//
+// Used by the residue-number-system (Chinese remainder) path of the multi-limb GEMM:
+// every operand entry is an integer held as its residues modulo L small primes
+// m_l < 512, stored as fp16 in the balanced range [-(m_l-1)/2, (m_l-1)/2].  For each
+// modulus the kernel forms S = A_l B_l^T with fp16 products accumulated in fp32 in
+// tensor memory.  Every partial sum is an integer of magnitude at most
+// 256 * 255^2 < 2^24 when at most 256 products are summed, so the fp32 accumulation
+// is exact; longer K is split over up to four accumulators of 256 each.  The
+// epilogue reduces S mod m_l and multiplies by the CRT factor c_l, writing
+// y_l = (S mod m_l) c_l mod m_l.
+#pragma once
+#include <cuda_fp16.h>
+
+#include "common.cuh"
+
+namespace sdpg {
+
+constexpr int kTcBM = 128;      // tile rows (tcgen05 M)
+constexpr int kTcBN = 128;      // tile columns (tcgen05 N)
+constexpr int kTcBK = 64;       // K block: one 128-byte swizzle row of fp16
+constexpr int kTcKChunk = 256;  // products per exact fp32 accumulator
+constexpr int kTcMaxK = 1024;   // four accumulators of 128 columns fill tensor memory
+
+struct TcModGemm {
+    const __half *A;  // planes [zA][Mpad][Kpad], K contiguous
+    const __half *B;  // planes [zB][Npad][Kpad], K contiguous
+    uint16_t *Y;      // planes [z][Mpad][Npad]
+    int L;            // moduli
+    int batch;        // z = b * L + l; A plane (bA * L + l) with bA = b if a_batched else 0
+    int a_batched, b_batched;
+    int Mpad, Npad, Kpad;  // multiples of 128, 128, 64; Kpad <= kTcMaxK
+    int lower_only;        // 1: skip tiles strictly above the diagonal (their Y is not written)
+    const int *moduli;     // device, L entries
+    const int *cfac;       // device, L entries
+    int *error;            // device word: set non-zero if a bounded wait timed out
+};
+
+// Y planes for all (b, l); grid (Npad/128, Mpad/128, batch*L), 128 threads, one tile each.
+void tc_modgemm(const TcModGemm &p, cudaStream_t s);
+
+}  // namespace sdpg

@@ -104,3 +104,14 @@ def test_small_cases_match_reference(sdpg, name, tmp_path):
 @pytest.mark.parametrize("name", LARGE)
 def test_config_shapes_match_reference(sdpg, name, tmp_path):
     check_case(sdpg, name, tmp_path)
+
+
+@pytest.mark.parametrize("name", ["example1", "maxcut40", "control30", "gpp40", "maxcut124pm", "control231"])
+def test_cases_match_reference_with_residue_gemm(sdpg, name, tmp_path):
+    """The same checks with every 256-bit GEMM (K <= 1024) on the tensor-core residue path."""
+    old = sdpg.set_gemm_method(2)
+    try:
+        check_case(sdpg, name, tmp_path)
+        assert sdpg.tensor_error(0) == 0
+    finally:
+        sdpg.set_gemm_method(old)
