@@ -40,6 +40,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "256-bit IPM iters/s (gpp n=500 m=501)"
 UNIT = "iters/s"
+RESIDUE_MODULI = 70  # primes of the 256-bit residue GEMM (csrc/crt_tables.h)
+# DRAM bytes (read + write) per launch of tc_modgemm_kernel for a 500^3 product, from
+# the ncu capture summarised in profiles/tc_modgemm_kernel_gemm500_256bit.md
+TC_TRAFFIC_BYTES = None
 
 
 def workload(precision: int):
@@ -224,22 +228,36 @@ def bench_ours(args) -> None:
     prof = solver.gemm_profile(enable=0)
     timers = solver.timers()
 
-    # roofline of the dominant kernel (the multi-limb digit GEMM) against the measured
-    # IMAD.WIDE throughput of this GPU
-    imad_peak = sdpg.probe_imad_wide(local)
-    D = 10 if args.precision <= 256 else 20
-    imad_per_mac = D * (D + 1) // 2
+    # roofline of the GEMM kernel (the bulk of the arithmetic): at 256 bits the tcgen05
+    # residue GEMM against the measured bf16 tensor peak (fp16 runs at the same rate;
+    # sustained figure, the kernel runs inside a long step); at 512 bits the integer
+    # digit GEMM against the measured IMAD.WIDE throughput.
     gemm_ms = prof["kernel_ms"]
     mac_rate = prof["macs"] / (gemm_ms * 1e-3) if gemm_ms > 0 else 0.0
-    achieved_imad = mac_rate * imad_per_mac
-    roofline = {"bound": "int", "kernel": "bfp_gemm_kernel",
-                "achieved": achieved_imad / 1e12, "peak": imad_peak / 1e12, "unit": "TIMAD.WIDE/s",
-                "frac": achieved_imad / imad_peak if imad_peak else None,
-                "peak_source": "measured in-run by sdpg_probe_imad_wide (MEASURED_PEAKS.json has no integer-pipe figure)",
-                "mac_rate_gmacs": mac_rate / 1e9, "imad_wide_per_mac": imad_per_mac,
-                "launches": prof["launches"], "avg_launch_us": 1e3 * gemm_ms / max(1, prof["launches"]),
-                "share_of_step": gemm_ms / ms if ms > 0 else None,
-                "traffic": None}
+    common = {"launches": prof["launches"], "avg_launch_us": 1e3 * gemm_ms / max(1, prof["launches"]),
+              "share_of_step": gemm_ms / ms if ms > 0 else None, "mac_rate_gmacs": mac_rate / 1e9}
+    if args.precision <= 256:
+        peaks = measured_peaks()
+        peak = peaks.get("bf16_tflops_sustained")
+        src = "bf16_tflops_sustained of measured (MEASURED_PEAKS.json)"
+        if not peak:
+            peak, src = 1700.0, "sustained bf16 fallback"
+        achieved = 2.0 * RESIDUE_MODULI * mac_rate / 1e12
+        roofline = {"bound": "tensor", "kernel": "tc_modgemm_kernel", "achieved": achieved, "peak": peak,
+                    "unit": "TFLOP/s", "frac": achieved / peak, "traffic": TC_TRAFFIC_BYTES, "peak_source": src,
+                    "algorithmic": f"2*M*N*K*{RESIDUE_MODULI} fp16 flops per multi-limb GEMM "
+                                   f"({RESIDUE_MODULI} residue GEMMs)", **common}
+    else:
+        imad_peak = sdpg.probe_imad_wide(local)
+        D = 20
+        imad_per_mac = D * (D + 1) // 2
+        achieved_imad = mac_rate * imad_per_mac
+        roofline = {"bound": "int", "kernel": "bfp_gemm_kernel",
+                    "achieved": achieved_imad / 1e12, "peak": imad_peak / 1e12, "unit": "TIMAD.WIDE/s",
+                    "frac": achieved_imad / imad_peak if imad_peak else None,
+                    "peak_source": "measured in-run by sdpg_probe_imad_wide (MEASURED_PEAKS.json has no "
+                                   "integer-pipe figure)",
+                    "imad_wide_per_mac": imad_per_mac, "traffic": None, **common}
 
     # end to end through the public API: host .dat-s -> parse -> upload -> full solve -> xVec back
     e2e = None
@@ -333,6 +351,7 @@ def bench_gemm(args) -> None:
         return torch.from_numpy(h.view(np.int32)).cuda()
 
     A, B, C = rnd(n * n), rnd(n * n), rnd(n * n)
+    sdpg.set_gemm_method(args.gemm_method)
     one = sdpg.ml_parse(["1"], limbs)
     zero = sdpg.ml_parse(["0"], limbs)
     st = torch.cuda.current_stream().cuda_stream
@@ -351,7 +370,7 @@ def bench_gemm(args) -> None:
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
-    print(json.dumps({"kernel": "gemm", "n": n, "limbs": limbs, "ms_per_gemm": ms,
+    print(json.dumps({"kernel": "gemm", "n": n, "limbs": limbs, "method": args.gemm_method, "ms_per_gemm": ms,
                       "gmacs": n ** 3 / (ms * 1e-3) / 1e9}))
 
 
@@ -360,6 +379,8 @@ def main():
     ap.add_argument("--kernel", choices=["gemm"], default=None,
                     help="kernel mode: time repeated multi-limb GEMMs instead of IPM iterations")
     ap.add_argument("--gemm-n", type=int, default=500)
+    ap.add_argument("--gemm-method", type=int, default=0, choices=[0, 1],
+                    help="kernel mode: 0 tensor-core residue path (256-bit), 1 integer digit GEMM")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)

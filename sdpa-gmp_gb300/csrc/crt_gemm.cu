@@ -87,14 +87,17 @@ __global__ void crt_exp_kernel(Operand<N> X, int O, int K, int Opad, int *E) {
 // Residues of op(X)[o,k] scaled to an integer below 2^R: Q[(b L + l)][o][k], padded
 // entries zero.  Threads run along k so that each modulus plane is written in
 // contiguous 64-byte rows.
+//
+// Small operands are spread over lgroups thread groups per entry, each taking every
+// lgroups-th modulus, so that enough threads are in flight.
 template <int N>
 __global__ void __launch_bounds__(256)
-    crt_residue_kernel(Operand<N> X, int O, int K, int Opad, int Kpad, const int *E, __half *Q) {
+    crt_residue_kernel(Operand<N> X, int O, int K, int Opad, int Kpad, const int *E, __half *Q, int lgroups) {
     constexpr int R = kCrtR;
     constexpr int LB = 10;
     const int k = blockIdx.x * 32 + threadIdx.x;
     const int o = blockIdx.y * 8 + threadIdx.y;
-    const int b = blockIdx.z;
+    const int b = blockIdx.z / lgroups, lg = blockIdx.z - b * lgroups;
     if (o >= Opad || k >= Kpad) return;
     uint32_t chunk[kCrtPowChunks];
 #pragma unroll
@@ -124,7 +127,7 @@ __global__ void __launch_bounds__(256)
     __half *q = Q + ((long long)b * kCrtL * Opad + o) * Kpad + k;
     const long long plane = (long long)Opad * Kpad;
 #pragma unroll 2
-    for (int l = 0; l < kCrtL; ++l) {
+    for (int l = lg; l < kCrtL; l += lgroups) {
         const int m = c_moduli[l];
         int acc = 0;  // < 18 * 65535 * 511 < 2^31
 #pragma unroll
@@ -153,7 +156,7 @@ __global__ void __launch_bounds__(128)
     unsigned long long acc[kCrtInvWords];
 #pragma unroll
     for (int w = 0; w < kCrtInvWords; ++w) acc[w] = 0;
-#pragma unroll 2
+#pragma unroll 10
     for (int l = 0; l < kCrtL; ++l) {
         const uint32_t yl = y[l * plane];
 #pragma unroll
@@ -227,6 +230,12 @@ CrtLayout crt_layout(const GemmProblem<N> &p) {
 
 inline char *align256(char *p) { return (char *)(((uintptr_t)p + 255) & ~(uintptr_t)255); }
 
+// modulus groups per entry for the residue kernel: aim at about 1200 blocks of 256
+inline int residue_groups(long long blocks) {
+    long long g = 1200 / (blocks > 0 ? blocks : 1);
+    return (int)(g < 1 ? 1 : g > 7 ? 7 : g);
+}
+
 }  // namespace
 
 // 0: tensor-core residue path where it applies and the product is not tiny;
@@ -277,8 +286,9 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
                 A.X += (long long)b0 * A.sb;
                 crt_exp_kernel<N><<<dim3(ceil_div(L.Mpad, kExpWarps), gA), 32 * kExpWarps, 0, s>>>(A, p.M, p.K, L.Mpad, EA);
                 SDPG_CHECK_LAUNCH();
-                crt_residue_kernel<N><<<dim3(L.Kpad / 32, L.Mpad / 8, gA), dim3(32, 8), 0, s>>>(A, p.M, p.K, L.Mpad,
-                                                                                            L.Kpad, EA, QA);
+                const int lgA = residue_groups(L.Kpad / 32 * (L.Mpad / 8) * gA);
+                crt_residue_kernel<N><<<dim3(L.Kpad / 32, L.Mpad / 8, gA * lgA), dim3(32, 8), 0, s>>>(
+                    A, p.M, p.K, L.Mpad, L.Kpad, EA, QA, lgA);
                 SDPG_CHECK_LAUNCH();
             }
             if (g == 0 || bb) {
@@ -286,8 +296,9 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
                 B.X += (long long)b0 * B.sb;
                 crt_exp_kernel<N><<<dim3(ceil_div(L.Npad, kExpWarps), gB), 32 * kExpWarps, 0, s>>>(B, p.Nn, p.K, L.Npad, EB);
                 SDPG_CHECK_LAUNCH();
-                crt_residue_kernel<N><<<dim3(L.Kpad / 32, L.Npad / 8, gB), dim3(32, 8), 0, s>>>(B, p.Nn, p.K, L.Npad,
-                                                                                            L.Kpad, EB, QB);
+                const int lgB = residue_groups(L.Kpad / 32 * (L.Npad / 8) * gB);
+                crt_residue_kernel<N><<<dim3(L.Kpad / 32, L.Npad / 8, gB * lgB), dim3(32, 8), 0, s>>>(
+                    B, p.Nn, p.K, L.Npad, L.Kpad, EB, QB, lgB);
                 SDPG_CHECK_LAUNCH();
             }
             TcModGemm t{};

@@ -18,6 +18,7 @@
 #include <float.h>
 
 #include <climits>
+#include <mutex>
 
 #include "kernels.cuh"
 #include "mlwarp.cuh"
@@ -46,6 +47,39 @@ __global__ void matvec_t_kernel(int n, const mlf<N> *A, int tri, const mlf<N> *x
     if (i < hi) a0 = ml_add(a0, ml_mul(col[i], x[i]));
     mlf<N> acc = ml_warp_sum(ml_add(a0, a1));
     if (lane == 0) y[o] = acc;
+}
+
+// The same with four warps per output (each a quarter of the rows, combined in shared
+// memory): four times the warps in flight for the single-vector products of Lanczos.
+constexpr int kMvSplit = 4;
+template <int N>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+    matvec_t_split_kernel(int n, const mlf<N> *A, int tri, const mlf<N> *x, mlf<N> *y) {
+    constexpr int kOut = kWarpsPerBlock / kMvSplit;
+    __shared__ mlf<N> part[kWarpsPerBlock];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int o = blockIdx.x * kOut + warp / kMvSplit, sp = warp % kMvSplit;
+    mlf<N> acc = ml_zero<N>();
+    if (o < n) {
+        const int lo = (tri == 1) ? o : 0;
+        const int hi = (tri == 2) ? o + 1 : n;
+        const mlf<N> *col = A + (long long)o * n;
+        mlf<N> a0 = ml_zero<N>(), a1 = ml_zero<N>();
+        int i = lo + sp * 32 + lane;
+        for (; i + 32 * kMvSplit < hi; i += 64 * kMvSplit) {
+            a0 = ml_add(a0, ml_mul(col[i], x[i]));
+            a1 = ml_add(a1, ml_mul(col[i + 32 * kMvSplit], x[i + 32 * kMvSplit]));
+        }
+        if (i < hi) a0 = ml_add(a0, ml_mul(col[i], x[i]));
+        acc = ml_warp_sum(ml_add(a0, a1));
+    }
+    if (lane == 0) part[warp] = acc;
+    __syncthreads();
+    const int oo = blockIdx.x * kOut + (int)threadIdx.x;
+    if ((int)threadIdx.x < kOut && oo < n) {
+        const mlf<N> *pp = part + threadIdx.x * kMvSplit;
+        y[oo] = ml_add(ml_add(pp[0], pp[1]), ml_add(pp[2], pp[3]));
+    }
 }
 
 // y[o] = sum_j A[o,j] x[j]  (op 'N': rows of A)
@@ -103,16 +137,16 @@ __device__ float ml_to_float_scaled(const mlf<N> &a, int E) {
     return a.s ? -f : f;
 }
 
-// p_k(lam), p_k'(lam) and p_{k-1}(lam) of det(lam I - T) at M limbs, from d, e held at N limbs
+// p_k(lam), p_k'(lam) and p_{k-1}(lam) of det(lam I - T) at M limbs, from the diagonal d
+// and the squared off-diagonal b2 held at N limbs in shared memory
 template <int M, int N>
-__device__ void charpoly_at(int k, const mlf<N> *d, const mlf<N> *e, const mlf<M> &lam, mlf<M> *pk, mlf<M> *dpk,
+__device__ void charpoly_at(int k, const mlf<N> *d, const mlf<N> *b2s, const mlf<M> &lam, mlf<M> *pk, mlf<M> *dpk,
                             mlf<M> *pkm1) {
     mlf<M> p_prev = ml_one<M>(), p_cur = ml_sub(lam, ml_narrow<M, N>(d[0]));
     mlf<M> dp_prev = ml_zero<M>(), dp_cur = ml_one<M>();
     for (int i = 1; i < k; ++i) {
         const mlf<M> a = ml_sub(lam, ml_narrow<M, N>(d[i]));
-        const mlf<M> ei = ml_narrow<M, N>(e[i - 1]);
-        const mlf<M> b2 = ml_mul(ei, ei);
+        const mlf<M> b2 = ml_narrow<M, N>(b2s[i - 1]);
         const mlf<M> p_new = ml_sub(ml_mul(a, p_cur), ml_mul(b2, p_prev));
         const mlf<M> dp_new = ml_sub(ml_add(p_cur, ml_mul(a, dp_cur)), ml_mul(b2, dp_prev));
         p_prev = p_cur;
@@ -128,12 +162,12 @@ __device__ void charpoly_at(int k, const mlf<N> *d, const mlf<N> *e, const mlf<M
 // Newton on det(lam I - T) at M limbs until the step is below 2^-tol of the scale
 // 2^scale_e (at most maxit evaluations).  Returns 1 when that tolerance was met.
 template <int M, int N>
-__device__ int newton_level(int k, const mlf<N> *d, const mlf<N> *e, mlf<M> &lam, int scale_e, int tol, int maxit,
+__device__ int newton_level(int k, const mlf<N> *d, const mlf<N> *b2s, mlf<M> &lam, int scale_e, int tol, int maxit,
                             mlf<M> *pkm1, mlf<M> *dpk) {
     int prev_e = INT_MAX;
     for (int it = 0; it < maxit; ++it) {
         mlf<M> pk;
-        charpoly_at<M, N>(k, d, e, lam, &pk, dpk, pkm1);
+        charpoly_at<M, N>(k, d, b2s, lam, &pk, dpk, pkm1);
         if (ml_is_zero(pk)) return 1;
         if (ml_is_zero(*dpk)) return 0;
         const mlf<M> delta = ml_div(pk, *dpk);
@@ -156,6 +190,7 @@ template <int N>
 __global__ void tridiag_min_kernel(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *status) {
     __shared__ float df[kMaxTri], e2f[kMaxTri];
     __shared__ float bounds[2];
+    extern __shared__ uint8_t tri_smem[];  // k diagonal entries, then k - 1 squared off-diagonals
     const int lane = threadIdx.x;
     if (k <= 0 || k > kMaxTri) {
         if (lane == 0) *status = 1;
@@ -222,6 +257,12 @@ __global__ void tridiag_min_kernel(int k, const mlf<N> *d, const mlf<N> *e, mlf<
         bounds[0] = lo;
         bounds[1] = hi;
     }
+    mlf<N> *ds = reinterpret_cast<mlf<N> *>(tri_smem);
+    mlf<N> *b2s = ds + k;
+    for (int i = lane; i < k; i += 32) {
+        ds[i] = d[i];
+        if (i + 1 < k) b2s[i] = ml_mul(e[i], e[i]);
+    }
     __syncwarp();
     if (lane != 0) return;
     const int scale_e = E + ilogbf(scale) + 1;
@@ -230,26 +271,26 @@ __global__ void tridiag_min_kernel(int k, const mlf<N> *d, const mlf<N> *e, mlf<
     int ok;
     {
         mlf<2> a, b;
-        newton_level<2, N>(k, d, e, l2, scale_e, 50, 8, &a, &b);
+        newton_level<2, N>(k, ds, b2s, l2, scale_e, 50, 8, &a, &b);
     }
     if constexpr (N <= 4) {
         lam = ml_widen<N, 2>(l2);
-        ok = newton_level<N, N>(k, d, e, lam, scale_e, 32 * N - 4, 8, &pkm1, &dpk);
+        ok = newton_level<N, N>(k, ds, b2s, lam, scale_e, 32 * N - 4, 8, &pkm1, &dpk);
     } else {
         mlf<4> l4 = ml_widen<4, 2>(l2);
         {
             mlf<4> a, b;
-            newton_level<4, N>(k, d, e, l4, scale_e, 110, 6, &a, &b);
+            newton_level<4, N>(k, ds, b2s, l4, scale_e, 110, 6, &a, &b);
         }
         if constexpr (N <= 8) {
             lam = ml_widen<N, 4>(l4);
         } else {
             mlf<8> l8 = ml_widen<8, 4>(l4);
             mlf<8> a, b;
-            newton_level<8, N>(k, d, e, l8, scale_e, 230, 6, &a, &b);
+            newton_level<8, N>(k, ds, b2s, l8, scale_e, 230, 6, &a, &b);
             lam = ml_widen<N, 8>(l8);
         }
-        ok = newton_level<N, N>(k, d, e, lam, scale_e, 32 * N - 4, 8, &pkm1, &dpk);
+        ok = newton_level<N, N>(k, ds, b2s, lam, scale_e, 32 * N - 4, 8, &pkm1, &dpk);
     }
     out[0] = lam;
     const mlf<N> z2 = ml_is_zero(dpk) ? ml_zero<N>() : ml_abs(ml_div(pkm1, dpk));
@@ -338,8 +379,12 @@ __global__ void tridiagonalize_kernel(int n, mlf<N> *A, mlf<N> *dout, mlf<N> *eo
 template <int N>
 void k_matvec(int n, const mlf<N> *A, char op, int tri, const mlf<N> *x, mlf<N> *y, cudaStream_t s) {
     const int g = ceil_div(n, kWarpsPerBlock);
-    if (op == 'T' || op == 't') matvec_t_kernel<N><<<g, 32 * kWarpsPerBlock, 0, s>>>(n, A, tri, x, y);
-    else matvec_n_kernel<N><<<g, 32 * kWarpsPerBlock, 0, s>>>(n, A, tri, x, y);
+    if ((op == 'T' || op == 't') && n >= 128)
+        matvec_t_split_kernel<N><<<ceil_div(n, kWarpsPerBlock / kMvSplit), 32 * kWarpsPerBlock, 0, s>>>(n, A, tri, x, y);
+    else if (op == 'T' || op == 't')
+        matvec_t_kernel<N><<<g, 32 * kWarpsPerBlock, 0, s>>>(n, A, tri, x, y);
+    else
+        matvec_n_kernel<N><<<g, 32 * kWarpsPerBlock, 0, s>>>(n, A, tri, x, y);
     SDPG_CHECK_LAUNCH();
 }
 
@@ -359,7 +404,12 @@ void k_lanczos_next(int n, const mlf<N> *r, const mlf<N> *beta, mlf<N> *q, mlf<N
 template <int N>
 void k_tridiag_min(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *status, cudaStream_t s) {
     if (k > kMaxTri) throw sdpg_error(SDPG_ERR_TOO_LARGE, "tridiagonal larger than 512");
-    tridiag_min_kernel<N><<<1, 32, 0, s>>>(k, d, e, out, status);
+    static std::once_flag once;
+    std::call_once(once, [] {
+        SDPG_CUDA(cudaFuncSetAttribute(tridiag_min_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(2 * kMaxTri * sizeof(mlf<N>))));
+    });
+    tridiag_min_kernel<N><<<1, 32, (size_t)(2 * k) * sizeof(mlf<N>), s>>>(k, d, e, out, status);
     SDPG_CHECK_LAUNCH();
 }
 

@@ -45,6 +45,7 @@ class Solver final : public SolverBase {
         V *C, *X, *Z, *Zinv, *LX, *LZ, *Dx, *Dz, *Rm, *XRDZ, *W1, *W2, *Dres, *Lt, *F;
         // Lanczos vectors and tridiagonal storage, one set per side (0: X, 1: Z)
         V *q[2], *qold[2], *r[2], *w[2], *tmp[2], *td[2], *te[2], *sl[2];
+        V *Mop[2] = {nullptr, nullptr}, *Mtmp[2] = {nullptr, nullptr};  // L X L^T of a Lanczos run (n > 20)
         V *SW1 = nullptr, *SW2 = nullptr;  // Z-side work matrices of the small-block eigenvalue path
         BlockDev<N> cons;
         std::vector<int> f1_owners_h;
@@ -137,7 +138,9 @@ class Solver final : public SolverBase {
         g_ = dalloc(m_);
         p_ = dalloc(m_);
         B_ = dalloc((size_t)m_ * m_);
-        Bdinv_ = (V *)dalloc_raw(ml_potrs_prepare_bytes<N>(m_));
+        BLinv_ = dalloc((size_t)m_ * m_);
+        BLinvT_ = dalloc((size_t)m_ * m_);
+        Dytmp_ = dalloc(m_);
         upload(b_, bh.data(), m_);
         b_h_ = bh;
         info_ = (int *)dalloc_raw(64);
@@ -300,6 +303,11 @@ class Solver final : public SolverBase {
             if (n <= 20) {
                 B.SW1 = dalloc(nn);
                 B.SW2 = dalloc(nn);
+            } else {
+                for (int side = 0; side < 2; ++side) {
+                    B.Mop[side] = dalloc(nn);
+                    B.Mtmp[side] = dalloc(nn);
+                }
             }
             // workspace need
             max_ws = std::max(max_ws, gemm_bytes(n, n, n, 1));
@@ -316,6 +324,7 @@ class Solver final : public SolverBase {
             max_ws = std::max(max_ws, ml_trtri_workspace_bytes<N>(n));
         }
         max_ws = std::max(max_ws, gemm_bytes(m_, m_, 32, 1));
+        max_ws = std::max(max_ws, ml_trtri_workspace_bytes<N>(m_));
         ws_.reserve(max_ws + (64u << 20));
         ws2_.reserve(max_ws + (64u << 20));
         SDPG_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
@@ -586,10 +595,13 @@ class Solver final : public SolverBase {
             SDPG_CUDA(cudaMemcpyAsync(&info, info_, sizeof(int), cudaMemcpyDeviceToHost, st_));
             SDPG_CUDA(cudaStreamSynchronize(st_));
             if (info != 0) return false;
-            ml_potrs_prepare<N>(m_, B_, m_, Bdinv_, st_);
+            // L^{-1} once per factorisation (recursive, GEMM based); each solve is then
+            // two triangular matrix-vector products, read column-wise for coalescing
+            ml_trtri_lower<N>(m_, B_, m_, BLinv_, ws_, st_);
+            k_transpose<N>(m_, BLinv_, BLinvT_, st_);
         }
-        k_copy<N>(m_, g_, Dy_, st_);
-        ml_potrs_solve<N>(m_, B_, m_, Bdinv_, Dy_, st_);
+        k_matvec<N>(m_, BLinvT_, 'T', 2, g_, Dytmp_, st_);  // L^{-1} g
+        k_matvec<N>(m_, BLinv_, 'T', 1, Dytmp_, Dy_, st_);  // L^{-T} L^{-1} g
         return true;
     }
 
@@ -655,9 +667,7 @@ class Solver final : public SolverBase {
         h2d_ += 2 * (long long)sizeof(V);
         SDPG_CUDA(cudaMemcpyAsync(sl + 0, t.hp + 0, 2 * sizeof(V), cudaMemcpyHostToDevice, t.st));
         k_lanczos_next<N>(n, B.r[s], sl + 0, B.q[s], B.qold[s], t.st);  // qold = q; q = r / beta
-        k_matvec<N>(n, t.L, 'T', 1, B.q[s], B.w[s], t.st);              // w = L^T q
-        k_matvec<N>(n, t.Xm, 'T', 0, B.w[s], B.tmp[s], t.st);           // tmp = X w (X symmetric)
-        k_matvec<N>(n, t.Lt, 'T', 2, B.tmp[s], B.w[s], t.st);           // w = L tmp
+        k_matvec<N>(n, B.Mop[s], 'T', 0, B.q[s], B.w[s], t.st);         // w = (L X L^T) q
         {
             const size_t mark = t.ws->used;
             k_dot<N>(n, B.q[s], B.w[s], B.td[s] + t.k, *t.ws, t.st);  // alpha = q . w -> diagVec[k]
@@ -702,7 +712,10 @@ class Solver final : public SolverBase {
             Lz &t = T[i];
             Blk &B = *t.B;
             t.hp = pinned_ + 8 * i;
-            k_transpose<N>(t.n, t.L, t.Lt, t.st);
+            // the Lanczos operator L X L^T, formed once per run (symmetric up to rounding;
+            // its columns are read as rows)
+            mm_on(t.st, *t.ws, t.n, B.Mtmp[t.side], t.Xm, 'N', t.L, 'T');
+            mm_on(t.st, *t.ws, t.n, B.Mop[t.side], t.L, 'N', B.Mtmp[t.side], 'N');
             k_fill<N>(t.n, B.r[t.side], ml_one<N>(), t.st);
             SDPG_CUDA(cudaMemsetAsync(B.q[t.side], 0, t.n * sizeof(V), t.st));
             t.min = R(1.0e+51);
@@ -1156,12 +1169,9 @@ class Solver final : public SolverBase {
         newton(1);
         step_length(1);
         {
-            // the Schur solves' bounded waits (step_length has synchronised the streams)
+            // the tensor-core GEMMs' bounded waits (step_length has synchronised the streams)
             int st = 0;
-            d2h_ += (long long)sizeof(int);
-            SDPG_CUDA(cudaMemcpy(&st, ml_potrs_status<N>(m_, Bdinv_), sizeof(int), cudaMemcpyDeviceToHost));
-            if (st != 0) throw sdpg_error(SDPG_ERR_TIMEOUT, "Schur triangular solve: a bounded wait timed out");
-            if (N == 8 && g_gemm_method == 0) {
+            if (N == 8 && g_gemm_method != 1) {
                 d2h_ += (long long)sizeof(int);
                 SDPG_CUDA(cudaMemcpy(&st, crt_error_word(), sizeof(int), cudaMemcpyDeviceToHost));
                 if (st != 0) throw sdpg_error(SDPG_ERR_TIMEOUT, "tensor-core GEMM: a bounded wait timed out");
@@ -1361,7 +1371,7 @@ class Solver final : public SolverBase {
     std::vector<Blk> blk_;
     int m_ = 0, nDim_ = 0;
     std::vector<V> b_h_;
-    V *Bdinv_ = nullptr;  // inverted 32 x 32 diagonal blocks of the Schur factor
+    V *BLinv_ = nullptr, *BLinvT_ = nullptr, *Dytmp_ = nullptr;  // inverse of the Schur factor and its transpose
     V *b_ = nullptr, *y_ = nullptr, *Dy_ = nullptr, *g_ = nullptr, *p_ = nullptr, *B_ = nullptr, *slot_ = nullptr;
     int *info_ = nullptr, *status_ = nullptr;
     R muInit_, muCur_, thP_, thD_, aP_, aD_, betaV_, rho_, etaP_, etaD_, objP_, objD_, normP_, normD_;

@@ -263,7 +263,13 @@ __global__ void __launch_bounds__(128, 1)
             uint32_t packed[16];
 #pragma unroll
             for (int q = 0; q < 32; q += 2) {
-                int y0 = r[q] % m, y1 = r[q + 1] % m;
+                // r < nacc m <= 4m: reduce with at most three subtractions
+                int y0 = r[q], y1 = r[q + 1];
+#pragma unroll
+                for (int t = 0; t < 3; ++t) {
+                    y0 -= (y0 >= m) ? m : 0;
+                    y1 -= (y1 >= m) ? m : 0;
+                }
                 y0 = mulmod(y0, c, m, inv_m);
                 y1 = mulmod(y1, c, m, inv_m);
                 packed[q / 2] = (uint32_t)y0 | ((uint32_t)y1 << 16);
