@@ -349,6 +349,64 @@ void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t 
     ws.used = mark;
 }
 
+template <int N>
+void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t s, const PotrfAux &aux) {
+    if (!aux.stream || !aux.ws || n <= 2 * NB) {
+        ml_potrf<N>(n, A, lda, info, ws, s);
+        return;
+    }
+    SDPG_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
+    const size_t mark = ws.used;
+    mlf<N> *rinv = (mlf<N> *)ws.carve(NB * sizeof(mlf<N>));
+    mlf<N> *Lsc = (mlf<N> *)ws.carve(NB * NB * sizeof(mlf<N>));
+    const mlf<N> mone = ml_from_int<N>(-1), one = ml_one<N>();
+    int panel = 0;
+    bool rest_pending = false;
+    for (int k0 = 0; k0 < n; k0 += NB, ++panel) {
+        const int kb = min(NB, n - k0);
+        mlf<N> *Akk = A + k0 + (long long)k0 * lda;
+        potf2_kernel<N><<<1, kPotf2Threads, 0, s>>>(Akk, lda, kb, k0, info, rinv, Lsc);
+        SDPG_CHECK_LAUNCH();
+        const int rows = n - k0 - kb;
+        if (rows <= 0) break;
+        mlf<N> *A21 = A + (k0 + kb) + (long long)k0 * lda;
+        panel_trsm_kernel<N><<<ceil_div((long long)rows * 32, 256), 256, 0, s>>>(Lsc, A21, lda, kb, rows, info, rinv);
+        SDPG_CHECK_LAUNCH();
+        const int c1 = k0 + kb;                 // first column of the next panel
+        const int kb2 = min(NB, n - c1);        // its width
+        const int rows2 = rows - kb2;           // rows (and columns) beyond it
+        if (rows2 > 0) {
+            // the rest of the trailing update on the auxiliary stream, once A21 is final
+            SDPG_CUDA(cudaEventRecord(aux.ev_panel, s));
+            SDPG_CUDA(cudaStreamWaitEvent(aux.stream, aux.ev_panel, 0));
+            GemmProblem<N> pb = gemm_nn<N>(rows2, rows2, kb, mone, A21 + kb2, lda, 'N', A21 + kb2, lda, 'T', one,
+                                           A + (c1 + kb2) + (long long)(c1 + kb2) * lda, lda);
+            pb.lower_only = 1;
+            const size_t m3 = aux.ws->used;
+            ml_gemm<N>(pb, *aux.ws, aux.stream);
+            aux.ws->used = m3;
+        }
+        // the next panel's columns on the main stream; they were last touched by the
+        // previous panel's trailing update
+        if (rest_pending) SDPG_CUDA(cudaStreamWaitEvent(s, aux.ev_rest[(panel - 1) & 1], 0));
+        if (rows2 > 0) {
+            SDPG_CUDA(cudaEventRecord(aux.ev_rest[panel & 1], aux.stream));
+            rest_pending = true;
+        } else {
+            rest_pending = false;
+        }
+        GemmProblem<N> pa = gemm_nn<N>(rows, kb2, kb, mone, A21, lda, 'N', A21, lda, 'T', one,
+                                       A + c1 + (long long)c1 * lda, lda);
+        pa.lower_only = 1;
+        const size_t m2 = ws.used;
+        ml_gemm<N>(pa, ws, s);
+        ws.used = m2;
+    }
+    // whatever the auxiliary stream still has in flight is ordered before later work on s
+    if (rest_pending) SDPG_CUDA(cudaStreamWaitEvent(s, aux.ev_rest[(panel - 1) & 1], 0));
+    ws.used = mark;
+}
+
 namespace {
 
 template <int N>
@@ -502,6 +560,7 @@ void ml_potrs(int n, const mlf<N> *L, int ldl, mlf<N> *x, Workspace &ws, cudaStr
 
 #define SDPG_INST_CHOL(N)                                                                       \
     template void ml_potrf<N>(int, mlf<N> *, int, int *, Workspace &, cudaStream_t);            \
+    template void ml_potrf<N>(int, mlf<N> *, int, int *, Workspace &, cudaStream_t, const PotrfAux &); \
     template void ml_trtri_lower<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t); \
     template size_t ml_trtri_workspace_bytes<N>(int);                                                       \
     template void ml_potrs<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t);             \

@@ -142,26 +142,11 @@ __global__ void __launch_bounds__(256)
 }
 
 // V / M as the centred fractional part of sum_l y_l / m_l (320-bit fixed point), then
-// C = alpha V 2^(EA + EB - 2R) + beta C.  Threads run along j (contiguous y loads).
+// C = alpha V 2^(EA + EB - 2R) + beta C.  Each thread takes two neighbouring outputs
+// along j and reads both residues of a plane with one 32-bit load.
 template <int N>
-__global__ void __launch_bounds__(128)
-    crt_reconstruct_kernel(const uint16_t *Y, int Mpad, int Npad, const int *EA, const int *EB, long long sEA,
-                           long long sEB, int b0, int alpha_one, GemmProblem<N> p) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y;
-    const int bl = blockIdx.z;
-    if (i >= p.M || j >= p.Nn || (p.lower_only && i < j)) return;
-    const uint16_t *y = Y + ((long long)bl * kCrtL * Mpad + i) * Npad + j;
-    const long long plane = (long long)Mpad * Npad;
-    unsigned long long acc[kCrtInvWords];
-#pragma unroll
-    for (int w = 0; w < kCrtInvWords; ++w) acc[w] = 0;
-#pragma unroll 10
-    for (int l = 0; l < kCrtL; ++l) {
-        const uint32_t yl = y[l * plane];
-#pragma unroll
-        for (int w = 0; w < kCrtInvWords; ++w) acc[w] += (unsigned long long)yl * c_inv[l][w];
-    }
+__device__ __forceinline__ void crt_finish(const unsigned long long (&acc)[kCrtInvWords], int escale, int alpha_one,
+                                           const GemmProblem<N> &p, mlf<N> *cp) {
     uint32_t W[kCrtInvWords];
     unsigned long long carry = 0;
 #pragma unroll
@@ -187,13 +172,43 @@ __global__ void __launch_bounds__(128)
     Mt.s = 0;
 #pragma unroll
     for (int w = 0; w < N; ++w) Mt.m[w] = c_mtot[w];
-    mlf<N> v = ml_mul(frac, Mt);
-    const int bg = b0 + bl;
-    v = ml_ldexp(v, EA[bl * sEA + i] + EB[bl * sEB + j] - 2 * kCrtR);
+    mlf<N> v = ml_ldexp(ml_mul(frac, Mt), escale);
     if (!alpha_one) v = ml_mul(v, p.alpha);
-    mlf<N> *cp = p.C + bg * p.sc + i + (long long)j * p.ldc;
     if (!ml_is_zero(p.beta)) v = ml_add(v, ml_mul(p.beta, *cp));
     *cp = v;
+}
+
+template <int N>
+__global__ void __launch_bounds__(128)
+    crt_reconstruct_kernel(const uint16_t *Y, int Mpad, int Npad, const int *EA, const int *EB, long long sEA,
+                           long long sEB, int b0, int alpha_one, GemmProblem<N> p) {
+    const int j = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int i = blockIdx.y;
+    const int bl = blockIdx.z;
+    const bool ok0 = j < p.Nn && !(p.lower_only && i < j);
+    const bool ok1 = j + 1 < p.Nn && !(p.lower_only && i < j + 1);
+    if (!ok0 && !ok1) return;
+    const uint32_t *y = reinterpret_cast<const uint32_t *>(Y + ((long long)bl * kCrtL * Mpad + i) * Npad + j);
+    const long long plane = (long long)Mpad * Npad / 2;  // in pairs
+    unsigned long long a0[kCrtInvWords], a1[kCrtInvWords];
+#pragma unroll
+    for (int w = 0; w < kCrtInvWords; ++w) a0[w] = a1[w] = 0;
+#pragma unroll 10
+    for (int l = 0; l < kCrtL; ++l) {
+        const uint32_t yy = __ldg(y + l * plane);
+        const uint32_t y0 = yy & 0xFFFFu, y1 = yy >> 16;
+#pragma unroll
+        for (int w = 0; w < kCrtInvWords; ++w) {
+            const uint32_t c = c_inv[l][w];
+            a0[w] += (unsigned long long)y0 * c;
+            a1[w] += (unsigned long long)y1 * c;
+        }
+    }
+    const int bg = b0 + bl;
+    const int ea = EA[bl * sEA + i] - 2 * kCrtR;
+    if (ok0) crt_finish<N>(a0, ea + EB[bl * sEB + j], alpha_one, p, p.C + bg * p.sc + i + (long long)j * p.ldc);
+    if (ok1)
+        crt_finish<N>(a1, ea + EB[bl * sEB + j + 1], alpha_one, p, p.C + bg * p.sc + i + (long long)(j + 1) * p.ldc);
 }
 
 struct CrtLayout {
@@ -319,7 +334,7 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
             if (p.ev_before) SDPG_CUDA(cudaEventRecord(p.ev_before, s));
             tc_modgemm(t, s);
             if (p.ev_after) SDPG_CUDA(cudaEventRecord(p.ev_after, s));
-            crt_reconstruct_kernel<N><<<dim3(ceil_div(p.Nn, 128), p.M, G), 128, 0, s>>>(
+            crt_reconstruct_kernel<N><<<dim3(ceil_div(p.Nn, 256), p.M, G), 128, 0, s>>>(
                 Y, L.Mpad, L.Npad, EA, EB, ab ? L.Mpad : 0, bb ? L.Npad : 0, b0, alpha_one, p);
             SDPG_CHECK_LAUNCH();
         }

@@ -53,6 +53,23 @@ MLHD int ml_clz32(uint32_t x) {
 #endif
 }
 
+// Low 32 bits of (hi:lo) >> r and high 32 bits of (hi:lo) << r, 0 <= r < 32, without a
+// branch on r (SIMT lanes with different shift counts stay converged).
+MLHD uint32_t ml_fshr(uint32_t lo, uint32_t hi, int r) {
+#if defined(__CUDA_ARCH__)
+    return __funnelshift_r(lo, hi, (unsigned)r);
+#else
+    return (uint32_t)((((uint64_t)hi << 32) | lo) >> r);
+#endif
+}
+MLHD uint32_t ml_fshl(uint32_t lo, uint32_t hi, int r) {
+#if defined(__CUDA_ARCH__)
+    return __funnelshift_l(lo, hi, (unsigned)r);
+#else
+    return (uint32_t)(((((uint64_t)hi << 32) | lo) << r) >> 32);
+#endif
+}
+
 template <int N>
 MLHD mlf<N> ml_zero() {
     mlf<N> r;
@@ -120,23 +137,15 @@ MLHD void ml_limb_shl(uint32_t (&a)[L], int q) {
 // a >>= r bits, 0 <= r < 32
 template <int L>
 MLHD void ml_bit_shr(uint32_t (&a)[L], int r) {
-    if (r == 0) return;
     ML_UNROLL
-    for (int k = 0; k < L; ++k) {
-        const uint32_t hi = (k + 1 < L) ? a[k + 1] : 0u;
-        a[k] = (a[k] >> r) | (hi << (32 - r));
-    }
+    for (int k = 0; k < L; ++k) a[k] = ml_fshr(a[k], (k + 1 < L) ? a[k + 1] : 0u, r);
 }
 
 // a <<= r bits, 0 <= r < 32
 template <int L>
 MLHD void ml_bit_shl(uint32_t (&a)[L], int r) {
-    if (r == 0) return;
     ML_UNROLL
-    for (int k = L - 1; k >= 0; --k) {
-        const uint32_t lo = (k >= 1) ? a[k - 1] : 0u;
-        a[k] = (a[k] << r) | (lo >> (32 - r));
-    }
+    for (int k = L - 1; k >= 0; --k) a[k] = ml_fshl((k >= 1) ? a[k - 1] : 0u, a[k], r);
 }
 
 // Number of leading zero bits of the L-limb number a (32*L if zero).
@@ -146,14 +155,8 @@ MLHD int ml_clz_limbs(const uint32_t (&a)[L]) {
     bool found = false;
     ML_UNROLL
     for (int k = L - 1; k >= 0; --k) {
-        if (!found) {
-            if (a[k] != 0) {
-                lz += ml_clz32(a[k]);
-                found = true;
-            } else {
-                lz += 32;
-            }
-        }
+        lz += found ? 0 : ml_clz32(a[k]);
+        found = found || a[k] != 0;
     }
     return lz;
 }
@@ -163,14 +166,14 @@ MLHD int ml_clz_limbs(const uint32_t (&a)[L]) {
 template <int N, int L>
 MLHD mlf<N> ml_pack(uint32_t (&a)[L], int e_top, uint32_t sign) {
     const int lz = ml_clz_limbs<L>(a);
-    if (lz >= 32 * L) return ml_zero<N>();
-    ml_limb_shl<L>(a, lz >> 5);
+    const bool zero = lz >= 32 * L;
+    ml_limb_shl<L>(a, zero ? 0 : (lz >> 5));
     ml_bit_shl<L>(a, lz & 31);
     mlf<N> r;
-    r.e = e_top - lz;
-    r.s = sign;
+    r.e = zero ? 0 : e_top - lz;
+    r.s = zero ? 0u : sign;
     ML_UNROLL
-    for (int k = 0; k < N; ++k) r.m[k] = a[L - N + k];
+    for (int k = 0; k < N; ++k) r.m[k] = zero ? 0u : a[L - N + k];
     return r;
 }
 
@@ -189,9 +192,9 @@ MLHD int ml_cmp_mant(const uint32_t (&a)[N], const uint32_t (&b)[N]) {
 template <int N>
 MLHD int ml_cmp_abs(const mlf<N> &a, const mlf<N> &b) {
     const bool za = ml_is_zero(a), zb = ml_is_zero(b);
-    if (za || zb) return za ? (zb ? 0 : -1) : 1;
-    if (a.e != b.e) return a.e > b.e ? 1 : -1;
-    return ml_cmp_mant<N>(a.m, b.m);
+    const int cm = ml_cmp_mant<N>(a.m, b.m);
+    const int c = (a.e > b.e) ? 1 : ((a.e < b.e) ? -1 : cm);
+    return za ? (zb ? 0 : -1) : (zb ? 1 : c);
 }
 
 template <int N>
@@ -208,16 +211,26 @@ MLHD int ml_cmp(const mlf<N> &a, const mlf<N> &b) {
 
 // --- addition -------------------------------------------------------------------
 
+// Straight-line code (selects, no data-dependent branches), so SIMT lanes adding
+// operands of different signs and exponents stay converged: the smaller operand is
+// aligned, added in two's complement (negated when the signs differ), a carry out of
+// a same-sign sum renormalises by one bit, and cancellation is normalised by ml_pack.
 template <int N>
 MLHD mlf<N> ml_add(const mlf<N> &a, const mlf<N> &b) {
-    if (ml_is_zero(b)) return a;
-    if (ml_is_zero(a)) return b;
-    const bool swap = ml_cmp_abs(b, a) > 0;
-    const mlf<N> &x = swap ? b : a;  // |x| >= |y|
-    const mlf<N> &y = swap ? a : b;
-    const int d = x.e - y.e;
     constexpr int L = N + 2;
-    if (d >= 32 * L) return x;
+    const bool swap = ml_cmp_abs(b, a) > 0;
+    mlf<N> x, y;  // |x| >= |y|
+    x.e = swap ? b.e : a.e;
+    x.s = swap ? b.s : a.s;
+    y.e = swap ? a.e : b.e;
+    y.s = swap ? a.s : b.s;
+    ML_UNROLL
+    for (int k = 0; k < N; ++k) {
+        x.m[k] = swap ? b.m[k] : a.m[k];
+        y.m[k] = swap ? a.m[k] : b.m[k];
+    }
+    int d = x.e - y.e;
+    d = (ml_is_zero(y) || d > 32 * L) ? 32 * L : d;
     uint32_t xx[L], yy[L];
     xx[0] = 0;
     xx[1] = 0;
@@ -230,35 +243,21 @@ MLHD mlf<N> ml_add(const mlf<N> &a, const mlf<N> &b) {
     }
     ml_limb_shr<L>(yy, d >> 5);
     ml_bit_shr<L>(yy, d & 31);
-    if (x.s == y.s) {
-        uint64_t c = 0;
-        ML_UNROLL
-        for (int k = 0; k < L; ++k) {
-            c += (uint64_t)xx[k] + yy[k];
-            xx[k] = (uint32_t)c;
-            c >>= 32;
-        }
-        int e = x.e;
-        if (c) {
-            ml_bit_shr<L>(xx, 1);
-            xx[L - 1] |= 0x80000000u;
-            e += 1;
-        }
-        mlf<N> r;
-        r.e = e;
-        r.s = x.s;
-        ML_UNROLL
-        for (int k = 0; k < N; ++k) r.m[k] = xx[k + 2];
-        return r;
-    }
-    int64_t br = 0;
+    const bool sub = x.s != y.s;
+    uint64_t c = sub ? 1u : 0u;
     ML_UNROLL
     for (int k = 0; k < L; ++k) {
-        br += (int64_t)xx[k] - (int64_t)yy[k];
-        xx[k] = (uint32_t)br;
-        br >>= 32;  // arithmetic: 0 or -1
+        c += (uint64_t)xx[k] + (sub ? ~yy[k] : yy[k]);
+        xx[k] = (uint32_t)c;
+        c >>= 32;
     }
-    return ml_pack<N, L>(xx, x.e, x.s);
+    const bool ovf = !sub && c != 0;  // same-sign sum one bit wider than x
+    ML_UNROLL
+    for (int k = 0; k < L; ++k) {
+        const uint32_t hi = (k + 1 < L) ? xx[k + 1] : 1u;
+        xx[k] = ovf ? ml_fshr(xx[k], hi, 1) : xx[k];
+    }
+    return ml_pack<N, L>(xx, x.e + (ovf ? 1 : 0), x.s);
 }
 
 template <int N>
@@ -306,7 +305,7 @@ MLHD uint32_t ml_bits32(const uint32_t (&W)[L], int off) {
 
 template <int N>
 MLHD mlf<N> ml_mul(const mlf<N> &a, const mlf<N> &b) {
-    if (ml_is_zero(a) || ml_is_zero(b)) return ml_zero<N>();
+    const bool zero = ml_is_zero(a) || ml_is_zero(b);
     using G = MulDigits<N>;
     uint32_t da[G::D], db[G::D];
     ml_digits28<N>(a.m, da);
@@ -340,15 +339,12 @@ MLHD mlf<N> ml_mul(const mlf<N> &a, const mlf<N> &b) {
     const bool top = (W[G::TOPREL >> 5] >> (G::TOPREL & 31)) & 1u;
     constexpr int off = G::TOPREL + 1 - 32 * N;  // lowest mantissa bit when the top bit is set
     mlf<N> o;
-    o.s = a.s ^ b.s;
-    if (top) {
-        o.e = a.e + b.e;
-        ML_UNROLL
-        for (int k = 0; k < N; ++k) o.m[k] = ml_bits32<G::LW>(W, off + 32 * k);
-    } else {
-        o.e = a.e + b.e - 1;
-        ML_UNROLL
-        for (int k = 0; k < N; ++k) o.m[k] = ml_bits32<G::LW>(W, off - 1 + 32 * k);
+    o.s = zero ? 0u : (a.s ^ b.s);
+    o.e = zero ? 0 : a.e + b.e - (top ? 0 : 1);
+    ML_UNROLL
+    for (int k = 0; k < N; ++k) {
+        const uint32_t hi = ml_bits32<G::LW>(W, off + 32 * k), lo = ml_bits32<G::LW>(W, off - 1 + 32 * k);
+        o.m[k] = zero ? 0u : (top ? hi : lo);
     }
     return o;
 }
