@@ -88,53 +88,81 @@ __global__ void __launch_bounds__(kPotf2Threads, 1)
     if (q < kb) rinv[q] = ri[q];
 }
 
+// strict lower triangle of an NB x NB block, packed column by column
+__host__ __device__ constexpr int packed_lower(int i, int j) { return j * NB - j * (j + 1) / 2 + (i - j - 1); }
+constexpr int kPackedLower = NB * (NB - 1) / 2;
+
 // Rows below the diagonal block: solve x L11^T = a for each row, one warp per row.
 // With a~ = a / diag(L11) and Lsc = diag(L11)^-1 L11 (unit lower), x_j = a~_j -
-// sum_{t<j} Lsc[j][t] x_t: each step is a broadcast and one multiply-subtract.
+// sum_{t<j} Lsc[j][t] x_t: each step is a broadcast and one multiply-subtract, with
+// Lsc read from shared memory (staged once per block).
 template <int N>
 __global__ void panel_trsm_kernel(const mlf<N> *Lsc, mlf<N> *R, int lda, int kb, int nrows, const int *info,
                                   const mlf<N> *rinv) {
+    __shared__ mlf<N> ls[kPackedLower];
     if (*info != 0) return;
+    for (int q = threadIdx.x; q < NB * NB; q += blockDim.x) {
+        const int i = q % NB, j = q / NB;
+        if (i > j && i < kb) ls[packed_lower(i, j)] = Lsc[i + NB * j];
+    }
+    __syncthreads();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= nrows) return;
     mlf<N> *row = R + warp;  // element t at row[t * lda]
     mlf<N> a = lane < kb ? ml_mul(row[(long long)lane * lda], rinv[lane]) : ml_zero<N>();
     for (int j = 0; j + 1 < kb; ++j) {
         const mlf<N> xj = ml_shfl(a, j);
-        if (lane > j && lane < kb) a = ml_sub(a, ml_mul(xj, Lsc[lane + NB * j]));
+        if (lane > j && lane < kb) a = ml_sub(a, ml_mul(xj, ls[packed_lower(lane, j)]));
     }
     if (lane < kb) row[(long long)lane * lda] = a;
 }
 
-// Invert every kb x kb diagonal block of the lower-triangular L into Linv.
+// Invert every NB x NB diagonal block of the lower-triangular L (n a multiple of NB)
+// into Linv, one block per CTA and one thread per lower-triangle entry of the inverse,
+// held in registers.  Column-oriented substitution X = T^-1: after step j - 1 row j of
+// X is final; its owners scale it by 1/T[j][j] and publish it, then every entry below
+// subtracts T[i][j] X[j][c] (T from shared memory): one barrier per step.
 template <int N>
-__global__ void trtri_diag_kernel(const mlf<N> *L, int ldl, mlf<N> *Linv, int ldi, int n) {
-    const int b = blockIdx.x;
-    const int o = b * NB;
-    const int kb = min(NB, n - o);
+__global__ void __launch_bounds__(kPotf2Threads, 1) trtri_diag_kernel(const mlf<N> *L, int ldl, mlf<N> *Linv, int ldi, int n) {
+    __shared__ mlf<N> ts[kPackedLower];
+    __shared__ mlf<N> rv[NB];
+    __shared__ mlf<N> xrow[2][NB];
+    const int o = blockIdx.x * NB;
     const mlf<N> *T = L + o + (long long)o * ldl;
     mlf<N> *X = Linv + o + (long long)o * ldi;
-    __shared__ mlf<N> rv[NB];
-    if (threadIdx.x < kb) rv[threadIdx.x] = ml_recip(T[threadIdx.x + (long long)threadIdx.x * ldl]);
-    // X = I (lower part)
-    for (int q = threadIdx.x; q < kb * kb; q += blockDim.x) {
-        const int i = q % kb, c = q / kb;
-        if (i >= c) X[i + (long long)c * ldi] = (i == c) ? ml_one<N>() : ml_zero<N>();
+    const int q = threadIdx.x;
+    for (int p = q; p < NB * NB; p += blockDim.x) {
+        const int i = p % NB, j = p / NB;
+        if (i > j) ts[packed_lower(i, j)] = T[i + (long long)j * ldl];
+    }
+    if (q < NB) rv[q] = ml_recip(T[q + (long long)q * ldl]);
+    // entry (i, c), c <= i, numbered column by column as in potf2_kernel
+    int c = 0;
+    while (c + 1 < NB && NB * (c + 1) - (c + 1) * c / 2 <= q) ++c;
+    const int i = c + (q - (NB * c - c * (c - 1) / 2));
+    const bool mine = q < NB * (NB + 1) / 2;
+    mlf<N> x = (mine && i == c) ? ml_one<N>() : ml_zero<N>();
+    __syncthreads();
+    // row 0 is final at the start: X[0][0] = 1 / T[0][0]
+    if (mine && i == 0) {
+        x = ml_mul(x, rv[0]);
+        xrow[0][c] = x;
     }
     __syncthreads();
-    for (int j = 0; j < kb; ++j) {
-        // row j of X scaled by 1/T[j,j] (columns c <= j)
-        for (int c = threadIdx.x; c <= j; c += blockDim.x) X[j + (long long)c * ldi] = ml_mul(X[j + (long long)c * ldi], rv[j]);
-        __syncthreads();
-        // X[i,c] -= T[i,j] X[j,c] for i > j, c <= j
-        const int rows = kb - j - 1, cols = j + 1;
-        for (int q = threadIdx.x; q < rows * cols; q += blockDim.x) {
-            const int i = j + 1 + q % rows, c = q / rows;
-            mlf<N> *x = X + i + (long long)c * ldi;
-            *x = ml_sub(*x, ml_mul(T[i + (long long)j * ldl], X[j + (long long)c * ldi]));
+    for (int j = 0; j + 1 < NB; ++j) {
+        if (mine && i > j && c <= j) {
+            x = ml_sub(x, ml_mul(ts[packed_lower(i, j)], xrow[j & 1][c]));
+            if (i == j + 1) {  // row j + 1 is now final
+                x = ml_mul(x, rv[j + 1]);
+                xrow[(j + 1) & 1][c] = x;
+            }
+        } else if (mine && i == j + 1 && c == j + 1) {  // the diagonal entry of row j + 1
+            x = ml_mul(x, rv[j + 1]);
+            xrow[(j + 1) & 1][c] = x;
         }
         __syncthreads();
     }
+    if (mine) X[i + (long long)c * ldi] = x;
 }
 
 // Inverses of the NB x NB diagonal blocks of the lower-triangular L, packed:
@@ -468,7 +496,7 @@ void ml_trtri_lower(int n, const mlf<N> *L, int ldl, mlf<N> *Linv, Workspace &ws
     pad_lower_kernel<N><<<ceil_div(pp, 256), 256, 0, s>>>(n, P, L, ldl, Lp);
     SDPG_CHECK_LAUNCH();
     SDPG_CUDA(cudaMemsetAsync(Xp, 0, pp * sizeof(mlf<N>), s));
-    trtri_diag_kernel<N><<<P / NB, 256, 0, s>>>(Lp, P, Xp, P, P);
+    trtri_diag_kernel<N><<<P / NB, kPotf2Threads, 0, s>>>(Lp, P, Xp, P, P);
     SDPG_CHECK_LAUNCH();
     const mlf<N> one = ml_one<N>(), zero = ml_zero<N>(), mone = ml_from_int<N>(-1);
     for (int b = 2 * NB; b <= P; b *= 2) {

@@ -263,7 +263,7 @@ bool crt_gemm_applies(const GemmProblem<N> &p) {
         return false;
     } else {
         if (g_gemm_method == 1 || p.K <= 0 || p.K > kTcMaxK || p.M <= 0 || p.Nn <= 0) return false;
-        return g_gemm_method == 2 || (double)p.M * p.Nn * p.K * p.batch >= (double)(1 << 21);
+        return g_gemm_method == 2 || (double)p.M * p.Nn * p.K * p.batch >= (double)(1 << 15);
     }
 }
 
