@@ -229,8 +229,8 @@ int sdpg_rpotrf(int limbs, int n, void *A, int lda, int *info) {
                 ws.reset();
                 GemmProblem<N> p{};
                 p.M = n;
-                p.Nn = n;
-                p.K = 32;
+                p.Nn = 32;
+                p.K = n;
                 p.batch = 1;
                 ws.reserve(gemm_workspace_bytes<N>(p) + (1 << 20));
                 ml_potrf<N>(n, (mlf<N> *)dA, lda, (int *)dinfo.p, ws, nullptr);

@@ -7,8 +7,12 @@
 // one CTA (pivot square roots and reciprocals in full multi-limb precision), the
 // panel below is solved one row per warp, and the trailing matrix is updated by
 // the block-floating-point GEMM (lower triangle only).
+#include <cooperative_groups.h>
+
 #include "kernels.cuh"
 #include "mlwarp.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace sdpg {
 
@@ -91,6 +95,80 @@ __global__ void __launch_bounds__(kPotf2Threads, 1)
 // strict lower triangle of an NB x NB block, packed column by column
 __host__ __device__ constexpr int packed_lower(int i, int j) { return j * NB - j * (j + 1) / 2 + (i - j - 1); }
 constexpr int kPackedLower = NB * (NB - 1) / 2;
+
+// The same elimination spread over a cluster of kPotf2Cluster CTAs (one per SM): CTA r
+// holds entries r*Q .. r*Q+Q-1 of the column-by-column numbering.  The pivot column,
+// the scale factors c_j and the pivots are replicated in every CTA's shared memory;
+// their owners write all copies through distributed shared memory, and one cluster
+// barrier per step publishes them.  Per SM a step now issues a quarter of the
+// multi-limb operations, which is what bounds the single-CTA version.
+constexpr int kPotf2Cluster = 4;
+constexpr int kPotf2PerCta = (NB * (NB + 1) / 2 + kPotf2Cluster - 1) / kPotf2Cluster;  // 132
+constexpr int kPotf2ClusterThreads = ((kPotf2PerCta + 31) / 32) * 32;                  // 160
+
+template <int N>
+__global__ void __cluster_dims__(kPotf2Cluster, 1, 1) __launch_bounds__(kPotf2ClusterThreads)
+    potf2_cluster_kernel(mlf<N> *A, int lda, int kb, int col0, int *info, mlf<N> *rinv, mlf<N> *Lsc) {
+    __shared__ mlf<N> col[2][NB];
+    __shared__ mlf<N> cs[NB];
+    __shared__ mlf<N> pv[NB];
+    __shared__ mlf<N> rs[NB];
+    __shared__ mlf<N> ri[NB];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    if (*info != 0) return;  // the same value for every CTA of the cluster
+    const int q = rank * kPotf2PerCta + (int)threadIdx.x;
+    int t = 0;
+    while (t + 1 < NB && NB * (t + 1) - (t + 1) * t / 2 <= q) ++t;
+    const int i = t + (q - (NB * t - t * (t - 1) / 2));  // entry (i, t), t <= i
+    const bool mine = (int)threadIdx.x < kPotf2PerCta && q < NB * (NB + 1) / 2 && i < kb;
+    mlf<N> a = mine ? A[i + (long long)t * lda] : ml_zero<N>();
+    // publish v at the same shared-memory slot of every CTA in the cluster
+    auto publish = [&](mlf<N> *slot, const mlf<N> &v) {
+#pragma unroll
+        for (int r = 0; r < kPotf2Cluster; ++r) *cluster.map_shared_rank(slot, r) = v;
+    };
+    if (mine && t == 0) publish(&col[0][i], a);
+    cluster.sync();
+    mlf<N> c = ml_one<N>();  // carried by entry (0, 0) (rank 0, thread 0), idle after step 0
+    int bad = 0;
+    for (int j = 0; j < kb; ++j) {
+        const mlf<N> p = col[j & 1][j];
+        if (ml_sign(p) <= 0) {
+            bad = col0 + j + 1;
+            break;
+        }
+        if (q == 0) {
+            publish(&cs[j], c);
+            c = ml_mul(c, ml_ldexp(p, -p.e));
+        }
+        if (mine && t > j) {
+            const mlf<N> u = ml_sub(ml_mul(p, a), ml_mul(col[j & 1][i], col[j & 1][t]));
+            a = ml_ldexp(u, -p.e);
+            if (t == j + 1) publish(&col[(j + 1) & 1][i], a);
+        }
+        cluster.sync();
+    }
+    if (!bad) {
+        if (mine && i == t) publish(&pv[t], a);
+        cluster.sync();
+        if ((int)threadIdx.x < kb) {  // every CTA forms the normalisers it needs
+            const mlf<N> r = ml_rsqrt(ml_mul(cs[threadIdx.x], pv[threadIdx.x]));
+            rs[threadIdx.x] = r;
+            ri[threadIdx.x] = ml_mul(cs[threadIdx.x], r);
+        }
+        __syncthreads();
+        if (mine) {
+            a = ml_mul(a, rs[t]);
+            A[i + (long long)t * lda] = a;
+            if (i > t) Lsc[i + NB * t] = ml_mul(a, ri[i]);
+        }
+        if (rank == 0 && (int)threadIdx.x < kb) rinv[threadIdx.x] = ri[threadIdx.x];
+    } else if (q == 0) {
+        *info = bad;
+    }
+    cluster.sync();  // no CTA leaves while another may still write its shared memory
+}
 
 // Rows below the diagonal block: solve x L11^T = a for each row, one warp per row.
 // With a~ = a / diag(L11) and Lsc = diag(L11)^-1 L11 (unit lower), x_j = a~_j -
@@ -350,6 +428,11 @@ GemmProblem<N> gemm_nn(int M, int Nn, int K, const mlf<N> &alpha, const mlf<N> *
 
 }  // namespace
 
+// Left-looking blocked Cholesky: before its diagonal block is factored, each 32-column
+// panel receives the contribution of every earlier panel in one GEMM,
+//     A[k0:, k0:k0+kb] -= L[k0:, :k0] L[k0:k0+kb, :k0]^T,
+// so the factorisation costs one exact (residue-path) product per panel whose output is
+// only the panel, not the whole trailing matrix.
 template <int N>
 void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t s) {
     SDPG_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
@@ -359,79 +442,22 @@ void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t 
     const mlf<N> mone = ml_from_int<N>(-1), one = ml_one<N>();
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int kb = min(NB, n - k0);
-        mlf<N> *Akk = A + k0 + (long long)k0 * lda;
-        potf2_kernel<N><<<1, kPotf2Threads, 0, s>>>(Akk, lda, kb, k0, info, rinv, Lsc);
-        SDPG_CHECK_LAUNCH();
         const int rows = n - k0 - kb;
-        if (rows <= 0) break;
-        mlf<N> *A21 = A + (k0 + kb) + (long long)k0 * lda;
-        panel_trsm_kernel<N><<<ceil_div((long long)rows * 32, 256), 256, 0, s>>>(Lsc, A21, lda, kb, rows, info, rinv);
-        SDPG_CHECK_LAUNCH();
-        GemmProblem<N> p = gemm_nn<N>(rows, rows, kb, mone, A21, lda, 'N', A21, lda, 'T', one,
-                                      A + (k0 + kb) + (long long)(k0 + kb) * lda, lda);
-        p.lower_only = 1;
-        const size_t m2 = ws.used;
-        ml_gemm<N>(p, ws, s);
-        ws.used = m2;
-    }
-    ws.used = mark;
-}
-
-template <int N>
-void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t s, const PotrfAux &aux) {
-    if (!aux.stream || !aux.ws || n <= 2 * NB) {
-        ml_potrf<N>(n, A, lda, info, ws, s);
-        return;
-    }
-    SDPG_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
-    const size_t mark = ws.used;
-    mlf<N> *rinv = (mlf<N> *)ws.carve(NB * sizeof(mlf<N>));
-    mlf<N> *Lsc = (mlf<N> *)ws.carve(NB * NB * sizeof(mlf<N>));
-    const mlf<N> mone = ml_from_int<N>(-1), one = ml_one<N>();
-    int panel = 0;
-    bool rest_pending = false;
-    for (int k0 = 0; k0 < n; k0 += NB, ++panel) {
-        const int kb = min(NB, n - k0);
         mlf<N> *Akk = A + k0 + (long long)k0 * lda;
-        potf2_kernel<N><<<1, kPotf2Threads, 0, s>>>(Akk, lda, kb, k0, info, rinv, Lsc);
+        if (k0 > 0) {
+            GemmProblem<N> p = gemm_nn<N>(n - k0, kb, k0, mone, A + k0, lda, 'N', A + k0, lda, 'T', one, Akk, lda);
+            p.lower_only = 1;
+            const size_t m2 = ws.used;
+            ml_gemm<N>(p, ws, s);
+            ws.used = m2;
+        }
+        potf2_cluster_kernel<N><<<kPotf2Cluster, kPotf2ClusterThreads, 0, s>>>(Akk, lda, kb, k0, info, rinv, Lsc);
         SDPG_CHECK_LAUNCH();
-        const int rows = n - k0 - kb;
         if (rows <= 0) break;
-        mlf<N> *A21 = A + (k0 + kb) + (long long)k0 * lda;
-        panel_trsm_kernel<N><<<ceil_div((long long)rows * 32, 256), 256, 0, s>>>(Lsc, A21, lda, kb, rows, info, rinv);
+        panel_trsm_kernel<N><<<ceil_div((long long)rows * 32, 256), 256, 0, s>>>(Lsc, Akk + kb, lda, kb, rows, info,
+                                                                               rinv);
         SDPG_CHECK_LAUNCH();
-        const int c1 = k0 + kb;                 // first column of the next panel
-        const int kb2 = min(NB, n - c1);        // its width
-        const int rows2 = rows - kb2;           // rows (and columns) beyond it
-        if (rows2 > 0) {
-            // the rest of the trailing update on the auxiliary stream, once A21 is final
-            SDPG_CUDA(cudaEventRecord(aux.ev_panel, s));
-            SDPG_CUDA(cudaStreamWaitEvent(aux.stream, aux.ev_panel, 0));
-            GemmProblem<N> pb = gemm_nn<N>(rows2, rows2, kb, mone, A21 + kb2, lda, 'N', A21 + kb2, lda, 'T', one,
-                                           A + (c1 + kb2) + (long long)(c1 + kb2) * lda, lda);
-            pb.lower_only = 1;
-            const size_t m3 = aux.ws->used;
-            ml_gemm<N>(pb, *aux.ws, aux.stream);
-            aux.ws->used = m3;
-        }
-        // the next panel's columns on the main stream; they were last touched by the
-        // previous panel's trailing update
-        if (rest_pending) SDPG_CUDA(cudaStreamWaitEvent(s, aux.ev_rest[(panel - 1) & 1], 0));
-        if (rows2 > 0) {
-            SDPG_CUDA(cudaEventRecord(aux.ev_rest[panel & 1], aux.stream));
-            rest_pending = true;
-        } else {
-            rest_pending = false;
-        }
-        GemmProblem<N> pa = gemm_nn<N>(rows, kb2, kb, mone, A21, lda, 'N', A21, lda, 'T', one,
-                                       A + c1 + (long long)c1 * lda, lda);
-        pa.lower_only = 1;
-        const size_t m2 = ws.used;
-        ml_gemm<N>(pa, ws, s);
-        ws.used = m2;
     }
-    // whatever the auxiliary stream still has in flight is ordered before later work on s
-    if (rest_pending) SDPG_CUDA(cudaStreamWaitEvent(s, aux.ev_rest[(panel - 1) & 1], 0));
     ws.used = mark;
 }
 
@@ -588,7 +614,6 @@ void ml_potrs(int n, const mlf<N> *L, int ldl, mlf<N> *x, Workspace &ws, cudaStr
 
 #define SDPG_INST_CHOL(N)                                                                       \
     template void ml_potrf<N>(int, mlf<N> *, int, int *, Workspace &, cudaStream_t);            \
-    template void ml_potrf<N>(int, mlf<N> *, int, int *, Workspace &, cudaStream_t, const PotrfAux &); \
     template void ml_trtri_lower<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t); \
     template size_t ml_trtri_workspace_bytes<N>(int);                                                       \
     template void ml_potrs<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t);             \

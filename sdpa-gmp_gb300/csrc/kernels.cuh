@@ -95,17 +95,6 @@ void k_schur_f1_dense_scatter(const BlockDev<N> &B, const int *owners, int cnt, 
 // triangle is left untouched.
 template <int N>
 void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t s);
-// Look-ahead variant: after each panel, the next panel's columns are updated on `s`
-// and the rest of the trailing matrix on aux.stream (scratch aux.ws), so the next
-// diagonal block is factored while the bulk of the update runs.  The three events
-// order the two streams; on return all work is ordered before later work on `s`.
-struct PotrfAux {
-    cudaStream_t stream = nullptr;
-    Workspace *ws = nullptr;
-    cudaEvent_t ev_panel = nullptr, ev_rest[2] = {nullptr, nullptr};
-};
-template <int N>
-void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t s, const PotrfAux &aux);
 // Linv = inverse of the lower-triangular L (Rtrsm on the identity, sdpa_linear.cpp:439-455);
 // Linv's strict upper triangle is set to zero.
 template <int N>

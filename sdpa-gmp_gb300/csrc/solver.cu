@@ -62,15 +62,7 @@ class Solver final : public SolverBase {
     ~Solver() override {
         if (st2_) cudaStreamSynchronize(st2_);
         if (st2_) cudaStreamDestroy(st2_);
-        for (auto &a : aux_) {
-            if (a.stream) {
-                cudaStreamSynchronize(a.stream);
-                cudaStreamDestroy(a.stream);
-            }
-            if (a.ev_panel) cudaEventDestroy(a.ev_panel);
-            for (auto &e : a.ev_rest)
-                if (e) cudaEventDestroy(e);
-        }
+
         if (ev_fork_) cudaEventDestroy(ev_fork_);
         if (ev_join_) cudaEventDestroy(ev_join_);
         if (pinned_) cudaFreeHost(pinned_);
@@ -333,23 +325,11 @@ class Solver final : public SolverBase {
             max_ws = std::max(max_ws, ml_trtri_workspace_bytes<N>(n));
         }
         max_ws = std::max(max_ws, gemm_bytes(m_, m_, 32, 1));
+        max_ws = std::max(max_ws, gemm_bytes(m_, 32, m_, 1));  // left-looking Cholesky panel update
         max_ws = std::max(max_ws, ml_trtri_workspace_bytes<N>(m_));
         ws_.reserve(max_ws + (64u << 20));
         ws2_.reserve(max_ws + (64u << 20));
         SDPG_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
-        // look-ahead Cholesky: one auxiliary stream (and scratch) per main stream
-        {
-            size_t aux_ws = gemm_bytes(m_, m_, 32, 1);
-            for (auto &B : blk_) aux_ws = std::max(aux_ws, gemm_bytes(B.n, B.n, 32, 1));
-            for (int a = 0; a < 2; ++a) {
-                aux_ws_[a].reserve(aux_ws + (16u << 20));
-                SDPG_CUDA(cudaStreamCreateWithFlags(&aux_[a].stream, cudaStreamNonBlocking));
-                SDPG_CUDA(cudaEventCreateWithFlags(&aux_[a].ev_panel, cudaEventDisableTiming));
-                SDPG_CUDA(cudaEventCreateWithFlags(&aux_[a].ev_rest[0], cudaEventDisableTiming));
-                SDPG_CUDA(cudaEventCreateWithFlags(&aux_[a].ev_rest[1], cudaEventDisableTiming));
-                aux_[a].ws = &aux_ws_[a];
-            }
-        }
         SDPG_CUDA(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
         SDPG_CUDA(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
         SDPG_CUDA(cudaMallocHost(&pinned_, kPinned * sizeof(V)));
@@ -611,7 +591,7 @@ class Solver final : public SolverBase {
     // Newton::compute_DyVec, sdpa_newton.cpp:1308-1344 (Lal::choleskyFactorWithAdjust + solveSystems)
     bool compute_DyVec(bool corrector) {
         if (!corrector) {
-            ml_potrf<N>(m_, B_, m_, info_, ws_, st_, aux_[0]);
+            ml_potrf<N>(m_, B_, m_, info_, ws_, st_);
             int info = 0;
             d2h_ += (long long)sizeof(int);
             SDPG_CUDA(cudaMemcpyAsync(&info, info_, sizeof(int), cudaMemcpyDeviceToHost, st_));
@@ -956,11 +936,10 @@ class Solver final : public SolverBase {
     // Jal::getInvChol / getInvCholAndInv (sdpa_jordan.cpp:123-171) for one block, enqueued
     // on `st`: factor a copy of A (Lal::getCholesky), invert the factor, optionally form
     // Inv = Linv^T Linv (Rtrmm).  A failed factorisation leaves its column in *info.
-    void inv_chol_issue(Blk &B, V *A, V *Fbuf, V *Linv, V *Inv, int *info, cudaStream_t st, Workspace &ws,
-                        const PotrfAux &aux) {
+    void inv_chol_issue(Blk &B, V *A, V *Fbuf, V *Linv, V *Inv, int *info, cudaStream_t st, Workspace &ws) {
         const int n = B.n;
         k_copy<N>((long long)n * n, A, Fbuf, st);
-        ml_potrf<N>(n, Fbuf, n, info, ws, st, aux);
+        ml_potrf<N>(n, Fbuf, n, info, ws, st);
         k_zero_strict_upper<N>(n, Fbuf, st);
         ml_trtri_lower<N>(n, Fbuf, n, Linv, ws, st);
         if (Inv) mm_on(st, ws, n, Inv, Linv, 'T', Linv, 'N');
@@ -973,10 +952,9 @@ class Solver final : public SolverBase {
         SDPG_CUDA(cudaEventRecord(ev_fork_, st_));
         SDPG_CUDA(cudaStreamWaitEvent(st2_, ev_fork_, 0));
         for (size_t l = 0; l < nb; ++l)
-            inv_chol_issue(blk_[l], blk_[l].X, blk_[l].F, blk_[l].LX, nullptr, info_all_ + l, st_, ws_, aux_[0]);
+            inv_chol_issue(blk_[l], blk_[l].X, blk_[l].F, blk_[l].LX, nullptr, info_all_ + l, st_, ws_);
         for (size_t l = 0; l < nb; ++l)
-            inv_chol_issue(blk_[l], blk_[l].Z, blk_[l].W2, blk_[l].LZ, blk_[l].Zinv, info_all_ + nb + l, st2_, ws2_,
-                           aux_[1]);
+            inv_chol_issue(blk_[l], blk_[l].Z, blk_[l].W2, blk_[l].LZ, blk_[l].Zinv, info_all_ + nb + l, st2_, ws2_);
         SDPG_CUDA(cudaEventRecord(ev_join_, st2_));
         SDPG_CUDA(cudaStreamWaitEvent(st_, ev_join_, 0));
         std::vector<int> info(2 * nb);
@@ -1388,8 +1366,7 @@ class Solver final : public SolverBase {
     Param par_;
     cudaStream_t st_;
     Workspace ws_, ws2_;  // ws2_ serves work issued on the second stream
-    Workspace aux_ws_[2];
-    PotrfAux aux_[2];     // look-ahead Cholesky helpers of the main (0) and second (1) streams
+
     cudaStream_t st2_ = nullptr;
     cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
     static constexpr int kPinned = 4096;
