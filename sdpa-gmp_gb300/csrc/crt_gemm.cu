@@ -65,14 +65,29 @@ CrtDevice crt_device() {
 
 constexpr int kExpWarps = 8;
 
+// Both operands of a product in one launch: operand 0 is op(A) (rows i), operand 1 is
+// op(B)^T (rows j); z indexes (operand, batch entry[, modulus group]).
 template <int N>
-__global__ void crt_exp_kernel(Operand<N> X, int O, int K, int Opad, int *E) {
+struct CrtOperands {
+    Operand<N> X[2];
+    int O[2], Opad[2];
+    int cnt[2];  // batch entries to process (0: operand not needed in this pass)
+    int *E[2];
+    __half *Q[2];
+    int lg[2];   // modulus groups per entry (residue kernel)
+};
+
+template <int N>
+__global__ void crt_exp_kernel(CrtOperands<N> ops, int K) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int z = blockIdx.y;
+    const int op = z < ops.cnt[0] ? 0 : 1;
+    const int b = op ? z - ops.cnt[0] : z;
     const int o = blockIdx.x * kExpWarps + warp;
-    const int b = blockIdx.y;
-    if (o >= Opad) return;
+    if (o >= ops.Opad[op]) return;
+    const Operand<N> X = ops.X[op];
     int emax = INT_MIN;
-    if (o < O) {
+    if (o < ops.O[op]) {
         const mlf<N> *base = X.X + b * X.sb + o * X.so;
         for (int k = lane; k < K; k += 32) {
             const mlf<N> *v = base + k * X.sk;
@@ -81,7 +96,7 @@ __global__ void crt_exp_kernel(Operand<N> X, int O, int K, int Opad, int *E) {
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, off));
-    if (lane == 0) E[(long long)b * Opad + o] = (emax == INT_MIN) ? 0 : emax;
+    if (lane == 0) ops.E[op][(long long)b * ops.Opad[op] + o] = (emax == INT_MIN) ? 0 : emax;
 }
 
 // Residues of op(X)[o,k] scaled to an integer below 2^R: Q[(b L + l)][o][k], padded
@@ -91,13 +106,20 @@ __global__ void crt_exp_kernel(Operand<N> X, int O, int K, int Opad, int *E) {
 // Small operands are spread over lgroups thread groups per entry, each taking every
 // lgroups-th modulus, so that enough threads are in flight.
 template <int N>
-__global__ void __launch_bounds__(256)
-    crt_residue_kernel(Operand<N> X, int O, int K, int Opad, int Kpad, const int *E, __half *Q, int lgroups) {
+__global__ void __launch_bounds__(256) crt_residue_kernel(CrtOperands<N> ops, int K, int Kpad) {
     constexpr int R = kCrtR;
     constexpr int LB = 10;
     const int k = blockIdx.x * 32 + threadIdx.x;
     const int o = blockIdx.y * 8 + threadIdx.y;
-    const int b = blockIdx.z / lgroups, lg = blockIdx.z - b * lgroups;
+    const int z0 = ops.cnt[0] * ops.lg[0];
+    const int op = (int)blockIdx.z < z0 ? 0 : 1;
+    const int zz = op ? (int)blockIdx.z - z0 : (int)blockIdx.z;
+    const int lgroups = ops.lg[op];
+    const int b = zz / lgroups, lg = zz - b * lgroups;
+    const int O = ops.O[op], Opad = ops.Opad[op];
+    const Operand<N> X = ops.X[op];
+    const int *E = ops.E[op];
+    __half *Q = ops.Q[op];
     if (o >= Opad || k >= Kpad) return;
     uint32_t chunk[kCrtPowChunks];
 #pragma unroll
@@ -182,9 +204,14 @@ template <int N>
 __global__ void __launch_bounds__(128)
     crt_reconstruct_kernel(const uint16_t *Y, int Mpad, int Npad, const int *EA, const int *EB, long long sEA,
                            long long sEB, int b0, int alpha_one, GemmProblem<N> p) {
-    const int j = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    const int i = blockIdx.y;
-    const int bl = blockIdx.z;
+    // outputs taken as (row, column pair) in row-major order, so narrow products
+    // still fill whole warps
+    const int npairs = (p.Nn + 1) >> 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)p.M * npairs) return;
+    const int i = (int)(t / npairs);
+    const int j = 2 * (int)(t - (long long)i * npairs);
+    const int bl = blockIdx.y;
     const bool ok0 = j < p.Nn && !(p.lower_only && i < j);
     const bool ok1 = j + 1 < p.Nn && !(p.lower_only && i < j + 1);
     if (!ok0 && !ok1) return;
@@ -296,24 +323,30 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
             const int b0 = g * L.G;
             const int G = min(L.G, p.batch - b0);
             const int gA = ab ? G : 1, gB = bb ? G : 1;
-            if (g == 0 || ab) {
-                Operand<N> A = p.A;
-                A.X += (long long)b0 * A.sb;
-                crt_exp_kernel<N><<<dim3(ceil_div(L.Mpad, kExpWarps), gA), 32 * kExpWarps, 0, s>>>(A, p.M, p.K, L.Mpad, EA);
+            CrtOperands<N> ops;
+            ops.X[0] = p.A;
+            ops.X[0].X += (long long)b0 * p.A.sb;
+            ops.X[1] = p.B;
+            ops.X[1].X += (long long)b0 * p.B.sb;
+            ops.O[0] = p.M;
+            ops.O[1] = p.Nn;
+            ops.Opad[0] = L.Mpad;
+            ops.Opad[1] = L.Npad;
+            ops.cnt[0] = (g == 0 || ab) ? gA : 0;  // an operand shared by the batch is done once
+            ops.cnt[1] = (g == 0 || bb) ? gB : 0;
+            ops.E[0] = EA;
+            ops.E[1] = EB;
+            ops.Q[0] = QA;
+            ops.Q[1] = QB;
+            const int opad = max(L.Mpad, L.Npad);
+            if (ops.cnt[0] + ops.cnt[1] > 0) {
+                crt_exp_kernel<N><<<dim3(ceil_div(opad, kExpWarps), ops.cnt[0] + ops.cnt[1]), 32 * kExpWarps, 0, s>>>(
+                    ops, p.K);
                 SDPG_CHECK_LAUNCH();
-                const int lgA = residue_groups(L.Kpad / 32 * (L.Mpad / 8) * gA);
-                crt_residue_kernel<N><<<dim3(L.Kpad / 32, L.Mpad / 8, gA * lgA), dim3(32, 8), 0, s>>>(
-                    A, p.M, p.K, L.Mpad, L.Kpad, EA, QA, lgA);
-                SDPG_CHECK_LAUNCH();
-            }
-            if (g == 0 || bb) {
-                Operand<N> B = p.B;
-                B.X += (long long)b0 * B.sb;
-                crt_exp_kernel<N><<<dim3(ceil_div(L.Npad, kExpWarps), gB), 32 * kExpWarps, 0, s>>>(B, p.Nn, p.K, L.Npad, EB);
-                SDPG_CHECK_LAUNCH();
-                const int lgB = residue_groups(L.Kpad / 32 * (L.Npad / 8) * gB);
-                crt_residue_kernel<N><<<dim3(L.Kpad / 32, L.Npad / 8, gB * lgB), dim3(32, 8), 0, s>>>(
-                    B, p.Nn, p.K, L.Npad, L.Kpad, EB, QB, lgB);
+                const int lg = residue_groups((long long)(L.Kpad / 32) * (opad / 8) * (ops.cnt[0] + ops.cnt[1]));
+                ops.lg[0] = ops.lg[1] = lg;
+                crt_residue_kernel<N><<<dim3(L.Kpad / 32, opad / 8, (ops.cnt[0] + ops.cnt[1]) * lg), dim3(32, 8), 0,
+                                        s>>>(ops, p.K, L.Kpad);
                 SDPG_CHECK_LAUNCH();
             }
             TcModGemm t{};
@@ -334,7 +367,7 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
             if (p.ev_before) SDPG_CUDA(cudaEventRecord(p.ev_before, s));
             tc_modgemm(t, s);
             if (p.ev_after) SDPG_CUDA(cudaEventRecord(p.ev_after, s));
-            crt_reconstruct_kernel<N><<<dim3(ceil_div(p.Nn, 256), p.M, G), 128, 0, s>>>(
+            crt_reconstruct_kernel<N><<<dim3(ceil_div((long long)p.M * ((p.Nn + 1) / 2), 128), G), 128, 0, s>>>(
                 Y, L.Mpad, L.Npad, EA, EB, ab ? L.Mpad : 0, bb ? L.Npad : 0, b0, alpha_one, p);
             SDPG_CHECK_LAUNCH();
         }

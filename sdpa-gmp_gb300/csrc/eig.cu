@@ -175,6 +175,9 @@ __device__ int newton_level(int k, const mlf<N> *d, const mlf<N> *b2s, mlf<M> &l
         if (ml_is_zero(delta) || delta.e < scale_e - tol) return 1;
         // steps that no longer shrink fourfold: the rounding floor of the recurrence
         if (delta.e > prev_e - 2) return 1;
+        // quadratic convergence: the error left after this step is about C delta^2 with
+        // C ~ delta / delta_prev^2; stop when that is already below the tolerance
+        if (prev_e != INT_MAX && 3 * delta.e - 2 * prev_e < scale_e - tol - 4) return 1;
         prev_e = delta.e;
     }
     return 0;
