@@ -259,6 +259,36 @@ def bench_ours(args) -> None:
                                    "integer-pipe figure)",
                     "imad_wide_per_mac": imad_per_mac, "traffic": None, **common}
 
+    # the same iterations with every product on the integer digit GEMM (the plain
+    # multi-limb path): the tensor-core path's speed-up at equal accuracy
+    plain = None
+    if args.precision <= 256 and not args.no_plain:
+        old_method = sdpg.set_gemm_method(1)
+        try:
+            sp = new_solver()
+            for _ in range(args.warmup):
+                if not sp.iterate():
+                    sp = new_solver()
+            torch.cuda.synchronize()
+            p0 = torch.cuda.Event(enable_timing=True)
+            p1 = torch.cuda.Event(enable_timing=True)
+            p0.record(stream)
+            k = 0
+            while k < args.steps:
+                if sp.iterate():
+                    k += 1
+                else:
+                    sp = new_solver()
+            p1.record(stream)
+            torch.cuda.synchronize()
+            pms = p0.elapsed_time(p1)
+            plain = {"value": args.steps / (pms * 1e-3), "unit": UNIT, "ms_per_step": pms / args.steps,
+                     "method": "integer digit GEMM on the CUDA cores (sdpg_set_gemm_method(1))",
+                     "tensor_speedup": (pms / args.steps) / (ms / args.steps) if ms > 0 else None}
+            sp.close()
+        finally:
+            sdpg.set_gemm_method(old_method)
+
     # end to end through the public API: host .dat-s -> parse -> upload -> full solve -> xVec back
     e2e = None
     if not args.no_e2e:
@@ -296,6 +326,7 @@ def bench_ours(args) -> None:
                 "data": "synthetic (seeded generator standing in for SDPLIB gpp500)",
                 "config": config(args.precision, ws_mb),
                 "impl": "ours", "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+                "plain_path": plain,
                 "clocks": clk, "phase_ms": {k: round(v, 3) for k, v in timers.items()},
                 "restarts": restarts, "peaks": {k: measured_peaks().get(k) for k in ("hbm_gbs", "bf16_tflops")}}
         print(json.dumps(line))
@@ -330,6 +361,46 @@ def bench_reference(args) -> None:
         line = {"impl": "reference", "unavailable": f"CPU port failed: {exc}"}
     print(json.dumps(line))
     shutil.rmtree(d, ignore_errors=True)
+
+
+def bench_batch(args) -> None:
+    """Batched mode (cfg4 shape): control/LMI instances with m ~ U[20, 350] and two
+    blocks of sizes ~ U[15, 90] (seeds 0 .. batch-1) solved by sdpg_solve_batch with
+    --concurrency solvers in flight, against the same solver run one problem at a time
+    on the first --serial instances; prints solves/s for both."""
+    import numpy as np
+    import torch
+    sdpg = importlib.import_module("sdpa-gmp_gb300")
+    problems = importlib.import_module("sdpa-gmp_gb300.problems")
+    t0 = time.perf_counter()
+    probs = [sdpg.Problem.from_dense(*problems.batch_instance(seed)) for seed in range(args.batch)]
+    gen_s = time.perf_counter() - t0
+    param = sdpg.Param.default()
+    param.precision = args.precision
+    # warm-up: one small solve (library set-up, tensor-core tables)
+    sdpg.solve_batch(probs[:1], param, concurrency=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    its, info = sdpg.solve_batch(probs, param, concurrency=args.concurrency)
+    torch.cuda.synchronize()
+    batched_s = time.perf_counter() - t0
+    ns = min(args.serial, args.batch)
+    t0 = time.perf_counter()
+    its_s, info_s = sdpg.solve_batch(probs[:ns], param, concurrency=1)
+    torch.cuda.synchronize()
+    serial_s = time.perf_counter() - t0
+    phases = [sdpg.PHASES[int(x)] for x in info[:, 0]]
+    line = {"metric": f"batched solves/s ({args.precision}-bit control/LMI SDPs, m~U[20,350], two blocks ~U[15,90])",
+            "value": args.batch / batched_s, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+            "config": {"workload": f"{args.batch} instances, seeds 0..{args.batch - 1}",
+                       "concurrency": args.concurrency, "precision_bits": args.precision},
+            "serial": {"value": ns / serial_s, "unit": "solves/s", "instances": ns},
+            "speedup_vs_serial": (args.batch / batched_s) / (ns / serial_s),
+            "iterations_mean": float(np.mean(its)), "pdOPT": sum(p == "pdOPT" for p in phases),
+            "failed": int(np.sum(its < 0)),
+            "identical_to_serial": bool(np.array_equal(info[:ns], info_s)),
+            "generation_s": gen_s, "data": "synthetic (seeded generator)"}
+    print(json.dumps(line))
 
 
 def bench_gemm(args) -> None:
@@ -388,11 +459,19 @@ def main():
     ap.add_argument("--precision", type=int, default=256)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the digit-GEMM (plain path) comparison")
+    ap.add_argument("--workload", choices=["ipm", "batch"], default="ipm",
+                    help="batch: many small control/LMI solves at once (solves/s) instead of IPM iterations")
+    ap.add_argument("--batch", type=int, default=64, help="batch mode: instances")
+    ap.add_argument("--concurrency", type=int, default=16, help="batch mode: solvers in flight")
+    ap.add_argument("--serial", type=int, default=8, help="batch mode: instances timed one at a time")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.kernel == "gemm":
         bench_gemm(args)
+    elif args.workload == "batch" and args.impl != "reference":
+        bench_batch(args)
     elif args.impl == "reference":
         bench_reference(args)
     else:

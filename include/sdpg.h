@@ -145,6 +145,11 @@ void sdpg_problem_free(sdpg_problem *p);
 int sdpg_problem_set_c(sdpg_problem *p, int k, const char *text);
 int sdpg_problem_add_entry(sdpg_problem *p, int k, int block, int i, int j, const char *text);
 int sdpg_problem_add_entry_mpf(sdpg_problem *p, int k, int block, int i, int j, const sdpg_mpf_t *v);
+/* Bulk input (no reference counterpart; the reference builds F_k entry by entry in
+ * IO::read): c_k from a double (exact), and the upper triangle of a dense symmetric
+ * n x n block of F_k from column-major doubles (each exact), n = the block size. */
+int sdpg_problem_set_c_double(sdpg_problem *p, int k, double v);
+int sdpg_problem_add_dense(sdpg_problem *p, int k, int block, int n, const double *A);
 
 /* GPU-resident solver state (the reference's Solutions, Residuals, Newton and
  * WorkVariables, sdpa_dataset.h:29-177, sdpa_newton.h:33-168).  stream may be NULL. */
@@ -210,8 +215,8 @@ int sdpg_solver_io_bytes(sdpg_solver *h, long long *h2d, long long *d2h);
 /* Total kernel launches made by the library in this process. */
 unsigned long long sdpg_launch_count(void);
 /* GEMM method for 256-bit products: 0 (default) the residue-number-system path on the
- * tcgen05 tensor cores wherever it applies (K <= 1024, not tiny), 1 the integer digit
- * GEMM everywhere, 2 the residue path for every product with K <= 1024 (tests).
+ * tcgen05 tensor cores wherever it applies (K <= 16384, not tiny), 1 the integer digit
+ * GEMM everywhere, 2 the residue path for every product with K <= 16384 (tests).
  * Returns the previous method.  Both paths meet the same error bound. */
 int sdpg_set_gemm_method(int method);
 /* *flag = non-zero if a tensor-core GEMM kernel on `device` ever gave up a bounded wait
@@ -222,6 +227,15 @@ int sdpg_tensor_error(int device, int *flag);
 int sdpg_probe_imad_wide(int device, double *ops_per_second);
 /* Read data + param, solve, write the result file: `sdpa_gmp -ds data -o out -p param`
  * (main / pinpal, sdpa_main.cpp:43-461, 501-677).  Returns iterations; info12 as above. */
+/* Batched solves (no reference counterpart; the reference solves one problem per
+ * process): `count` problems with one parameter set (NULL: defaults), up to
+ * `concurrency` solvers in flight at once, one host thread and its own CUDA streams
+ * each, so many small latency-bound solves share the GPU.  info12[12 i] and
+ * iterations[i] (either may be NULL) receive each problem's summary and iteration
+ * count, or iterations[i] < 0 (an SDPG_ERR_* code) if that solve failed.  Returns the
+ * number of problems solved without error. */
+int sdpg_solve_batch(int count, sdpg_problem *const *problems, const sdpg_param *param, int device, int concurrency,
+                     double *info12, int *iterations);
 int sdpg_solve_file(const char *data_path, const char *param_path, const char *out_path, int device,
                     double *info12);
 

@@ -81,6 +81,9 @@ def _setup(lib: ctypes.CDLL) -> ctypes.CDLL:
         "sdpg_problem_set_c": (i, [vp, i, c.c_char_p]),
         "sdpg_problem_add_entry": (i, [vp, i, i, i, i, c.c_char_p]),
         "sdpg_problem_add_entry_mpf": (i, [vp, i, i, i, i, vp]),
+        "sdpg_problem_set_c_double": (i, [vp, i, c.c_double]),
+        "sdpg_problem_add_dense": (i, [vp, i, i, i, vp]),
+        "sdpg_solve_batch": (i, [i, vp, c.POINTER(Param), i, i, vp, vp]),
         "sdpg_solver_create": (vp, [vp, c.POINTER(Param), i, vp, c.POINTER(i)]),
         "sdpg_solver_destroy": (None, [vp]),
         "sdpg_solver_limbs": (i, [vp]),
@@ -283,6 +286,29 @@ class Problem:
     def add_entry(self, k: int, block: int, i: int, j: int, value) -> None:
         check(lib().sdpg_problem_add_entry(self.h, k, block, i, j, str(value).encode()))
 
+    def set_c_double(self, k: int, value: float) -> None:
+        check(lib().sdpg_problem_set_c_double(self.h, k, float(value)))
+
+    def add_dense(self, k: int, block: int, A: np.ndarray) -> None:
+        """Upper triangle of the dense symmetric block `block` of F_k (doubles, exact)."""
+        A = np.asfortranarray(A, dtype=np.float64)
+        check(lib().sdpg_problem_add_dense(self.h, k, block, A.shape[0], A.ctypes.data))
+
+    @classmethod
+    def from_dense(cls, c, F0, F) -> "Problem":
+        """min c.x  s.t.  sum_i F_i x_i - F0 >= 0, with dense symmetric blocks:
+        c (m,), F0 list of (n_l, n_l), F list over blocks of (m, n_l, n_l)."""
+        m = len(c)
+        blocks = [int(b.shape[0]) for b in F0]
+        prob = cls.new(m, blocks)
+        for k in range(m):
+            prob.set_c_double(k + 1, float(c[k]))
+        for l, b in enumerate(F0):
+            prob.add_dense(0, l + 1, b)
+            for k in range(m):
+                prob.add_dense(k + 1, l + 1, F[l][k])
+        return prob
+
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:
             _lib.sdpg_problem_free(self.h)
@@ -426,7 +452,7 @@ class Solver:
 
 def set_gemm_method(method: int) -> int:
     """0: tensor-core residue path for 256-bit GEMMs where it applies; 1: digit GEMM only;
-    2: residue path for every 256-bit GEMM with K <= 1024.  Returns the previous method."""
+    2: residue path for every 256-bit GEMM with K <= 16384.  Returns the previous method."""
     return check(lib().sdpg_set_gemm_method(method))
 
 
@@ -434,6 +460,20 @@ def tensor_error(device: int = 0) -> int:
     flag = ctypes.c_int(0)
     check(lib().sdpg_tensor_error(device, ctypes.byref(flag)))
     return flag.value
+
+
+def solve_batch(problems, param: Param | None = None, device: int = 0, concurrency: int = 16):
+    """Solve many problems with up to `concurrency` solvers in flight on the GPU.
+    Returns (iterations, info): iterations[i] < 0 is the error code of a failed solve;
+    info[i] holds the 12 summary values of Solver.info() in INFO_KEYS order."""
+    n = len(problems)
+    handles = (ctypes.c_void_p * max(n, 1))(*[p.h for p in problems])
+    info = np.zeros((max(n, 1), 12), dtype=np.float64)
+    its = np.zeros(max(n, 1), dtype=np.int32)
+    prm = param if param is not None else Param.default()
+    check(lib().sdpg_solve_batch(n, handles, ctypes.byref(prm), device, concurrency, info.ctypes.data,
+                                 its.ctypes.data))
+    return its[:n], info[:n]
 
 
 def launch_count() -> int:

@@ -5,7 +5,7 @@
 #include "sdpg.h"
 
 namespace sdpg {
-unsigned long long g_kernel_launches = 0;
+std::atomic<unsigned long long> g_kernel_launches{0};
 }
 
 using namespace sdpg;
@@ -41,7 +41,7 @@ __global__ void imad_wide_probe_kernel(const int *in, long long *out, int iters)
 
 extern "C" {
 
-unsigned long long sdpg_launch_count(void) { return g_kernel_launches; }
+unsigned long long sdpg_launch_count(void) { return g_kernel_launches.load(); }
 
 int sdpg_set_gemm_method(int method) {
     return sdpg_guard([&] {

@@ -2,7 +2,11 @@
 // step-wise Newton / step-length / update entry points.
 #include <string.h>
 
+#include <algorithm>
+#include <atomic>
 #include <memory>
+#include <thread>
+#include <vector>
 
 #include "capi_util.cuh"
 #include "ml_host.h"
@@ -155,6 +159,35 @@ int sdpg_problem_set_c(sdpg_problem *p, int k, const char *text) {
         mlf<16> v;
         if (!ml_parse<16>(text, &v)) throw sdpg_error(SDPG_ERR_ARG, "not a number");
         p->P.c[k - 1] = v;
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_problem_set_c_double(sdpg_problem *p, int k, double v) {
+    return sdpg_guard([&] {
+        if (!p || k < 1 || k > p->P.m) throw sdpg_error(SDPG_ERR_ARG, "bad c index");
+        p->P.c[k - 1] = ml_from_double<16>(v);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_problem_add_dense(sdpg_problem *p, int k, int block, int n, const double *A) {
+    return sdpg_guard([&] {
+        if (!p || !A || k < 0 || k > p->P.m || block < 1 || block > (int)p->P.blockStruct.size())
+            throw sdpg_error(SDPG_ERR_ARG, "entry index out of range");
+        const int bs = p->P.blockStruct[block - 1];
+        if (bs < 0 || n != bs) throw sdpg_error(SDPG_ERR_ARG, "n must equal the (SDP) block size");
+        p->P.entries.reserve(p->P.entries.size() + (size_t)n * (n + 1) / 2);
+        for (int b = 0; b < n; ++b)
+            for (int a = 0; a <= b; ++a) {
+                RawEntry e;
+                e.k = k;
+                e.block = block - 1;
+                e.i = a;
+                e.j = b;
+                e.v = ml_from_double<16>(A[a + (size_t)b * n]);
+                p->P.entries.push_back(e);
+            }
         return (int)SDPG_OK;
     });
 }
@@ -420,6 +453,48 @@ int sdpg_solve_file(const char *data_path, const char *param_path, const char *o
         if (out) fclose(out);
         if (info12) h->s->info(info12);
         return it;
+    });
+}
+
+int sdpg_solve_batch(int count, sdpg_problem *const *problems, const sdpg_param *param, int device, int concurrency,
+                     double *info12, int *iterations) {
+    return sdpg_guard([&] {
+        if (count < 0 || (count > 0 && !problems) || concurrency < 1)
+            throw sdpg_error(SDPG_ERR_ARG, "bad batch arguments");
+        for (int i = 0; i < count; ++i)
+            if (!problems[i]) throw sdpg_error(SDPG_ERR_ARG, "null problem in batch");
+        const Param q = param ? to_param(param) : Param();
+        check_param(q);
+        std::atomic<int> next{0}, solved{0};
+        auto worker = [&]() {
+            if (cudaSetDevice(device) != cudaSuccess) return;
+            for (;;) {
+                const int i = next.fetch_add(1);
+                if (i >= count) break;
+                int its;
+                try {
+                    // each solver owns its streams and scratch: solvers on different
+                    // host threads run concurrently on the GPU
+                    std::unique_ptr<sdpg_solver> h(wrap(problems[i]->P, q, device, nullptr));
+                    its = h->s->run(nullptr, nullptr);
+                    if (info12) h->s->info(info12 + 12 * (size_t)i);
+                    solved.fetch_add(1);
+                } catch (const sdpg_error &e) {
+                    set_last_error(e.what());
+                    its = e.code;
+                } catch (const std::exception &e) {
+                    set_last_error(e.what());
+                    its = SDPG_ERR_ARG;
+                }
+                if (iterations) iterations[i] = its;
+            }
+        };
+        const int nt = std::min(concurrency, std::max(count, 1));
+        std::vector<std::thread> threads;
+        threads.reserve(nt);
+        for (int t = 0; t < nt; ++t) threads.emplace_back(worker);
+        for (auto &t : threads) t.join();
+        return solved.load();
     });
 }
 

@@ -1,6 +1,7 @@
 // Shared host-side plumbing for the CUDA kernels: error codes, a growable
 // device workspace, and launch helpers.
 #pragma once
+#include <atomic>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -28,11 +29,11 @@ struct sdpg_error : std::runtime_error {
 
 // Every kernel launch in the library is followed by SDPG_CHECK_LAUNCH(), which also
 // counts it (sdpg_launch_count reports the total).
-extern unsigned long long g_kernel_launches;
-#define SDPG_CHECK_LAUNCH()                 \
-    do {                                    \
-        ++::sdpg::g_kernel_launches;        \
-        SDPG_CUDA(cudaGetLastError());      \
+extern std::atomic<unsigned long long> g_kernel_launches;
+#define SDPG_CHECK_LAUNCH()                                                         \
+    do {                                                                            \
+        ::sdpg::g_kernel_launches.fetch_add(1, std::memory_order_relaxed);          \
+        SDPG_CUDA(cudaGetLastError());                                              \
     } while (0)
 
 // Device scratch that only grows; one per problem handle (or per C-ABI call).

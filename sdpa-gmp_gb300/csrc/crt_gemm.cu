@@ -1,5 +1,5 @@
 // Residue-number-system (Chinese remainder) multi-limb GEMM on the tensor cores, for
-// 256-bit operands.
+// 256-bit operands and K up to 16384.
 //
 //   1. Exponents: EA_i = max_k exponent(op(A)[i,k]), EB_j likewise over op(B)[:,j].
 //   2. Residues: each entry becomes the integer X = trunc(x 2^(R - E)), |X| < 2^R with
@@ -280,6 +280,9 @@ inline int residue_groups(long long blocks) {
 
 }  // namespace
 
+// Longest sum the moduli cover: K 2^(2R) = 2^566 keeps |V / M| below 1/4.
+constexpr int kCrtMaxK = 1 << 14;
+
 // 0: tensor-core residue path where it applies and the product is not tiny;
 // 1: digit GEMM only; 2: residue path for every 256-bit product with K <= 1024
 int g_gemm_method = 0;
@@ -289,7 +292,7 @@ bool crt_gemm_applies(const GemmProblem<N> &p) {
     if constexpr (N != 8) {
         return false;
     } else {
-        if (g_gemm_method == 1 || p.K <= 0 || p.K > kTcMaxK || p.M <= 0 || p.Nn <= 0) return false;
+        if (g_gemm_method == 1 || p.K <= 0 || p.K > kCrtMaxK || p.M <= 0 || p.Nn <= 0) return false;
         return g_gemm_method == 2 || (double)p.M * p.Nn * p.K * p.batch >= (double)(1 << 15);
     }
 }
@@ -359,13 +362,20 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
             t.b_batched = bb;
             t.Mpad = L.Mpad;
             t.Npad = L.Npad;
-            t.Kpad = L.Kpad;
+            t.kpitch = L.Kpad;
             t.lower_only = p.lower_only;
             t.moduli = dev.moduli;
             t.cfac = dev.cfac;
             t.error = dev.error;
             if (p.ev_before) SDPG_CUDA(cudaEventRecord(p.ev_before, s));
-            tc_modgemm(t, s);
+            // K beyond the tensor memory's four exact accumulators runs in chunks whose
+            // residues are added modulo each prime in the epilogue
+            for (int k0 = 0; k0 < L.Kpad; k0 += kTcMaxK) {
+                t.k0 = k0;
+                t.Kpad = min(kTcMaxK, L.Kpad - k0);
+                t.accumulate = k0 > 0;
+                tc_modgemm(t, s);
+            }
             if (p.ev_after) SDPG_CUDA(cudaEventRecord(p.ev_after, s));
             crt_reconstruct_kernel<N><<<dim3(ceil_div((long long)p.M * ((p.Nn + 1) / 2), 128), G), 128, 0, s>>>(
                 Y, L.Mpad, L.Npad, EA, EB, ab ? L.Mpad : 0, bb ? L.Npad : 0, b0, alpha_one, p);

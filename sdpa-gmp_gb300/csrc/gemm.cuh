@@ -70,7 +70,7 @@ template <int N>
 size_t gemm_workspace_bytes(const GemmProblem<N> &p);
 
 // Runs the GEMM on `stream`; scratch is carved from ws (which must already hold
-// gemm_workspace_bytes(p) beyond ws.used).  256-bit products with K <= 1024 that are
+// gemm_workspace_bytes(p) beyond ws.used).  256-bit products with K <= 16384 that are
 // not tiny go through the residue-number-system path on the tensor cores
 // (crt_gemm.cu); everything else through the digit GEMM below.
 template <int N>

@@ -196,8 +196,8 @@ __global__ void __launch_bounds__(128, 1)
             const uint32_t fb = smem_u32(&full[s]);
             mbar_expect_tx(fb, kStageBytes);
             uint8_t *st = smem + s * kStageBytes;
-            tma_load_2d(smem_u32(st), &tmA, kb * kTcBK, arow, fb);
-            tma_load_2d(smem_u32(st + kTileBytes), &tmB, kb * kTcBK, brow, fb);
+            tma_load_2d(smem_u32(st), &tmA, p.k0 + kb * kTcBK, arow, fb);
+            tma_load_2d(smem_u32(st + kTileBytes), &tmB, p.k0 + kb * kTcBK, brow, fb);
             ++issued;
         }
         if (!ok) {
@@ -261,6 +261,18 @@ __global__ void __launch_bounds__(128, 1)
                 for (int q = 0; q < 32; ++q) r[q] += mod_of_float(__uint_as_float(v[q]), m, inv_m);
             }
             uint32_t packed[16];
+            uint4 *dst = reinterpret_cast<uint4 *>(yrow + cb * 32);
+            uint32_t prev[16];
+            if (p.accumulate) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint4 v = dst[q];
+                    prev[4 * q] = v.x;
+                    prev[4 * q + 1] = v.y;
+                    prev[4 * q + 2] = v.z;
+                    prev[4 * q + 3] = v.w;
+                }
+            }
 #pragma unroll
             for (int q = 0; q < 32; q += 2) {
                 // r < nacc m <= 4m: reduce with at most three subtractions
@@ -272,9 +284,14 @@ __global__ void __launch_bounds__(128, 1)
                 }
                 y0 = mulmod(y0, c, m, inv_m);
                 y1 = mulmod(y1, c, m, inv_m);
+                if (p.accumulate) {  // an earlier K chunk of the same product: add mod m
+                    y0 += (int)(prev[q / 2] & 0xFFFFu);
+                    y1 += (int)(prev[q / 2] >> 16);
+                    y0 -= (y0 >= m) ? m : 0;
+                    y1 -= (y1 >= m) ? m : 0;
+                }
                 packed[q / 2] = (uint32_t)y0 | ((uint32_t)y1 << 16);
             }
-            uint4 *dst = reinterpret_cast<uint4 *>(yrow + cb * 32);
 #pragma unroll
             for (int q = 0; q < 4; ++q)
                 dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
@@ -322,7 +339,7 @@ CUtensorMap make_map(const __half *base, long long rows, int cols) {
 
 void tc_modgemm(const TcModGemm &p, cudaStream_t s) {
     if (p.Mpad % kTcBM || p.Npad % kTcBN || p.Kpad % kTcBK || p.Kpad <= 0 || p.Kpad > kTcMaxK || p.L <= 0 ||
-        p.batch <= 0)
+        p.batch <= 0 || p.k0 % kTcBK || p.k0 < 0 || p.kpitch % kTcBK || p.k0 + p.Kpad > p.kpitch)
         throw sdpg_error(SDPG_ERR_ARG, "tc_modgemm: unsupported shape");
     if (((uintptr_t)p.A | (uintptr_t)p.B | (uintptr_t)p.Y) & 15)
         throw sdpg_error(SDPG_ERR_ARG, "tc_modgemm: operands must be 16-byte aligned");
@@ -332,8 +349,8 @@ void tc_modgemm(const TcModGemm &p, cudaStream_t s) {
     });
     const long long arows = (long long)(p.a_batched ? p.batch : 1) * p.L * p.Mpad;
     const long long brows = (long long)(p.b_batched ? p.batch : 1) * p.L * p.Npad;
-    const CUtensorMap ma = make_map(p.A, arows, p.Kpad);
-    const CUtensorMap mb = make_map(p.B, brows, p.Kpad);
+    const CUtensorMap ma = make_map(p.A, arows, p.kpitch);
+    const CUtensorMap mb = make_map(p.B, brows, p.kpitch);
     dim3 grid(p.Npad / kTcBN, p.Mpad / kTcBM, p.batch * p.L);
     tc_modgemm_kernel<<<grid, 128, kSmemBytes, s>>>(ma, mb, p);
     SDPG_CHECK_LAUNCH();

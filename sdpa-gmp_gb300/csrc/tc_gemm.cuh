@@ -29,7 +29,10 @@ struct TcModGemm {
     int L;            // moduli
     int batch;        // z = b * L + l; A plane (bA * L + l) with bA = b if a_batched else 0
     int a_batched, b_batched;
-    int Mpad, Npad, Kpad;  // multiples of 128, 128, 64; Kpad <= kTcMaxK
+    int Mpad, Npad, Kpad;  // multiples of 128, 128, 64; Kpad <= kTcMaxK: the K range of this call
+    int k0;                // first K index of this call within the planes (a multiple of 64)
+    int kpitch;            // K extent of the planes (their row length)
+    int accumulate;        // 1: Y = (Y + new) mod m (a later K chunk of the same product)
     int lower_only;        // 1: skip tiles strictly above the diagonal (their Y is not written)
     const int *moduli;     // device, L entries
     const int *cfac;       // device, L entries

@@ -263,3 +263,40 @@ def write_workload(name: str, directory: str) -> tuple[str, str]:
     with open(par, "w") as f:
         f.write(param_text(precision=prec))
     return dat, par
+
+
+def _spd_np(n: int, rng: np.random.Generator) -> np.ndarray:
+    """Q diag(U[0.5, 2]) Q^T with Q Haar-orthogonal (numpy sums)."""
+    q, r = np.linalg.qr(rng.standard_normal((n, n)))
+    q = q * np.sign(np.diag(r))
+    lam = rng.uniform(0.5, 2.0, n)
+    return (q * lam) @ q.T
+
+
+def control_dense(m: int, blocks, rng: np.random.Generator):
+    """The control/LMI construction of `control` with numpy sums, returned as dense
+    arrays for Problem.from_dense (c, F0 blocks, F blocks of shape (m, n, n)); entries
+    are dyadic (k / 2^24).  Not byte-identical across machines (BLAS sums); used for
+    the batched workload, whose instances are generated where they are solved."""
+    scale = float(1 << _DYADIC_BITS)
+    dy = lambda x: np.round(x * scale) / scale  # noqa: E731
+    F = []
+    for nb in blocks:
+        g = rng.standard_normal((m, nb, nb))
+        F.append(dy((g + g.transpose(0, 2, 1)) / math.sqrt(2.0)))
+    X0 = [_spd_np(nb, rng) for nb in blocks]
+    y0 = rng.standard_normal(m)
+    Z0 = [_spd_np(nb, rng) for nb in blocks]
+    c = dy(sum(np.einsum("iab,ab->i", F[l], X0[l]) for l in range(len(blocks))))
+    F0 = [dy(-(Z0[l] + np.tensordot(y0, F[l], axes=1))) for l in range(len(blocks))]
+    F0 = [(b + b.T) / 2 for b in F0]  # exactly symmetric (the halves are dyadic)
+    return c, F0, F
+
+
+def batch_instance(seed: int):
+    """One instance of the batched workload: m ~ U[20, 350], two blocks of sizes
+    ~ U[15, 90], control/LMI construction, all drawn from `seed`."""
+    rng = np.random.default_rng(seed)
+    m = int(rng.integers(20, 351))
+    blocks = [int(x) for x in rng.integers(15, 91, size=2)]
+    return control_dense(m, blocks, rng)

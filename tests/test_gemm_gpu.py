@@ -79,12 +79,14 @@ def _wide_case(sdpg, exact):
     assert exact.max_rel_err(got, ref, scale) <= 2.0 ** -240
 
 
-@pytest.mark.parametrize("m,n,k", [(500, 500, 500), (257, 131, 1024), (300, 200, 1025), (640, 384, 96)])
+@pytest.mark.parametrize("m,n,k", [(500, 500, 500), (257, 131, 1024), (300, 200, 1025), (640, 384, 96),
+                                   (130, 70, 4000), (16, 20, 16400)])
 def test_residue_path_agrees_with_digit_gemm_at_full_size(sdpg, exact, m, n, k):
     """At sizes the exact oracle cannot reach in seconds, the tensor-core residue path
     and the digit GEMM (both checked against exact arithmetic above) must agree within
-    twice the normwise bound, entry by entry.  K = 1025 exceeds the tensor path's limit
-    and falls back to the digit GEMM (identical results)."""
+    twice the normwise bound, entry by entry.  K above 1024 runs the tensor GEMM in
+    chunks whose residues are added modulo each prime; K = 16400 exceeds the residue
+    path's range and falls back to the digit GEMM (identical results)."""
     import numpy as np
     rng = random.Random(m * 7 + n * 3 + k)
     A = exact.random_ml(m * k, 8, rng, -20, 20, zero_frac=0.02)
@@ -99,7 +101,7 @@ def test_residue_path_agrees_with_digit_gemm_at_full_size(sdpg, exact, m, n, k):
             out[method] = sdpg.rgemm("N", "N", m, n, k, alpha, A, m, B, k, beta, C, m)
         finally:
             sdpg.set_gemm_method(old)
-    if k > 1024:
+    if k > 16384:
         assert (out[0] == out[1]).all()
         return
     # normwise scale per entry: |alpha| K max_t|a_it| max_t|b_tj| + |beta c_ij|, in doubles
