@@ -4,9 +4,50 @@
 #include "gemm.cuh"
 #include "sdpg.h"
 
+#include <map>
+#include <mutex>
+#include <vector>
+
 namespace sdpg {
 std::atomic<unsigned long long> g_kernel_launches{0};
+
+void keep_pool_memory(int device) {
+    static std::mutex mu;
+    static bool done[64] = {};
+    if (device < 0 || device >= 64) return;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done[device]) return;
+    cudaMemPool_t pool;
+    SDPG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t keep = UINT64_MAX;
+    SDPG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    done[device] = true;
 }
+
+static std::mutex g_pinned_mu;
+static std::map<size_t, std::vector<void *>> g_pinned_free;
+
+void *pinned_acquire(size_t bytes) {
+    {
+        std::lock_guard<std::mutex> lock(g_pinned_mu);
+        auto &v = g_pinned_free[bytes];
+        if (!v.empty()) {
+            void *p = v.back();
+            v.pop_back();
+            return p;
+        }
+    }
+    void *p = nullptr;
+    SDPG_CUDA(cudaMallocHost(&p, bytes));
+    return p;
+}
+
+void pinned_release(void *p, size_t bytes) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lock(g_pinned_mu);
+    g_pinned_free[bytes].push_back(p);
+}
+}  // namespace sdpg
 
 using namespace sdpg;
 

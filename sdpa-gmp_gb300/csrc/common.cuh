@@ -36,23 +36,33 @@ extern std::atomic<unsigned long long> g_kernel_launches;
         SDPG_CUDA(cudaGetLastError());                                              \
     } while (0)
 
-// Device scratch that only grows; one per problem handle (or per C-ABI call).
+// Device scratch that only grows; one per problem handle (or per C-ABI call).  With an
+// allocation stream set, memory comes from the device's stream-ordered pool
+// (cudaMallocAsync / cudaFreeAsync), so creating and destroying solvers does not
+// synchronise the device under other solvers' work.
 struct Workspace {
     char *base = nullptr;
     size_t cap = 0;
     size_t used = 0;
-    ~Workspace() {
-        if (base) cudaFree(base);
+    cudaStream_t stream = nullptr;
+    ~Workspace() { release(); }
+    void release() {
+        if (base) {
+            if (stream) cudaFreeAsync(base, stream);
+            else cudaFree(base);
+        }
+        base = nullptr;
+        cap = 0;
+        used = 0;
     }
     void reserve(size_t bytes) {
         if (bytes <= cap) return;
         if (base) {
-            SDPG_CUDA(cudaDeviceSynchronize());
-            SDPG_CUDA(cudaFree(base));
+            if (!stream) SDPG_CUDA(cudaDeviceSynchronize());
+            release();
         }
-        base = nullptr;
-        cap = 0;
-        SDPG_CUDA(cudaMalloc(&base, bytes));
+        if (stream) SDPG_CUDA(cudaMallocAsync((void **)&base, bytes, stream));
+        else SDPG_CUDA(cudaMalloc(&base, bytes));
         cap = bytes;
     }
     // carve `bytes` (256-aligned) out of a reservation of `total` made beforehand
@@ -64,6 +74,15 @@ struct Workspace {
     }
     void reset() { used = 0; }
 };
+
+// Keep memory freed to the device's default pool cached there (instead of returning it
+// to the driver at every synchronisation), once per device.
+void keep_pool_memory(int device);
+
+// Page-locked host staging buffers of `bytes`, recycled across solvers (allocating
+// page-locked memory is slow and serialises); released buffers stay in the pool.
+void *pinned_acquire(size_t bytes);
+void pinned_release(void *p, size_t bytes);
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }

@@ -57,16 +57,25 @@ class Solver final : public SolverBase {
   public:
     Solver(const RawProblem &P, const Param &par, int device, cudaStream_t stream) : par_(par), st_(stream) {
         SDPG_CUDA(cudaSetDevice(device));
+        if (!st_) throw sdpg_error(SDPG_ERR_ARG, "the solver needs a stream");
+        keep_pool_memory(device);
+        ws_.stream = st_;
+        ws2_.stream = st_;
         setup(P);
+        SDPG_CUDA(cudaStreamSynchronize(st_));  // allocations and uploads complete
     }
+    // Device memory goes back to the stream-ordered pool on the main stream once both
+    // streams are idle: no device-wide synchronisation, so concurrent solvers keep running.
     ~Solver() override {
+        cudaStreamSynchronize(st_);
         if (st2_) cudaStreamSynchronize(st2_);
         if (st2_) cudaStreamDestroy(st2_);
-
         if (ev_fork_) cudaEventDestroy(ev_fork_);
         if (ev_join_) cudaEventDestroy(ev_join_);
-        if (pinned_) cudaFreeHost(pinned_);
-        for (void *p : allocs_) cudaFree(p);
+        pinned_release(pinned_, kPinned * sizeof(V));
+        for (void *p : allocs_) cudaFreeAsync(p, st_);
+        ws_.release();
+        ws2_.release();
         for (auto &e : ev_) cudaEventDestroy(e);
         for (auto &e : prof_ev_) cudaEventDestroy(e);
     }
@@ -332,7 +341,7 @@ class Solver final : public SolverBase {
         SDPG_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
         SDPG_CUDA(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
         SDPG_CUDA(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
-        SDPG_CUDA(cudaMallocHost(&pinned_, kPinned * sizeof(V)));
+        pinned_ = (V *)pinned_acquire(kPinned * sizeof(V));
         info2_ = (int *)dalloc_raw(sizeof(int) * (4 * blk_.size() + 16));
         info_all_ = (int *)dalloc_raw(sizeof(int) * (4 * blk_.size() + 16));
         ev_.resize(2);
@@ -358,14 +367,68 @@ class Solver final : public SolverBase {
         return gemm_workspace_bytes<N>(p);
     }
 
+    // ---------------------------------------------------------------- CUDA graphs
+    //
+    // A launch-heavy, host-sync-free sequence (a factorisation with its panel products)
+    // runs eagerly on its first call (one-time set-up: tables, kernel attributes), is
+    // captured into a graph on the second and replayed from then on: one host call
+    // instead of hundreds, which is what bounds small problems and concurrent solvers.
+    // Everything such a sequence touches (buffers, workspace offsets, sizes) is fixed
+    // for the life of the solver.
+    struct GraphSlot {
+        cudaGraphExec_t exec = nullptr;
+        int calls = 0;
+        unsigned long long launches = 0;  // kernels in the graph (for the launch counter)
+        GraphSlot() = default;
+        GraphSlot(const GraphSlot &) = delete;
+        GraphSlot(GraphSlot &&o) noexcept : exec(o.exec), calls(o.calls), launches(o.launches) { o.exec = nullptr; }
+        ~GraphSlot() {
+            if (exec) cudaGraphExecDestroy(exec);
+        }
+    };
+    template <class F>
+    void graphed(GraphSlot &g, cudaStream_t st, F &&f) {
+        if (g.exec) {
+            SDPG_CUDA(cudaGraphLaunch(g.exec, st));
+            g_kernel_launches.fetch_add(g.launches, std::memory_order_relaxed);
+            return;
+        }
+        if (g.calls++ == 0) {
+            f();
+            return;
+        }
+        cudaGraph_t graph = nullptr;
+        const unsigned long long l0 = g_kernel_launches.load();
+        SDPG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        capturing_ = true;
+        try {
+            f();
+        } catch (...) {
+            capturing_ = false;
+            cudaStreamEndCapture(st, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        capturing_ = false;
+        SDPG_CUDA(cudaStreamEndCapture(st, &graph));
+        g.launches = g_kernel_launches.load() - l0;
+        const cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        SDPG_CUDA(e);
+        SDPG_CUDA(cudaGraphLaunch(g.exec, st));
+    }
+    GraphSlot g_schur_chol_, g_schur_inv_;
+    bool capturing_ = false;  // GEMMs issued into a graph are not bracketed by profiling events
+    std::vector<GraphSlot> g_invchol_;  // per block: X (main stream), then Z (second stream)
+
     // ---------------------------------------------------------------- memory helpers
 
     static constexpr int kSlots = 64;
     std::vector<void *> allocs_;
     void *dalloc_raw(size_t bytes) {
         void *p = nullptr;
-        SDPG_CUDA(cudaMalloc(&p, bytes ? bytes : 16));
-        SDPG_CUDA(cudaMemset(p, 0, bytes ? bytes : 16));
+        SDPG_CUDA(cudaMallocAsync(&p, bytes ? bytes : 16, st_));
+        SDPG_CUDA(cudaMemsetAsync(p, 0, bytes ? bytes : 16, st_));
         allocs_.push_back(p);
         return p;
     }
@@ -374,12 +437,16 @@ class Solver final : public SolverBase {
     T *upload_new(const std::vector<T> &h) {
         h2d_ += (long long)(h.size() * sizeof(T));
         T *d = (T *)dalloc_raw(h.size() * sizeof(T));
-        if (!h.empty()) SDPG_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+        if (!h.empty()) {
+            SDPG_CUDA(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st_));
+            SDPG_CUDA(cudaStreamSynchronize(st_));  // h is the caller's
+        }
         return d;
     }
     void upload(V *d, const V *h, size_t count) {
         h2d_ += (long long)(count * sizeof(V));
-        SDPG_CUDA(cudaMemcpy(d, h, count * sizeof(V), cudaMemcpyHostToDevice));
+        SDPG_CUDA(cudaMemcpyAsync(d, h, count * sizeof(V), cudaMemcpyHostToDevice, st_));
+        SDPG_CUDA(cudaStreamSynchronize(st_));
     }
     // read device scalar slots [0, cnt)
     std::vector<R> fetch(int cnt) {
@@ -424,7 +491,7 @@ class Solver final : public SolverBase {
     void gemm(const GemmProblem<N> &p0) { gemm(p0, st_, ws_); }
     void gemm(const GemmProblem<N> &p0, cudaStream_t st, Workspace &ws) {
         GemmProblem<N> p = p0;
-        if (prof_on_) {
+        if (prof_on_ && !capturing_) {
             if (prof_used_ * 2 + 2 > (int)prof_ev_.size()) {
                 if (prof_used_ >= 4096) collect_gemm_events();
                 while (prof_used_ * 2 + 2 > (int)prof_ev_.size()) {
@@ -591,7 +658,7 @@ class Solver final : public SolverBase {
     // Newton::compute_DyVec, sdpa_newton.cpp:1308-1344 (Lal::choleskyFactorWithAdjust + solveSystems)
     bool compute_DyVec(bool corrector) {
         if (!corrector) {
-            ml_potrf<N>(m_, B_, m_, info_, ws_, st_);
+            graphed(g_schur_chol_, st_, [&] { ml_potrf<N>(m_, B_, m_, info_, ws_, st_); });
             int info = 0;
             d2h_ += (long long)sizeof(int);
             SDPG_CUDA(cudaMemcpyAsync(&info, info_, sizeof(int), cudaMemcpyDeviceToHost, st_));
@@ -599,8 +666,10 @@ class Solver final : public SolverBase {
             if (info != 0) return false;
             // L^{-1} once per factorisation (recursive, GEMM based); each solve is then
             // two triangular matrix-vector products, read column-wise for coalescing
-            ml_trtri_lower<N>(m_, B_, m_, BLinv_, ws_, st_);
-            k_transpose<N>(m_, BLinv_, BLinvT_, st_);
+            graphed(g_schur_inv_, st_, [&] {
+                ml_trtri_lower<N>(m_, B_, m_, BLinv_, ws_, st_);
+                k_transpose<N>(m_, BLinv_, BLinvT_, st_);
+            });
         }
         k_matvec<N>(m_, BLinvT_, 'T', 2, g_, Dytmp_, st_);  // L^{-1} g
         k_matvec<N>(m_, BLinv_, 'T', 1, Dytmp_, Dy_, st_);  // L^{-T} L^{-1} g
@@ -805,8 +874,10 @@ class Solver final : public SolverBase {
             if (blk_[l].n <= 20)
                 for (int side = 0; side < 2; ++side) {
                     d2h_ += (long long)sizeof(V);
-                    SDPG_CUDA(cudaMemcpy(&h[2 * l + side], blk_[l].sl[side] + 4, sizeof(V), cudaMemcpyDeviceToHost));
+                    SDPG_CUDA(cudaMemcpyAsync(&h[2 * l + side], blk_[l].sl[side] + 4, sizeof(V),
+                                              cudaMemcpyDeviceToHost, st_));
                 }
+        SDPG_CUDA(cudaStreamSynchronize(st_));
         size_t ti = 0;
         for (size_t l = 0; l < blk_.size(); ++l) {
             for (int side = 0; side < 2; ++side) {
@@ -951,10 +1022,16 @@ class Solver final : public SolverBase {
         const size_t nb = blk_.size();
         SDPG_CUDA(cudaEventRecord(ev_fork_, st_));
         SDPG_CUDA(cudaStreamWaitEvent(st2_, ev_fork_, 0));
+        if (g_invchol_.size() != 2 * nb) g_invchol_.resize(2 * nb);
         for (size_t l = 0; l < nb; ++l)
-            inv_chol_issue(blk_[l], blk_[l].X, blk_[l].F, blk_[l].LX, nullptr, info_all_ + l, st_, ws_);
+            graphed(g_invchol_[l], st_, [&] {
+                inv_chol_issue(blk_[l], blk_[l].X, blk_[l].F, blk_[l].LX, nullptr, info_all_ + l, st_, ws_);
+            });
         for (size_t l = 0; l < nb; ++l)
-            inv_chol_issue(blk_[l], blk_[l].Z, blk_[l].W2, blk_[l].LZ, blk_[l].Zinv, info_all_ + nb + l, st2_, ws2_);
+            graphed(g_invchol_[nb + l], st2_, [&] {
+                inv_chol_issue(blk_[l], blk_[l].Z, blk_[l].W2, blk_[l].LZ, blk_[l].Zinv, info_all_ + nb + l, st2_,
+                               ws2_);
+            });
         SDPG_CUDA(cudaEventRecord(ev_join_, st2_));
         SDPG_CUDA(cudaStreamWaitEvent(st_, ev_join_, 0));
         std::vector<int> info(2 * nb);
@@ -1176,7 +1253,8 @@ class Solver final : public SolverBase {
             int st = 0;
             if (N == 8 && g_gemm_method != 1) {
                 d2h_ += (long long)sizeof(int);
-                SDPG_CUDA(cudaMemcpy(&st, crt_error_word(), sizeof(int), cudaMemcpyDeviceToHost));
+                SDPG_CUDA(cudaMemcpyAsync(&st, crt_error_word(), sizeof(int), cudaMemcpyDeviceToHost, st_));
+                SDPG_CUDA(cudaStreamSynchronize(st_));
                 if (st != 0) throw sdpg_error(SDPG_ERR_TIMEOUT, "tensor-core GEMM: a bounded wait timed out");
             }
         }
@@ -1310,7 +1388,8 @@ class Solver final : public SolverBase {
     void get_y(void *out, int form) const override {
         std::vector<V> h(m_);
         d2h_ += (long long)m_ * (long long)sizeof(V);
-        SDPG_CUDA(cudaMemcpy(h.data(), y_, m_ * sizeof(V), cudaMemcpyDeviceToHost));
+        SDPG_CUDA(cudaMemcpyAsync(h.data(), y_, m_ * sizeof(V), cudaMemcpyDeviceToHost, st_));
+        SDPG_CUDA(cudaStreamSynchronize(st_));
         for (int i = 0; i < m_; ++i) {
             if (form == 0) ((double *)out)[i] = ml_to_double(ml_neg(h[i]));
             else ((V *)out)[i] = ml_neg(h[i]);
@@ -1324,7 +1403,8 @@ class Solver final : public SolverBase {
         if (which < 0 || which > 8) throw sdpg_error(SDPG_ERR_ARG, "bad matrix selector");
         const V *src = srcs[which];
         d2h_ += (long long)(nn * sizeof(V));
-        SDPG_CUDA(cudaMemcpy(h.data(), src, nn * sizeof(V), cudaMemcpyDeviceToHost));
+        SDPG_CUDA(cudaMemcpyAsync(h.data(), src, nn * sizeof(V), cudaMemcpyDeviceToHost, st_));
+        SDPG_CUDA(cudaStreamSynchronize(st_));
         for (size_t i = 0; i < nn; ++i) {
             if (form == 0) ((double *)out)[i] = ml_to_double(h[i]);
             else ((V *)out)[i] = h[i];
@@ -1348,7 +1428,8 @@ class Solver final : public SolverBase {
     void get_vec(int which, void *out) const override {
         const V *srcs[] = {y_, Dy_, b_, p_};
         if (which < 0 || which > 3) throw sdpg_error(SDPG_ERR_ARG, "bad vector selector");
-        SDPG_CUDA(cudaMemcpy(out, srcs[which], m_ * sizeof(V), cudaMemcpyDeviceToHost));
+        SDPG_CUDA(cudaMemcpyAsync(out, srcs[which], m_ * sizeof(V), cudaMemcpyDeviceToHost, st_));
+        SDPG_CUDA(cudaStreamSynchronize(st_));
     }
 
     // ---------------------------------------------------------------- timing
