@@ -6,10 +6,11 @@
 //      R = 276, and is stored as its balanced residues modulo L = 70 primes below 512
 //      (fp16, exact), K contiguous.
 //   3. Tensor cores (tc_gemm.cu): for each prime, S = A_l B_l^T exactly in fp32, then
-//      y_l = (S mod m_l) (M / m_l)^-1 mod m_l.
+//      y_l = S mod m_l.
 //   4. Reconstruction: the exact sum V = sum_k X_ik X_kj satisfies
-//      V / M = sum_l y_l / m_l (mod 1) with |V / M| < 2^-6, so V / M is the centred
-//      fractional part of that sum, formed in 320-bit fixed point; then
+//      V / M = sum_l y_l c_l / m_l (mod 1), c_l = (M / m_l)^-1 mod m_l, with
+//      |V / M| < 2^-6, so V / M is the centred fractional part of that sum, formed in
+//      320-bit fixed point from the table floor(2^320 c_l / m_l); then
 //      C = alpha V 2^(EA_i + EB_j - 2R) + beta C.
 //
 // The only rounding is the truncation of the inputs to R bits (relative 2^-276 of
@@ -30,11 +31,10 @@ __constant__ int c_pow16[kCrtL][kCrtPowChunks];
 __constant__ uint32_t c_inv[kCrtL][kCrtInvWords];
 __constant__ uint32_t c_mtot[8];
 __device__ int d_moduli[kCrtL];
-__device__ int d_cfac[kCrtL];
 __device__ int d_error;
 
 struct CrtDevice {
-    int *moduli = nullptr, *cfac = nullptr, *error = nullptr;
+    int *moduli = nullptr, *error = nullptr;
 };
 
 // Per device: upload the tables once and look up the global-memory copies' addresses.
@@ -52,10 +52,8 @@ CrtDevice crt_device() {
         SDPG_CUDA(cudaMemcpyToSymbol(c_inv, kCrtInv, sizeof(kCrtInv)));
         SDPG_CUDA(cudaMemcpyToSymbol(c_mtot, kCrtMtotMant, sizeof(kCrtMtotMant)));
         SDPG_CUDA(cudaMemcpyToSymbol(d_moduli, kCrtModuli, sizeof(kCrtModuli)));
-        SDPG_CUDA(cudaMemcpyToSymbol(d_cfac, kCrtCfac, sizeof(kCrtCfac)));
         CrtDevice c;
         SDPG_CUDA(cudaGetSymbolAddress((void **)&c.moduli, d_moduli));
-        SDPG_CUDA(cudaGetSymbolAddress((void **)&c.cfac, d_cfac));
         SDPG_CUDA(cudaGetSymbolAddress((void **)&c.error, d_error));
         cache[dev] = c;
         ready[dev] = true;
@@ -163,7 +161,7 @@ __global__ void __launch_bounds__(256) crt_residue_kernel(CrtOperands<N> ops, in
     }
 }
 
-// V / M as the centred fractional part of sum_l y_l / m_l (320-bit fixed point), then
+// V / M as the centred fractional part of sum_l y_l c_l / m_l (320-bit fixed point), then
 // C = alpha V 2^(EA + EB - 2R) + beta C.  Each thread takes two neighbouring outputs
 // along j and reads both residues of a plane with one 32-bit load.
 template <int N>
@@ -365,7 +363,6 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
             t.kpitch = L.Kpad;
             t.lower_only = p.lower_only;
             t.moduli = dev.moduli;
-            t.cfac = dev.cfac;
             t.error = dev.error;
             if (p.ev_before) SDPG_CUDA(cudaEventRecord(p.ev_before, s));
             // K beyond the tensor memory's four exact accumulators runs in chunks whose

@@ -1,7 +1,8 @@
 // tcgen05 modular GEMM: TMA loads of 128 x 64 fp16 tiles (128-byte swizzle) into a
 // three-stage shared-memory ring, one thread issuing tcgen05.mma (M = N = 128,
 // K = 16) into fp32 accumulators in tensor memory, and a four-warp epilogue that
-// reads the accumulators with tcgen05.ld and reduces them modulo the tile's prime.
+// reads the accumulators with tcgen05.ld and reduces them modulo the tile's prime
+// (the CRT factor is folded into the reconstruction's table instead).
 //
 // Every wait on an mbarrier is bounded by a cycle budget; on time-out the kernel
 // records an error, lets the copies and products it issued finish (again with a
@@ -124,23 +125,7 @@ __device__ __forceinline__ uint64_t sw128_kmajor_desc(uint32_t saddr) {
 constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(kTcBN >> 3) << 17) |
                             ((uint32_t)(kTcBM >> 4) << 24);
 
-__device__ __forceinline__ int mod_of_float(float S, int m, float inv_m) {
-    // S is an integer-valued float, |S| < 2^24: S - m floor(S/m), corrected by one step
-    const float q = floorf(S * inv_m);
-    int r = (int)fmaf(-q, (float)m, S);
-    if (r < 0) r += m;
-    if (r >= m) r -= m;
-    return r;
-}
 
-__device__ __forceinline__ int mulmod(int a, int b, int m, float inv_m) {
-    const int p = a * b;  // < 2^18
-    int q = (int)((float)p * inv_m);
-    int r = p - q * m;
-    if (r < 0) r += m;
-    if (r >= m) r -= m;
-    return r;
-}
 
 __global__ void __launch_bounds__(128, 1)
     tc_modgemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcModGemm p) {
@@ -243,12 +228,14 @@ __global__ void __launch_bounds__(128, 1)
     tc_fence_after();
 
     if (!abort_flag) {
-        const int m = p.moduli[l], c = p.cfac[l];
+        const int m = p.moduli[l];
         const float inv_m = 1.0f / (float)m;
         const int row = warp * 32 + lane;
         uint16_t *yrow = p.Y + ((size_t)z * p.Mpad + m0 + row) * p.Npad + n0;
 #pragma unroll 1
         for (int cb = 0; cb < kTcBN / 32; ++cb) {
+            // the accumulators hold exact integers below 2^24: sum them as integers, then
+            // reduce once (|x| < 2^26, so the float quotient is off by at most one)
             int r[32];
 #pragma unroll
             for (int q = 0; q < 32; ++q) r[q] = 0;
@@ -258,9 +245,8 @@ __global__ void __launch_bounds__(128, 1)
                 tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * kTcBN + cb * 32), v);
                 tmem_ld_wait();
 #pragma unroll
-                for (int q = 0; q < 32; ++q) r[q] += mod_of_float(__uint_as_float(v[q]), m, inv_m);
+                for (int q = 0; q < 32; ++q) r[q] += __float2int_rn(__uint_as_float(v[q]));
             }
-            uint32_t packed[16];
             uint4 *dst = reinterpret_cast<uint4 *>(yrow + cb * 32);
             uint32_t prev[16];
             if (p.accumulate) {
@@ -273,24 +259,23 @@ __global__ void __launch_bounds__(128, 1)
                     prev[4 * q + 3] = v.w;
                 }
             }
+            uint32_t packed[16];
 #pragma unroll
             for (int q = 0; q < 32; q += 2) {
-                // r < nacc m <= 4m: reduce with at most three subtractions
-                int y0 = r[q], y1 = r[q + 1];
+                int y[2];
 #pragma unroll
-                for (int t = 0; t < 3; ++t) {
-                    y0 -= (y0 >= m) ? m : 0;
-                    y1 -= (y1 >= m) ? m : 0;
+                for (int u = 0; u < 2; ++u) {
+                    const int x = r[q + u];
+                    int t = x - (int)floorf((float)x * inv_m) * m;
+                    t += (t < 0) ? m : 0;
+                    t -= (t >= m) ? m : 0;
+                    if (p.accumulate) {  // an earlier K chunk of the same product: add mod m
+                        t += (int)((prev[q / 2] >> (16 * u)) & 0xFFFFu);
+                        t -= (t >= m) ? m : 0;
+                    }
+                    y[u] = t;
                 }
-                y0 = mulmod(y0, c, m, inv_m);
-                y1 = mulmod(y1, c, m, inv_m);
-                if (p.accumulate) {  // an earlier K chunk of the same product: add mod m
-                    y0 += (int)(prev[q / 2] & 0xFFFFu);
-                    y1 += (int)(prev[q / 2] >> 16);
-                    y0 -= (y0 >= m) ? m : 0;
-                    y1 -= (y1 >= m) ? m : 0;
-                }
-                packed[q / 2] = (uint32_t)y0 | ((uint32_t)y1 << 16);
+                packed[q / 2] = (uint32_t)y[0] | ((uint32_t)y[1] << 16);
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q)

@@ -7,8 +7,7 @@
 // tensor memory.  Every partial sum is an integer of magnitude at most
 // 256 * 255^2 < 2^24 when at most 256 products are summed, so the fp32 accumulation
 // is exact; longer K is split over up to four accumulators of 256 each.  The
-// epilogue reduces S mod m_l and multiplies by the CRT factor c_l, writing
-// y_l = (S mod m_l) c_l mod m_l.
+// epilogue writes y_l = S mod m_l (the CRT factor lives in the reconstruction table).
 #pragma once
 #include <cuda_fp16.h>
 
@@ -25,7 +24,7 @@ constexpr int kTcMaxK = 1024;   // four accumulators of 128 columns fill tensor 
 struct TcModGemm {
     const __half *A;  // planes [zA][Mpad][Kpad], K contiguous
     const __half *B;  // planes [zB][Npad][Kpad], K contiguous
-    uint16_t *Y;      // planes [z][Mpad][Npad]
+    uint16_t *Y;      // planes [z][Mpad][Npad]: S mod m_l
     int L;            // moduli
     int batch;        // z = b * L + l; A plane (bA * L + l) with bA = b if a_batched else 0
     int a_batched, b_batched;
@@ -35,7 +34,6 @@ struct TcModGemm {
     int accumulate;        // 1: Y = (Y + new) mod m (a later K chunk of the same product)
     int lower_only;        // 1: skip tiles strictly above the diagonal (their Y is not written)
     const int *moduli;     // device, L entries
-    const int *cfac;       // device, L entries
     int *error;            // device word: set non-zero if a bounded wait timed out
 };
 

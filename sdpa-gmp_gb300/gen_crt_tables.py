@@ -5,7 +5,9 @@ K <= 1024), |V| < 2^562; the moduli are the largest primes below 512 whose produ
 M exceeds 2^568, so V / M lies well inside (-1/2, 1/2).  Per modulus m:
   cfac  = (M / m)^-1 mod m                  (CRT factor applied in the GEMM epilogue)
   pow16 = 2^(16 c) mod m, c = 0 .. 17        (residue of a 288-bit integer from 16-bit chunks)
-  inv   = floor(2^320 / m) as ten 32-bit words (V / M = sum_l y_l / m_l mod 1)
+  inv   = floor(2^320 cfac / m) as ten 32-bit words: with r_l = V mod m_l,
+          V / M = sum_l r_l cfac_l / m_l (mod 1), so the tensor-core epilogue stores r_l
+          and the CRT factor is folded into this table
 and M itself as a 256-bit mantissa with its exponent.
 
 Run: python sdpa-gmp_gb300/gen_crt_tables.py  (writes the header beside the sources)
@@ -33,7 +35,7 @@ def main():
     L = len(moduli)
     cfac = [pow(prod // m, -1, m) for m in moduli]
     pow16 = [[pow(2, 16 * c, m) for c in range(18)] for m in moduli]
-    inv = [(1 << 320) // m for m in moduli]
+    inv = [(c << 320) // m for c, m in zip(cfac, moduli)]
     inv_words = [[(v >> (32 * w)) & 0xFFFFFFFF for w in range(10)] for v in inv]
     bl = prod.bit_length()
     mant = prod >> (bl - 256)  # top 256 bits (truncated)
@@ -45,7 +47,7 @@ def main():
     out.append("namespace sdpg {")
     out.append(f"constexpr int kCrtL = {L};              // moduli")
     out.append("constexpr int kCrtR = 276;             // bits of the integer operands")
-    out.append("constexpr int kCrtInvWords = 10;       // 2^320 / m as 32-bit words")
+    out.append("constexpr int kCrtInvWords = 10;       // 2^320 cfac / m as 32-bit words")
     out.append("constexpr int kCrtPowChunks = 18;      // 16-bit chunks of a 288-bit integer")
     out.append(f"constexpr int kCrtMtotExp = {bl};       // M = 0.mant * 2^kCrtMtotExp")
     out.append("static const int kCrtModuli[kCrtL] = {" + ", ".join(map(str, moduli)) + "};")
