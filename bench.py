@@ -403,6 +403,29 @@ def bench_batch(args) -> None:
     print(json.dumps(line))
 
 
+def bench_learned(args) -> None:
+    """Learned mode (cfg5 family): the committed lambdaStar / beta policy against the
+    default parameters on held-out MaxCut instances (n = 124, p ~ U[0.02, 0.2], edge
+    weights +-1); prints mean iterations of both and the largest objective difference
+    from the default solve, which judges the learned path's error."""
+    learned = importlib.import_module("sdpa-gmp_gb300.learned")
+    sdpg = importlib.import_module("sdpa-gmp_gb300")
+    pol = sdpg.Policy.load(learned.POLICY_FILE)
+    seeds = range(learned.HOLDOUT_BASE, learned.HOLDOUT_BASE + args.batch)
+    t0 = time.perf_counter()
+    ev = learned.evaluate(pol, seeds, workers=args.concurrency)
+    secs = time.perf_counter() - t0
+    line = {"metric": "mean IPM iterations to pdOPT, learned lambdaStar/beta vs default (MaxCut n=124, +-1)",
+            "value": ev["mean_iterations_learned"], "unit": "iterations", "n_gpus": 1, "higher_is_better": False,
+            "config": {"workload": f"{args.batch} held-out seeds from {learned.HOLDOUT_BASE}",
+                       "precision_bits": learned.PRECISION, "policy": os.path.basename(learned.POLICY_FILE)},
+            "default_iterations": ev["mean_iterations_default"], "iteration_reduction": ev["iteration_reduction"],
+            "fallback_solves": ev["fallback_solves"], "beta_fallback_rate": ev["beta_fallback_rate"],
+            "mean_lambda_star": ev["mean_lambda"], "max_objective_rel_error": ev["max_objective_rel_error"],
+            "seconds": secs, "data": "synthetic (seeded generator)"}
+    print(json.dumps(line))
+
+
 def bench_gemm(args) -> None:
     """Kernel mode: repeated n x n x n multi-limb GEMMs through sdpg_rgemm_device
     (the profiling target of the digit-GEMM kernel); prints GMAC/s."""
@@ -460,8 +483,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the digit-GEMM (plain path) comparison")
-    ap.add_argument("--workload", choices=["ipm", "batch"], default="ipm",
-                    help="batch: many small control/LMI solves at once (solves/s) instead of IPM iterations")
+    ap.add_argument("--workload", choices=["ipm", "batch", "learned"], default="ipm",
+                    help="batch: many small control/LMI solves at once (solves/s); learned: the committed "
+                         "lambdaStar/beta policy against the defaults (mean iterations) on --batch held-out seeds")
     ap.add_argument("--batch", type=int, default=64, help="batch mode: instances")
     ap.add_argument("--concurrency", type=int, default=16, help="batch mode: solvers in flight")
     ap.add_argument("--serial", type=int, default=8, help="batch mode: instances timed one at a time")
@@ -472,6 +496,8 @@ def main():
         bench_gemm(args)
     elif args.workload == "batch" and args.impl != "reference":
         bench_batch(args)
+    elif args.workload == "learned" and args.impl != "reference":
+        bench_learned(args)
     elif args.impl == "reference":
         bench_reference(args)
     else:

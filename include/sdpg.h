@@ -225,8 +225,6 @@ int sdpg_tensor_error(int device, int *flag);
 /* Measured throughput of signed 32x32->64 multiply-adds (IMAD.WIDE) on one GPU, the
  * instruction the multi-limb GEMM is built from; the plain path's roofline denominator. */
 int sdpg_probe_imad_wide(int device, double *ops_per_second);
-/* Read data + param, solve, write the result file: `sdpa_gmp -ds data -o out -p param`
- * (main / pinpal, sdpa_main.cpp:43-461, 501-677).  Returns iterations; info12 as above. */
 /* Batched solves (no reference counterpart; the reference solves one problem per
  * process): `count` problems with one parameter set (NULL: defaults), up to
  * `concurrency` solvers in flight at once, one host thread and its own CUDA streams
@@ -236,8 +234,55 @@ int sdpg_probe_imad_wide(int device, double *ops_per_second);
  * number of problems solved without error. */
 int sdpg_solve_batch(int count, sdpg_problem *const *problems, const sdpg_param *param, int device, int concurrency,
                      double *info12, int *iterations);
+/* Read data + param, solve, write the result file: `sdpa_gmp -ds data -o out -p param`
+ * (main / pinpal, sdpa_main.cpp:43-461, 501-677).  Returns iterations; info12 as above. */
 int sdpg_solve_file(const char *data_path, const char *param_path, const char *out_path, int device,
                     double *info12);
+
+/* ---- learned parameter proposal (no reference counterpart) ------------------
+ * A fully connected FP32 network (6 inputs, three hidden layers of 64 tanh units,
+ * 2 outputs) run and trained by the library's own CUDA kernels.  Inputs per sample:
+ *   log10 mu, log10 max-norm primal residual, log10 max-norm dual residual,
+ *   previous primal step length, previous dual step length,
+ *   the corrector centering value of the reference's rule (DirectionParameter::
+ *   MehrotraCorrector, sdpa_parts.cpp:555-586) at this iteration;
+ * outputs: log10 lambdaStar (used at the initial point, Solutions::initialize,
+ * sdpa_dataset.cpp:35-60) and the corrector's beta.  Parameters are a flat float array
+ * (W1[64][6] b1 W2[64][64] b2 W3[64][64] b3 W4[2][64] b4, row-major [out][in]); the
+ * scaling block holds x_mean[6] x_std[6] y_mean[2] y_std[2]: the network sees
+ * (x - x_mean) / x_std and its output z is reported as y_mean + y_std z. */
+#define SDPG_POLICY_INPUTS 6
+#define SDPG_POLICY_OUTPUTS 2
+#define SDPG_POLICY_PARAMS 8898
+#define SDPG_POLICY_SCALE 16
+typedef struct sdpg_policy sdpg_policy;
+/* Glorot-uniform weights from a fixed seed, zero biases, identity scaling. */
+int sdpg_policy_create(int device, sdpg_policy **out);
+void sdpg_policy_destroy(sdpg_policy *p);
+/* Either pointer may be NULL (left unchanged); resets the optimiser state. */
+int sdpg_policy_set(sdpg_policy *p, const float *params, const float *scale);
+int sdpg_policy_get(sdpg_policy *p, float *params, float *scale);
+/* y[count][2] = network(x[count][6]) (host buffers). */
+int sdpg_policy_forward(sdpg_policy *p, const float *x, int count, float *y);
+/* Loss sum_i,o mask[i][o] (z[i][o] - (t[i][o] - y_mean[o]) / y_std[o])^2 / count in
+ * standardised units, and its gradient with respect to every parameter. */
+int sdpg_policy_gradient(sdpg_policy *p, const float *x, const float *t, const float *mask, int count, float *grad,
+                         float *loss);
+/* Adam (lr, 0.9, 0.999, 1e-8) on that loss over shuffled mini-batches of `batch`
+ * samples for `epochs` passes; epoch_loss[e] (may be NULL) = mean batch loss of pass e. */
+int sdpg_policy_train(sdpg_policy *p, const float *x, const float *t, const float *mask, int count, int epochs,
+                      int batch, float lr, unsigned long long seed, float *epoch_loss);
+/* Attach (NULL detaches) a policy to a solver on the same device.  flags: 1 propose the
+ * corrector beta each iteration, 2 propose lambdaStar at initialize().  A proposed beta
+ * whose step fails the checks (the predicted mu must fall by a factor 1 - min(alphaP,
+ * alphaD) / 4 or more; a residual that is not yet zero needs a step length of at least
+ * 0.5) is replaced by the reference's own value for that iteration.  The policy must outlive its use and not be trained meanwhile. */
+int sdpg_solver_set_policy(sdpg_solver *h, sdpg_policy *p, int flags);
+/* [proposals, fallbacks, lambdaStar in use, lambdaStar proposed (0 if none)]. */
+int sdpg_solver_policy_stats(sdpg_solver *h, double *out4);
+/* Per-iteration policy inputs recorded by the solver (with or without a policy): up to
+ * cap rows of 6 floats, one per row of sdpg_solver_history.  Returns the row count. */
+int sdpg_solver_features(sdpg_solver *h, float *out, int cap);
 
 #ifdef __cplusplus
 }

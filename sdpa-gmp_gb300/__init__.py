@@ -114,6 +114,16 @@ def _setup(lib: ctypes.CDLL) -> ctypes.CDLL:
         "sdpg_tensor_error": (i, [i, c.POINTER(i)]),
         "sdpg_probe_imad_wide": (i, [i, c.POINTER(c.c_double)]),
         "sdpg_solve_file": (i, [c.c_char_p, c.c_char_p, c.c_char_p, i, c.POINTER(c.c_double)]),
+        "sdpg_policy_create": (i, [i, c.POINTER(vp)]),
+        "sdpg_policy_destroy": (None, [vp]),
+        "sdpg_policy_set": (i, [vp, vp, vp]),
+        "sdpg_policy_get": (i, [vp, vp, vp]),
+        "sdpg_policy_forward": (i, [vp, vp, i, vp]),
+        "sdpg_policy_gradient": (i, [vp, vp, vp, vp, i, vp, vp]),
+        "sdpg_policy_train": (i, [vp, vp, vp, vp, i, i, i, c.c_float, c.c_ulonglong, vp]),
+        "sdpg_solver_set_policy": (i, [vp, vp, i]),
+        "sdpg_solver_policy_stats": (i, [vp, c.POINTER(c.c_double)]),
+        "sdpg_solver_features": (i, [vp, vp, i]),
     }
     for name, (res, args) in sig.items():
         if hasattr(lib, name):
@@ -448,6 +458,103 @@ class Solver:
         a, b = ctypes.c_longlong(), ctypes.c_longlong()
         check(lib().sdpg_solver_io_bytes(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def set_policy(self, policy: "Policy | None", beta: bool = True, lam: bool = True) -> None:
+        """Attach a learned proposal (the policy must outlive the solver's use of it)."""
+        self._policy = policy  # keep it alive
+        flags = (1 if beta else 0) | (2 if lam else 0)
+        check(lib().sdpg_solver_set_policy(self.h, policy.h if policy else None, flags if policy else 0))
+
+    def policy_stats(self) -> dict:
+        out = (ctypes.c_double * 4)()
+        check(lib().sdpg_solver_policy_stats(self.h, out))
+        return {"proposals": int(out[0]), "fallbacks": int(out[1]), "lambda_star": out[2],
+                "lambda_proposed": out[3]}
+
+    def features(self) -> np.ndarray:
+        """Policy inputs: row 0 at the initial point, row k + 1 at iteration k."""
+        n = check(lib().sdpg_solver_features(self.h, None, 0))
+        out = np.zeros((max(n, 1), POLICY_INPUTS), dtype=np.float32)
+        check(lib().sdpg_solver_features(self.h, out.ctypes.data, n))
+        return out[:n]
+
+
+POLICY_INPUTS = 6
+POLICY_OUTPUTS = 2
+POLICY_PARAMS = 8898
+POLICY_SCALE = 16
+
+
+class Policy:
+    """The learned lambdaStar / beta proposal: a 6-64-64-64-2 tanh network in FP32 whose
+    forward, backward and Adam steps run as the library's CUDA kernels."""
+
+    def __init__(self, device: int = 0):
+        h = ctypes.c_void_p()
+        check(lib().sdpg_policy_create(device, ctypes.byref(h)))
+        self.h = h.value
+        self.device = device
+
+    def close(self) -> None:
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.sdpg_policy_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def get(self) -> tuple[np.ndarray, np.ndarray]:
+        w = np.zeros(POLICY_PARAMS, dtype=np.float32)
+        sc = np.zeros(POLICY_SCALE, dtype=np.float32)
+        check(lib().sdpg_policy_get(self.h, w.ctypes.data, sc.ctypes.data))
+        return w, sc
+
+    def set(self, params: np.ndarray | None = None, scale: np.ndarray | None = None) -> None:
+        w = None if params is None else np.ascontiguousarray(params, dtype=np.float32)
+        sc = None if scale is None else np.ascontiguousarray(scale, dtype=np.float32)
+        if w is not None and w.size != POLICY_PARAMS:
+            raise ValueError(f"expected {POLICY_PARAMS} parameters")
+        if sc is not None and sc.size != POLICY_SCALE:
+            raise ValueError(f"expected {POLICY_SCALE} scaling values")
+        check(lib().sdpg_policy_set(self.h, None if w is None else w.ctypes.data,
+                                    None if sc is None else sc.ctypes.data))
+
+    def forward(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, POLICY_INPUTS)
+        y = np.zeros((x.shape[0], POLICY_OUTPUTS), dtype=np.float32)
+        check(lib().sdpg_policy_forward(self.h, x.ctypes.data, x.shape[0], y.ctypes.data))
+        return y
+
+    def gradient(self, x: np.ndarray, t: np.ndarray, mask: np.ndarray) -> tuple[np.ndarray, float]:
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, POLICY_INPUTS)
+        t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, POLICY_OUTPUTS)
+        mask = np.ascontiguousarray(mask, dtype=np.float32).reshape(-1, POLICY_OUTPUTS)
+        g = np.zeros(POLICY_PARAMS, dtype=np.float32)
+        loss = ctypes.c_float()
+        check(lib().sdpg_policy_gradient(self.h, x.ctypes.data, t.ctypes.data, mask.ctypes.data, x.shape[0],
+                                         g.ctypes.data, ctypes.byref(loss)))
+        return g, loss.value
+
+    def train(self, x: np.ndarray, t: np.ndarray, mask: np.ndarray, epochs: int, batch: int = 256,
+              lr: float = 1e-3, seed: int = 0) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, POLICY_INPUTS)
+        t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, POLICY_OUTPUTS)
+        mask = np.ascontiguousarray(mask, dtype=np.float32).reshape(-1, POLICY_OUTPUTS)
+        losses = np.zeros(max(epochs, 1), dtype=np.float32)
+        check(lib().sdpg_policy_train(self.h, x.ctypes.data, t.ctypes.data, mask.ctypes.data, x.shape[0], epochs,
+                                      batch, lr, seed, losses.ctypes.data))
+        return losses[:epochs]
+
+    def save(self, path: str) -> None:
+        w, sc = self.get()
+        np.savez(path, params=w, scale=sc)
+
+    @classmethod
+    def load(cls, path: str, device: int = 0) -> "Policy":
+        d = np.load(path)
+        p = cls(device)
+        p.set(d["params"], d["scale"])
+        return p
 
 
 def set_gemm_method(method: int) -> int:

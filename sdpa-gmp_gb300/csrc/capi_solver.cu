@@ -430,6 +430,33 @@ int sdpg_solver_reset_counters(sdpg_solver *h) {
     });
 }
 
+int sdpg_solver_set_policy(sdpg_solver *h, sdpg_policy *p, int flags) {
+    return sdpg_guard([&] {
+        if (flags < 0 || flags > 3) throw sdpg_error(SDPG_ERR_ARG, "policy flags are 0..3");
+        S(h).set_policy(p ? &p->p : nullptr, flags);
+        return SDPG_OK;
+    });
+}
+
+int sdpg_solver_policy_stats(sdpg_solver *h, double *out4) {
+    return sdpg_guard([&] {
+        if (!out4) throw sdpg_error(SDPG_ERR_ARG, "null output");
+        S(h).policy_stats(out4);
+        return SDPG_OK;
+    });
+}
+
+int sdpg_solver_features(sdpg_solver *h, float *out, int cap) {
+    return sdpg_guard([&] {
+        const auto &f = S(h).features();
+        const int rows = (int)f.size();
+        if (out)
+            for (int r = 0; r < std::min(rows, cap); ++r)
+                for (int i = 0; i < kPolIn; ++i) out[(size_t)r * kPolIn + i] = f[r][i];
+        return rows;
+    });
+}
+
 int sdpg_solve_file(const char *data_path, const char *param_path, const char *out_path, int device, double *info12) {
     return sdpg_guard([&] {
         Param q;

@@ -55,7 +55,8 @@ class Solver final : public SolverBase {
     };
 
   public:
-    Solver(const RawProblem &P, const Param &par, int device, cudaStream_t stream) : par_(par), st_(stream) {
+    Solver(const RawProblem &P, const Param &par, int device, cudaStream_t stream)
+        : par_(par), lambda_default_(par.lambdaStar), dev_(device), st_(stream) {
         SDPG_CUDA(cudaSetDevice(device));
         if (!st_) throw sdpg_error(SDPG_ERR_ARG, "the solver needs a stream");
         keep_pool_memory(device);
@@ -120,6 +121,57 @@ class Solver final : public SolverBase {
         *d2h = d2h_;
     }
     void sync() override { SDPG_CUDA(cudaStreamSynchronize(st_)); }
+
+    // ---------------------------------------------------------------- learned proposal
+
+    void set_policy(const Policy *p, int flags) override {
+        if (p && p->device != dev_) throw sdpg_error(SDPG_ERR_ARG, "the policy lives on another device");
+        if (p && !pol_dev_) pol_dev_ = (float *)dalloc_raw(16 * sizeof(float));
+        policy_ = p;
+        pol_flags_ = p ? flags : 0;
+    }
+    void policy_stats(double *o) const override {
+        o[0] = (double)pol_props_;
+        o[1] = (double)pol_fallbacks_;
+        o[2] = par_.lambdaStar;
+        o[3] = pol_lambda_prop_;
+    }
+    const std::vector<std::array<float, kPolIn>> &features() const override { return feats_; }
+
+    // log10 mu, log10 primal / dual residual max-norms, previous step lengths, the rule's beta
+    std::array<float, kPolIn> policy_features(const R &beta_rule) const {
+        auto lg = [](const R &v) {
+            const double d = fabs(v.d());
+            return (float)log10(d > 1e-40 ? d : 1e-40);
+        };
+        return {lg(muCur_), lg(normP_), lg(normD_), (float)lastAP_.d(), (float)lastAD_.d(), (float)beta_rule.d()};
+    }
+    void policy_eval(const std::array<float, kPolIn> &f, float y[kPolOut]) {
+        float *h = reinterpret_cast<float *>(pinned_ + kPinned - 4);  // 4 spare slots at the end
+        for (int i = 0; i < kPolIn; ++i) h[i] = f[i];
+        h2d_ += kPolIn * (long long)sizeof(float);
+        d2h_ += kPolOut * (long long)sizeof(float);
+        SDPG_CUDA(cudaMemcpyAsync(pol_dev_, h, kPolIn * sizeof(float), cudaMemcpyHostToDevice, st_));
+        policy_forward_device(*policy_, pol_dev_, 1, pol_dev_ + 8, st_);
+        SDPG_CUDA(cudaMemcpyAsync(h + 8, pol_dev_ + 8, kPolOut * sizeof(float), cudaMemcpyDeviceToHost, st_));
+        SDPG_CUDA(cudaStreamSynchronize(st_));
+        for (int o = 0; o < kPolOut; ++o) y[o] = h[8 + o];
+    }
+    // the checks a proposed corrector must pass: the predicted mu falls by at least a
+    // quarter of the shorter step, and a residual that is not yet zero is reduced by a
+    // step of at least one half
+    bool proposal_ok() {
+        const R xMatvMat = ip_blocks(&Blk::X, &Blk::Dz);
+        const R uMatzMat = ip_blocks(&Blk::Dx, &Blk::Z);
+        const R uMatvMat = ip_blocks(&Blk::Dx, &Blk::Dz);
+        const R muNew = muCur_ + (aP_ * uMatzMat + aD_ * xMatvMat + aP_ * aD_ * uMatvMat) / R(nDim_);
+        if (!(muNew <= (R(1.0) - R(0.25) * rmin(aP_, aD_)) * muCur_)) return false;
+        const bool primal_open = phase_ == noINFO || phase_ == dFEAS;
+        const bool dual_open = phase_ == noINFO || phase_ == pFEAS;
+        if (primal_open && aP_ < R(0.5)) return false;
+        if (dual_open && aD_ < R(0.5)) return false;
+        return true;
+    }
 
     // ---------------------------------------------------------------- setup
 
@@ -563,8 +615,8 @@ class Solver final : public SolverBase {
     }
 
     // Newton::Make_gVec, sdpa_newton.cpp:840-895
-    void Make_gVec(bool corrector) {
-        compute_rMat(corrector);
+    void Make_gVec(bool corrector, bool keep_rmat = false) {
+        if (!keep_rmat) compute_rMat(corrector);
         if (phase_ == pFEAS || phase_ == noINFO) {
             if (!corrector) {
                 for (auto &B : blk_) {
@@ -693,6 +745,16 @@ class Solver final : public SolverBase {
         for (auto &B : blk_) k_symmetrize<N>(B.n, B.Dx, st_);
     }
 
+    // The corrector again with beta + delta: R Z^-1 is affine in beta (compute_rMat), so
+    // it is shifted by delta mu Z^-1 and the rest of the direction recomputed from it.
+    void newton_rebeta(const R &delta) {
+        axpby_blocks(&Blk::Rm, R(1), &Blk::Rm, delta * muCur_, &Blk::Zinv);
+        Make_gVec(true, true);
+        compute_DyVec(true);
+        compute_DzMat();
+        compute_DxMat();
+    }
+
     // Newton::Mehrotra, sdpa_newton.cpp:1375-1414
     bool newton(int corrector) override {
         ev_start();
@@ -778,7 +840,7 @@ class Solver final : public SolverBase {
 
     // all Lanczos runs advance in lockstep: one host synchronisation per step for all of them
     void lanczos_all(std::vector<Lz> &T) {
-        if (8 * T.size() > (size_t)kPinned) throw sdpg_error(SDPG_ERR_TOO_LARGE, "too many Lanczos runs at once");
+        if (8 * T.size() > (size_t)kPinned - 4) throw sdpg_error(SDPG_ERR_TOO_LARGE, "too many Lanczos runs at once");
         for (size_t i = 0; i < T.size(); ++i) {
             Lz &t = T[i];
             Blk &B = *t.B;
@@ -1160,8 +1222,28 @@ class Solver final : public SolverBase {
                    ((primal * dual + omega * (primal * (R(1.0) - dual) + (R(1.0) - primal) * dual)) * x0z0 + xMatzMat);
     }
 
-    // Solutions::initialize (sdpa_dataset.cpp:35-60) and the set-up part of pinpal (sdpa_main.cpp:229-287)
+    // Solutions::initialize (sdpa_dataset.cpp:35-60) and the set-up part of pinpal
+    // (sdpa_main.cpp:229-287); with a policy attached (flag 2) the point is set up once at
+    // param.sdpa's lambdaStar, the policy reads it and proposes the lambdaStar used instead
     void initialize() override {
+        par_.lambdaStar = lambda_default_;
+        pol_lambda_prop_ = 0;
+        pol_props_ = pol_fallbacks_ = 0;
+        init_point();
+        lastAP_ = lastAD_ = R(0.0);
+        feats_.clear();
+        feats_.push_back(policy_features(betaV_));
+        if (policy_ && (pol_flags_ & 2)) {
+            float y[kPolOut];
+            policy_eval(feats_[0], y);
+            const double e = std::min(6.0, std::max(-3.0, (double)y[0]));
+            pol_lambda_prop_ = pow(10.0, e);
+            par_.lambdaStar = pol_lambda_prop_;
+            init_point();
+        }
+    }
+
+    void init_point() {
         const R lambda(par_.lambdaStar);
         const R invsq = R(1.0) / rsqrt_(lambda);
         const R inv = R(1.0) / lambda;
@@ -1245,9 +1327,28 @@ class Solver final : public SolverBase {
         if (!newton(0)) return stop();
         step_length(0);
         direction_corrector();
-        if (phase_ == pdFEAS && (betaV_ > R(5) || objP_ < objD_)) return stop();
+        const R beta_rule = betaV_;
+        const std::array<float, kPolIn> feat = policy_features(beta_rule);
+        bool proposed = false;
+        if (policy_ && (pol_flags_ & 1)) {
+            float y[kPolOut];
+            policy_eval(feat, y);
+            betaV_ = R(std::min(1.0, std::max(0.01, (double)y[1])));
+            proposed = true;
+        }
+        if (phase_ == pdFEAS && (beta_rule > R(5) || objP_ < objD_)) return stop();
         newton(1);
         step_length(1);
+        if (proposed) {
+            ++pol_props_;
+            if (!proposal_ok()) {  // the fallback: the reference's own beta for this iteration
+                ++pol_fallbacks_;
+                const R delta = beta_rule - betaV_;
+                betaV_ = beta_rule;
+                newton_rebeta(delta);
+                step_length(1);
+            }
+        }
         {
             // the tensor-core GEMMs' bounded waits (step_length has synchronised the streams)
             int st = 0;
@@ -1259,6 +1360,9 @@ class Solver final : public SolverBase {
             }
         }
         record_iteration();
+        feats_.push_back(feat);
+        lastAP_ = aP_;
+        lastAD_ = aD_;
         print_iteration(out);
         trace_line();
         if (!update()) {
@@ -1445,6 +1549,8 @@ class Solver final : public SolverBase {
 
   private:
     Param par_;
+    double lambda_default_;  // param.sdpa's lambdaStar (a proposal replaces par_'s copy)
+    int dev_;
     cudaStream_t st_;
     Workspace ws_, ws2_;  // ws2_ serves work issued on the second stream
 
@@ -1475,6 +1581,14 @@ class Solver final : public SolverBase {
     double prof_ms_ = 0;
     long long prof_launches_ = 0, prof_macs_ = 0;
     mutable long long h2d_ = 0, d2h_ = 0;
+    // learned proposal
+    const Policy *policy_ = nullptr;
+    int pol_flags_ = 0;
+    float *pol_dev_ = nullptr;  // device: inputs at 0, outputs at 8
+    long long pol_props_ = 0, pol_fallbacks_ = 0;
+    double pol_lambda_prop_ = 0;
+    R lastAP_, lastAD_;
+    std::vector<std::array<float, kPolIn>> feats_;
 };
 
 }  // namespace

@@ -3,10 +3,12 @@
 #pragma once
 #include <stdio.h>
 
+#include <array>
 #include <string>
 #include <vector>
 
 #include "kernels.cuh"
+#include "mlp.cuh"
 #include "problem.h"
 #include "real.h"
 
@@ -77,6 +79,12 @@ class SolverBase {
     // bytes copied host->device and device->host since construction (setup included)
     virtual void io_bytes(long long *h2d, long long *d2h) const = 0;
     virtual void sync() = 0;
+    // learned proposal (flags: 1 corrector beta, 2 lambdaStar); null detaches
+    virtual void set_policy(const Policy *p, int flags) = 0;
+    // [proposals, fallbacks, lambdaStar in use, lambdaStar proposed or 0]
+    virtual void policy_stats(double *out4) const = 0;
+    // policy inputs: row 0 at the initial point, row k + 1 at iteration k
+    virtual const std::vector<std::array<float, kPolIn>> &features() const = 0;
 };
 
 // Build a solver for the SDP blocks of P at the precision in `param`.
