@@ -66,6 +66,10 @@ int sdpg_ml_elem_bytes(int limbs);
  * sdpa_io.cpp:138-142, and prints them with gmp_fprintf, sdpa_io.cpp:1086-1162). */
 int sdpg_ml_parse(int limbs, const char *text, void *out);
 int sdpg_ml_format(int limbs, const void *v, int digits, char *buf, int cap);
+/* One value through a GMP printf format for an mpf operand, as gmp_fprintf renders the
+ * result file's xPrint / XPrint / YPrint (e.g. "%+50.40Fe"; conversions e E f g G, flags
+ * "-+ 0#", rounded half up like mpf_get_str).  Returns the length written. */
+int sdpg_ml_format_gmp(int limbs, const void *v, const char *fmt, char *buf, int cap);
 int sdpg_ml_from_double(int limbs, const double *x, long long n, void *out);
 int sdpg_ml_to_double(int limbs, const void *v, long long n, double *out);
 int sdpg_ml_from_mpf(int limbs, const sdpg_mpf_t *src, long long n, void *out);
@@ -238,6 +242,12 @@ int sdpg_solve_batch(int count, sdpg_problem *const *problems, const sdpg_param 
  * (main / pinpal, sdpa_main.cpp:43-461, 501-677).  Returns iterations; info12 as above. */
 int sdpg_solve_file(const char *data_path, const char *param_path, const char *out_path, int device,
                     double *info12);
+/* The same with, if print_to_stdout, the iteration table and summary also on stdout:
+ * what the command-line driver sdpa_gmp_gb300 calls.  param (may be NULL) gives the
+ * parameters directly and param_path is then only echoed in the header; with param NULL
+ * a param_path is read as a param.sdpa file, and without either the defaults apply. */
+int sdpg_solve_file_ex(const char *data_path, const sdpg_param *param, const char *param_path, const char *out_path,
+                       int device, int print_to_stdout, double *info12);
 
 /* ---- learned parameter proposal (no reference counterpart) ------------------
  * A fully connected FP32 network (6 inputs, three hidden layers of 64 tanh units,

@@ -61,6 +61,7 @@ def _setup(lib: ctypes.CDLL) -> ctypes.CDLL:
         "sdpg_ml_elem_bytes": (i, [i]),
         "sdpg_ml_parse": (i, [i, c.c_char_p, vp]),
         "sdpg_ml_format": (i, [i, vp, i, c.c_char_p, i]),
+        "sdpg_ml_format_gmp": (i, [i, vp, c.c_char_p, c.c_char_p, i]),
         "sdpg_ml_from_double": (i, [i, vp, ll, vp]),
         "sdpg_ml_to_double": (i, [i, vp, ll, vp]),
         "sdpg_ml_from_mpf": (i, [i, vp, ll, vp]),
@@ -190,6 +191,18 @@ def ml_format(a: np.ndarray, digits: int = 17) -> list[str]:
         check(lib().sdpg_ml_format(limbs, a[k].ctypes.data, digits, buf, len(buf)))
         res.append(buf.value.decode())
     return res
+
+
+def ml_format_gmp(a: np.ndarray, fmt: str) -> list[str]:
+    """Each value through a GMP printf format such as "%+50.40Fe" (the result file's)."""
+    limbs = a.shape[1] - 2
+    a = np.ascontiguousarray(a)
+    buf = ctypes.create_string_buffer(4096)
+    out = []
+    for row in a:
+        check(lib().sdpg_ml_format_gmp(limbs, row.ctypes.data, fmt.encode(), buf, len(buf)))
+        out.append(buf.value.decode())
+    return out
 
 
 def ml_host_op(op: int, a: np.ndarray, b: np.ndarray | None = None) -> np.ndarray:

@@ -46,9 +46,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     headers = sorted(glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
                      + glob.glob(os.path.join(ROOT, "include", "*.h")))
+    cli = sorted(glob.glob(os.path.join(PKG, "cli", "*.cpp")))
     flags = " ".join(ARCH + CFLAGS)
     stamp = os.path.join(BUILD, "libsdpg.stamp")
-    digest = _digest(sources + headers, flags + os.uname().machine)
+    digest = _digest(sources + headers + cli, flags + os.uname().machine)
     if not force and os.path.exists(LIB) and os.path.exists(stamp):
         with open(stamp) as f:
             if f.read().strip() == digest:
@@ -79,9 +80,24 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     with open(stamp, "w") as f:
         f.write(digest)
     return LIB
+
+
+def build_cli() -> str:
+    """The command-line driver ``sdpa_gmp_gb300`` beside the library (rpath $ORIGIN)."""
+    src = os.path.join(PKG, "cli", "sdpa_gmp_gb300.cpp")
+    exe = os.path.join(PKG, "sdpa_gmp_gb300")
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), src, "-o", exe + ".tmp",
+           "-L" + PKG, "-lsdpg", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(exe + ".tmp", exe)
+    return exe
 
 
 if __name__ == "__main__":

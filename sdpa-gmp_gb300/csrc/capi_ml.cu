@@ -63,6 +63,21 @@ int sdpg_ml_format(int limbs, const void *v, int digits, char *buf, int cap) {
     });
 }
 
+int sdpg_ml_format_gmp(int limbs, const void *v, const char *fmt, char *buf, int cap) {
+    return sdpg_guard([&] {
+        if (!v || !fmt || !buf) throw sdpg_error(SDPG_ERR_ARG, "null argument");
+        return dispatch_limbs(limbs, [&](auto tag) {
+            constexpr int N = decltype(tag)::value;
+            mlf<N> x;
+            memcpy(&x, v, sizeof x);
+            const std::string s = ml_format_gmp<N>(fmt, x);
+            if ((int)s.size() + 1 > cap) throw sdpg_error(SDPG_ERR_ARG, "buffer too small");
+            memcpy(buf, s.c_str(), s.size() + 1);
+            return (int)s.size();
+        });
+    });
+}
+
 int sdpg_ml_from_double(int limbs, const double *x, long long n, void *out) {
     return sdpg_guard([&] {
         return dispatch_limbs(limbs, [&](auto tag) {

@@ -3,6 +3,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
+#include <ctime>
 #include <atomic>
 #include <memory>
 #include <thread>
@@ -93,6 +95,54 @@ sdpg_solver *wrap(const RawProblem &P, const Param &q, int device, void *stream)
 SolverBase &S(sdpg_solver *h) {
     if (!h || !h->s) throw sdpg_error(SDPG_ERR_ARG, "null solver handle");
     return *h->s;
+}
+
+// The reference driver's file output around the solve (main, sdpa_main.cpp:43-461):
+// start line, the data file's title/comment lines (IO::read, sdpa_io.cpp:123-134), the
+// file names, "DENSE computation" (Newton::initialize, sdpa_newton.cpp:349-350), the
+// iteration table and summary, then parameters, time table, solution and final times.
+int solve_file_impl(const char *data_path, const Param &q, const char *param_path, const char *out_path, int device,
+                    FILE *display, double *info12) {
+    if (!data_path) throw sdpg_error(SDPG_ERR_ARG, "no data file");
+    const auto t0 = std::chrono::steady_clock::now();
+    std::string err;
+    RawProblem P;
+    if (!read_sdpa(data_path, false, P, &err)) throw sdpg_error(SDPG_ERR_IO, err);
+    const double read_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::unique_ptr<sdpg_solver> h(wrap(P, q, device, nullptr));
+    FILE *out = nullptr;
+    if (out_path && out_path[0]) {
+        out = fopen(out_path, "w");
+        if (!out) throw sdpg_error(SDPG_ERR_IO, std::string("cannot open out file ") + out_path);
+    }
+    int it;
+    try {
+        if (out) {
+            const time_t now = time(nullptr);
+            fprintf(out, "SDPA-GMP start at %s", ctime(&now));
+            fputs(P.title.c_str(), out);
+            fprintf(out, "data      is %s\n", data_path);
+            if (param_path && param_path[0]) fprintf(out, "parameter is %s\n", param_path);
+            fprintf(out, "out       is %s\n", out_path);
+            fprintf(out, "DENSE computation\n");
+        }
+        if (display) fprintf(display, "DENSE computations\n");
+        it = h->s->run(out, display);
+        if (out) {
+            h->s->print_result_tail(out, read_s);
+            const double loop = h->s->timers().total / 1000.0;
+            fprintf(out, "    main loop time = %.6f\n", loop);
+            fprintf(out, "        total time = %.6f\n",
+                    std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+            fprintf(out, "  file   read time = %.6f\n", read_s);
+        }
+    } catch (...) {
+        if (out) fclose(out);
+        throw;
+    }
+    if (out) fclose(out);
+    if (info12) h->s->info(info12);
+    return it;
 }
 
 }  // namespace
@@ -462,24 +512,19 @@ int sdpg_solve_file(const char *data_path, const char *param_path, const char *o
         Param q;
         std::string err;
         if (param_path && param_path[0] && !param_read(q, param_path, &err)) throw sdpg_error(SDPG_ERR_IO, err);
-        RawProblem P;
-        if (!read_sdpa(data_path, false, P, &err)) throw sdpg_error(SDPG_ERR_IO, err);
-        std::unique_ptr<sdpg_solver> h(wrap(P, q, device, nullptr));
-        FILE *out = nullptr;
-        if (out_path && out_path[0]) {
-            out = fopen(out_path, "w");
-            if (!out) throw sdpg_error(SDPG_ERR_IO, std::string("cannot open out file ") + out_path);
-        }
-        int it;
-        try {
-            it = h->s->run(out, nullptr);
-        } catch (...) {
-            if (out) fclose(out);
-            throw;
-        }
-        if (out) fclose(out);
-        if (info12) h->s->info(info12);
-        return it;
+        return solve_file_impl(data_path, q, param_path, out_path, device, nullptr, info12);
+    });
+}
+
+int sdpg_solve_file_ex(const char *data_path, const sdpg_param *param, const char *param_path, const char *out_path,
+                       int device, int print_to_stdout, double *info12) {
+    return sdpg_guard([&] {
+        Param q = to_param(param);
+        std::string err;
+        if (!param && param_path && param_path[0] && !param_read(q, param_path, &err))
+            throw sdpg_error(SDPG_ERR_IO, err);
+        return solve_file_impl(data_path, q, param_path, out_path, device, print_to_stdout ? stdout : nullptr,
+                               info12);
     });
 }
 

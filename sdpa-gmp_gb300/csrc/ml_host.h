@@ -219,7 +219,30 @@ inline void ml_decimal_digits(const mlf<N> &a, int ndig, std::string *digits, lo
     *e10 = E;
 }
 
-// printf-like "%[+]W.Pe" rendering of an mlf (digits truncated, not rounded).
+// ndig significant digits of |a| rounded half up, as GMP's mpf_get_str rounds (one
+// further digit decides; that digit is exact because the digits are truncated).
+template <int N>
+inline void ml_decimal_rounded(const mlf<N> &a, int ndig, std::string *digits, long *e10) {
+    std::string d;
+    long e = 0;
+    ml_decimal_digits(a, ndig + 1, &d, &e);
+    const bool up = d[ndig] >= '5';
+    d.resize(ndig);
+    if (up) {
+        int i = ndig - 1;
+        while (i >= 0 && d[i] == '9') d[i--] = '0';
+        if (i >= 0) {
+            ++d[i];
+        } else {  // 99..9 rounded up to 100..0
+            d = "1" + std::string(ndig - 1, '0');
+            ++e;
+        }
+    }
+    *digits = d;
+    *e10 = e;
+}
+
+// printf-like "%[+]W.Pe" rendering of an mlf, rounded half up in the last digit.
 template <int N>
 inline std::string ml_format_e(const mlf<N> &a, int prec, bool plus = false, int width = 0) {
     std::string out;
@@ -228,7 +251,7 @@ inline std::string ml_format_e(const mlf<N> &a, int prec, bool plus = false, int
     } else {
         std::string dg;
         long e10;
-        ml_decimal_digits(a, prec + 1, &dg, &e10);
+        ml_decimal_rounded(a, prec + 1, &dg, &e10);
         out = a.s ? "-" : (plus ? "+" : "");
         out += dg.substr(0, 1);
         if (prec > 0) out += "." + dg.substr(1);
@@ -238,6 +261,120 @@ inline std::string ml_format_e(const mlf<N> &a, int prec, bool plus = false, int
     }
     if ((int)out.size() < width) out = std::string(width - out.size(), ' ') + out;
     return out;
+}
+
+// One value rendered through a GMP-style printf format for mpf operands, as the
+// reference's result file does (gmp_fprintf with xPrint / XPrint / YPrint, e.g.
+// "%+50.40Fe"): text around a single conversion "%[flags][width][.prec][F](e|E|f|g|G)"
+// with flags from "-+ 0#", rounded half up in the last printed digit.
+template <int N>
+inline std::string ml_format_gmp(const std::string &fmt, const mlf<N> &a) {
+    const size_t pc = fmt.find('%');
+    if (pc == std::string::npos) return fmt;
+    size_t i = pc + 1;
+    bool left = false, plus = false, space = false, zero = false, alt = false;
+    for (; i < fmt.size(); ++i) {
+        const char c = fmt[i];
+        if (c == '-') left = true;
+        else if (c == '+') plus = true;
+        else if (c == ' ') space = true;
+        else if (c == '0') zero = true;
+        else if (c == '#') alt = true;
+        else break;
+    }
+    int width = 0, prec = 6;
+    while (i < fmt.size() && fmt[i] >= '0' && fmt[i] <= '9') width = 10 * width + (fmt[i++] - '0');
+    if (i < fmt.size() && fmt[i] == '.') {
+        prec = 0;
+        ++i;
+        while (i < fmt.size() && fmt[i] >= '0' && fmt[i] <= '9') prec = 10 * prec + (fmt[i++] - '0');
+    }
+    if (i < fmt.size() && fmt[i] == 'F') ++i;
+    if (i >= fmt.size()) return fmt;
+    const char conv = fmt[i];
+    const std::string tail = fmt.substr(i + 1);
+    const bool neg = !ml_is_zero(a) && a.s;
+    std::string body;  // digits without sign
+    auto exp_form = [&](int p, bool upper) {
+        std::string dg;
+        long e10 = 0;
+        if (ml_is_zero(a)) {
+            dg = std::string(p + 1, '0');
+        } else {
+            ml_decimal_rounded(a, p + 1, &dg, &e10);
+        }
+        std::string r = dg.substr(0, 1);
+        if (p > 0 || alt) r += ".";
+        r += dg.substr(1);
+        char eb[32];
+        snprintf(eb, sizeof eb, "%c%c%02ld", upper ? 'E' : 'e', e10 < 0 ? '-' : '+', e10 < 0 ? -e10 : e10);
+        return r + eb;
+    };
+    auto fixed_form = [&](int p) {
+        if (ml_is_zero(a)) return std::string("0") + (p > 0 || alt ? "." + std::string(p, '0') : "");
+        std::string dg;
+        long e10 = 0;
+        ml_decimal_digits(a, 1, &dg, &e10);
+        long nd = e10 + 1 + p;  // significant digits printed
+        std::string intpart, frac;
+        if (nd == 0) {  // below the last printed place: rounds to 0 or to one unit there
+            const bool up = dg[0] >= '5';
+            intpart = p == 0 && up ? "1" : "0";
+            frac = std::string(p, '0');
+            if (p > 0 && up) frac[p - 1] = '1';
+        } else if (nd < 0) {
+            intpart = "0";
+            frac = std::string(p, '0');
+        } else {
+            ml_decimal_rounded(a, (int)nd, &dg, &e10);
+            if ((long)dg.size() < e10 + 1 + p) dg += std::string(e10 + 1 + p - (long)dg.size(), '0');
+            const long ni = e10 + 1;  // integer digits (may be <= 0)
+            if (ni > 0) {
+                intpart = dg.substr(0, ni);
+                frac = dg.substr(ni);
+            } else {
+                intpart = "0";
+                frac = std::string(-ni, '0') + dg;
+            }
+            frac.resize(p, '0');
+        }
+        return intpart + (p > 0 || alt ? "." + frac : "");
+    };
+    switch (conv) {
+        case 'e':
+        case 'E': body = exp_form(prec, conv == 'E'); break;
+        case 'f': body = fixed_form(prec); break;
+        case 'g':
+        case 'G': {
+            const int P = prec == 0 ? 1 : prec;
+            long e10 = 0;
+            if (!ml_is_zero(a)) {
+                std::string dg;
+                ml_decimal_rounded(a, P, &dg, &e10);
+            }
+            if (e10 < -4 || e10 >= P) body = exp_form(P - 1, conv == 'G');
+            else body = fixed_form((int)(P - 1 - e10));
+            if (!alt) {  // strip trailing zeros of the fraction
+                const size_t epos = body.find_first_of("eE");
+                std::string mant = body.substr(0, epos), ex = epos == std::string::npos ? "" : body.substr(epos);
+                if (mant.find('.') != std::string::npos) {
+                    while (!mant.empty() && mant.back() == '0') mant.pop_back();
+                    if (!mant.empty() && mant.back() == '.') mant.pop_back();
+                }
+                body = mant + ex;
+            }
+            break;
+        }
+        default: return fmt;  // not a floating conversion: left as is
+    }
+    const std::string sign = neg ? "-" : (plus ? "+" : (space ? " " : ""));
+    std::string out;
+    const int pad = width - (int)(sign.size() + body.size());
+    if (pad <= 0) out = sign + body;
+    else if (left) out = sign + body + std::string(pad, ' ');
+    else if (zero) out = sign + std::string(pad, '0') + body;
+    else out = std::string(pad, ' ') + sign + body;
+    return fmt.substr(0, pc) + out + tail;
 }
 
 // GMP mpf public layout (gmp.h: __mpf_struct {int _mp_prec; int _mp_size;

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <chrono>
 #include <map>
+#include <utility>
 
 #include "solver.cuh"
 
@@ -1459,6 +1460,114 @@ class Solver final : public SolverBase {
         fprintf(f, "relative eps = %s\n", R(ml_ldexp(ml_one<N>(), -32 * N)).fmt(16).c_str());
         fprintf(f, "total time   = %.3f\n", tm_.total / 1000.0);
         fflush(f);
+    }
+
+    // The rest of IO::printLastInfo's file output (sdpa_io.cpp:1152-1173): the parameter
+    // block (Parameter::display, sdpa_parts.cpp:227-255), the time table
+    // (ComputeTime::display, sdpa_parts.cpp:72-122) and the solution with the
+    // REVERSE_PRIMAL_DUAL naming: xVec = -y, xMat = Z, yMat = X, each through its format.
+    void print_result_tail(FILE *f, double file_read_s) override {
+        if (!f) return;
+        fprintf(f, "\n\nParameters are\n");
+        fprintf(f, "** Parameters **\n");
+        fprintf(f, "maxIteration =    %d\n", par_.maxIteration);
+        fprintf(f, "epsilonStar  = %8.3e\n", par_.epsilonStar);
+        fprintf(f, "lambdaStar   = %8.3e\n", par_.lambdaStar);
+        fprintf(f, "omegaStar    = %8.3e\n", par_.omegaStar);
+        fprintf(f, "lowerBound   = %8.3e\n", par_.lowerBound);
+        fprintf(f, "upperBound   = %8.3e\n", par_.upperBound);
+        fprintf(f, "betaStar     = %8.3e\n", par_.betaStar);
+        fprintf(f, "betaBar      = %8.3e\n", par_.betaBar);
+        fprintf(f, "gammaStar    = %8.3e\n", par_.gammaStar);
+        fprintf(f, "epsilonDash  = %8.3e\n", par_.epsilonDash);
+        fprintf(f, "precision    =    %d\n", par_.precision);
+        fprintf(f, "xPrint       = %s \n", par_.xPrint.c_str());
+        fprintf(f, "XPrint       = %s \n", par_.XPrint.c_str());
+        fprintf(f, "YPrint       = %s \n", par_.YPrint.c_str());
+        fprintf(f, "infPrint     = %s \n", par_.infPrint.c_str());
+        // time table: this solver's phase timers under the reference's row names; rows it
+        // does not time separately print zero
+        const double loop = tm_.total / 1000.0;
+        const double bmat = tm_.schur / 1000.0;
+        const std::pair<const char *, double> rows[] = {
+            {" Predictor time  ", 0.0},           {" Corrector time  ", 0.0},
+            {" Make bMat time  ", bmat},          {" Make bDia time  ", 0.0},
+            {" Make bF1  time  ", 0.0},           {" Make bF2  time  ", 0.0},
+            {" Make bF3  time  ", 0.0},           {" Make bPRE time  ", 0.0},
+            {" Make rMat time  ", 0.0},           {" Make gVec Mul   ", 0.0},
+            {" Make gVec time  ", tm_.rmat_gvec / 1000.0},
+            {" Cholesky bMat   ", tm_.cholesky / 1000.0},
+            {" Ste Pre time    ", 0.0},           {" Ste Cor time    ", tm_.steplen / 1000.0},
+            {" solve           ", 0.0},           {" sumDz           ", 0.0},
+            {" makedX          ", 0.0},           {" symmetriseDx    ", 0.0},
+            {" makedXdZ        ", tm_.dxdz / 1000.0},
+            {" xMatTime        ", 0.0},           {" zMatTime        ", 0.0},
+            {" invzMatTime     ", 0.0},           {" xMatzMatTime    ", tm_.update / 1000.0},
+            {" EigxMatTime     ", 0.0},           {" EigzMatTime     ", 0.0},
+            {" EigxMatzMatTime ", 0.0},           {" updateRes       ", tm_.residual / 1000.0},
+            {" EigTime         ", 0.0},           {" sub_total_bMat  ", loop - bmat},
+            {" Main Loop       ", loop},          {" File Check      ", 0.0},
+            {" File Change     ", 0.0},           {" File Read       ", file_read_s},
+            {" Total           ", loop + file_read_s}};
+        fprintf(f, "\n");
+        fprintf(f, "                         Time(sec) ");
+        fprintf(f, " Ratio(%% : MainLoop) \n");
+        for (const auto &r : rows) fprintf(f, "%s=       %f,  %f\n", r.first, r.second, r.second / loop * 100.0);
+        fprintf(f, "\n");
+        // solution
+        fprintf(f, "xVec = \n");
+        {
+            std::vector<V> h(m_);
+            d2h_ += (long long)m_ * (long long)sizeof(V);
+            SDPG_CUDA(cudaMemcpyAsync(h.data(), y_, m_ * sizeof(V), cudaMemcpyDeviceToHost, st_));
+            SDPG_CUDA(cudaStreamSynchronize(st_));
+            if (par_.xPrint == "NOPRINT") {
+                fprintf(f, "NOPRINT\n");
+            } else {
+                fprintf(f, "{");
+                for (int i = 0; i < m_; ++i) {
+                    fputs(ml_format_gmp<N>(par_.xPrint, ml_neg(h[i])).c_str(), f);
+                    fputs(i + 1 < m_ ? "," : "}\n", f);
+                }
+                if (m_ == 0) fprintf(f, "  }\n");
+            }
+        }
+        fprintf(f, "xMat = \n");
+        print_blocks(f, &Blk::Z, par_.XPrint);
+        fprintf(f, "yMat = \n");
+        print_blocks(f, &Blk::X, par_.YPrint);
+    }
+    // IO::displayDenseLinarSpaceLast (sdpa_io.cpp:1186-1220) with DenseMatrix::display
+    // (sdpa_struct.cpp:706-746) for every block, column-major entries
+    void print_blocks(FILE *f, V *Blk::*M, const std::string &fmt) const {
+        if (fmt == "NOPRINT") {
+            fprintf(f, "NOPRINT\n");
+            return;
+        }
+        fprintf(f, "{\n");
+        for (const Blk &B : blk_) {
+            const int n = B.n;
+            std::vector<V> h((size_t)n * n);
+            d2h_ += (long long)h.size() * (long long)sizeof(V);
+            SDPG_CUDA(cudaMemcpyAsync(h.data(), B.*M, h.size() * sizeof(V), cudaMemcpyDeviceToHost, st_));
+            SDPG_CUDA(cudaStreamSynchronize(st_));
+            auto at = [&](int i, int j) { return ml_format_gmp<N>(fmt, h[i + (size_t)n * j]); };
+            fprintf(f, "{");
+            for (int i = 0; i + 1 < n; ++i) {
+                fputs(i == 0 ? " {" : "  {", f);
+                for (int j = 0; j < n; ++j) {
+                    fputs(at(i, j).c_str(), f);
+                    fputs(j + 1 < n ? "," : " },\n", f);
+                }
+            }
+            if (n > 1) fputs("  {", f);
+            for (int j = 0; j < n; ++j) {
+                fputs(at(n - 1, j).c_str(), f);
+                fputs(j + 1 < n ? "," : " }", f);
+            }
+            fputs(n > 1 ? "   }\n" : "\n", f);
+        }
+        fprintf(f, "}\n");
     }
 
     // info: [phase, iteration, objValPrimal, objValDual, mu, relgap, p.feas.error, d.feas.error,

@@ -79,6 +79,28 @@ def parse_result(text: str) -> dict:
     xv = re.search(r"xVec = \n\{(.*?)\}\n", text, re.S)
     if xv:
         out["xVec"] = [s.strip() for s in xv.group(1).split(",")]
+    for key, nxt in (("xMat", "yMat = "), ("yMat", "    main loop time")):
+        mt = re.search(key + r" = \n(.*?)\n" + re.escape(nxt), text, re.S)
+        if mt:
+            out[key] = NUM_RE.findall(mt.group(1))
+    out["layout"] = result_layout(text)
+    return out
+
+
+NUM_RE = re.compile(r"[+-]?(?:\d+\.?\d*(?:[eE][+-]?\d+)?|nan|inf)")
+
+
+def result_layout(text: str) -> list[str]:
+    """The result file's lines with every number replaced by '#' and the start time and
+    file names masked: what must agree between two solvers' result files."""
+    out = []
+    for ln in text.splitlines():
+        if ln.startswith("SDPA-GMP start at"):
+            ln = "SDPA-GMP start at <time>"
+        for tag in ("data      is ", "parameter is ", "out       is "):
+            if ln.startswith(tag):
+                ln = tag + "<path>"
+        out.append(NUM_RE.sub("#", ln))
     return out
 
 

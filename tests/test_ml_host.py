@@ -54,7 +54,7 @@ def test_parse_format_roundtrip(sdpg, exact):
         got = exact.to_fraction(d)
         assert abs(got - ref) <= abs(ref) / (1 << 250)
     s = sdpg.ml_format(sdpg.ml_parse(["3.14159265358979323846264338327950288"], 8), 30)[0]
-    assert s.startswith("3.14159265358979323846264338327")
+    assert s.startswith("3.14159265358979323846264338328")  # 30 digits, rounded half up
     assert sdpg.ml_to_double(sdpg.ml_from_double([1.5, -2.0**-300, 0.0], 8)).tolist() == [1.5, -2.0**-300, 0.0]
 
 
@@ -64,3 +64,42 @@ def test_precision_mapping(sdpg):
     assert sdpg.limbs_for_precision(512) == 16
     with pytest.raises(sdpg.SdpgError):
         sdpg.limbs_for_precision(1024)
+
+
+def _py_format(x: Fraction, spec: str) -> str:
+    """C printf semantics of one conversion with half-up rounding, via decimal
+    (Python writes at least one exponent digit where C writes two: widened here)."""
+    import decimal
+    import re
+    m = re.fullmatch(r"([<+]*)(\d*)\.(\d+)([eEf])", spec)
+    flags, width, prec, conv = m.group(1), int(m.group(2) or 0), m.group(3), m.group(4)
+    with decimal.localcontext() as ctx:
+        ctx.prec = 400
+        ctx.rounding = decimal.ROUND_HALF_UP
+        d = decimal.Decimal(x.numerator) / decimal.Decimal(x.denominator)
+        body = format(d, ("+" if "+" in flags else "") + "." + prec + conv)
+    body = re.sub(r"([eE])([+-])(\d)$", r"\g<1>\g<2>0\g<3>", body)
+    return body.ljust(width) if "<" in flags else body.rjust(width)
+
+
+@pytest.mark.parametrize("limbs", [8, 16])
+def test_gmp_printf_formats(sdpg, exact, limbs):
+    """sdpg_ml_format_gmp against Python's decimal formatting (exact value, half-up
+    rounding) for the conversions the result file uses and a few others."""
+    rng = random.Random(77 + limbs)
+    vals = exact.random_ml(60, limbs, rng, -200, 200)
+    vals[0] = 0
+    extra = sdpg.ml_parse(["5.9", "-1.375", "0.00449999", "9.9999999", "-0.5", "123456789.125", "1e-31"], limbs)
+    vals = np.concatenate([vals, extra])
+    fr = [exact.to_fraction(v) for v in exact.ml_decode(vals)]
+    for fmt, spec in [("%+50.40Fe", "+50.40e"), ("%+8.3Fe", "+8.3e"), ("%10.16Fe", "10.16e"), ("%4.16Fe", "4.16e"),
+                      ("%.6Fe", ".6e"), ("%-20.5FE", "<20.5E"), ("%.3Ff", ".3f"), ("%+12.0Ff", "+12.0f")]:
+        got = sdpg.ml_format_gmp(vals, fmt)
+        for g, x in zip(got, fr):
+            if spec.endswith("f") and abs(x) > 10 ** 30:
+                continue  # fixed notation of huge values: not used by result files
+            # zero through C's own printf (Python's % operator on a float)
+            want = (fmt.replace("F", "") % 0.0) if x == 0 else _py_format(x, spec)
+            assert g == want, (fmt, g, want)
+    # text around the conversion is copied
+    assert sdpg.ml_format_gmp(extra[:1], "x=%+.2Fe;")[0] == "x=+5.90e+00;"
