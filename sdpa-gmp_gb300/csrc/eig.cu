@@ -416,6 +416,50 @@ void k_tridiag_min(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *st
     SDPG_CHECK_LAUNCH();
 }
 
+// The LP rule of Jal::getMinEigen (sdpa_jordan.cpp:79-85): min over k of
+// X[k][k] * L[k][k] * L[k][k] for a diagonal block (L its inverse Cholesky factor),
+// one CTA; out[0] = the minimum, out[1] = 0 (no Lanczos error term).
+template <int N>
+__global__ void lp_ratio_min_kernel(int n, const mlf<N> *X, const mlf<N> *L, mlf<N> *out) {
+    __shared__ mlf<N> part[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    mlf<N> best = ml_zero<N>();
+    bool have = false;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const size_t kk = (size_t)k + (size_t)n * k;
+        const mlf<N> v = ml_mul(ml_mul(X[kk], L[kk]), L[kk]);
+        if (!have || ml_cmp(v, best) < 0) best = v;
+        have = true;
+    }
+    // lanes without an entry carry +1e50, the reference's starting minimum
+    if (!have) best = ml_from_double<N>(1.0e50);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const mlf<N> o = ml_shfl_xor(best, off);
+        if (ml_cmp(o, best) < 0) best = o;
+    }
+    if (lane == 0) part[warp] = best;
+    __syncthreads();
+    if (warp == 0) {
+        best = lane < (int)(blockDim.x >> 5) ? part[lane] : ml_from_double<N>(1.0e50);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const mlf<N> o = ml_shfl_xor(best, off);
+            if (ml_cmp(o, best) < 0) best = o;
+        }
+        if (lane == 0) {
+            out[0] = best;
+            out[1] = ml_zero<N>();
+        }
+    }
+}
+
+template <int N>
+void k_lp_ratio_min(int n, const mlf<N> *X, const mlf<N> *L, mlf<N> *out, cudaStream_t s) {
+    lp_ratio_min_kernel<N><<<1, 256, 0, s>>>(n, X, L, out);
+    SDPG_CHECK_LAUNCH();
+}
+
 template <int N>
 void k_tridiagonalize_small(int n, mlf<N> *A, mlf<N> *d, mlf<N> *e, cudaStream_t s) {
     if (n > 64) throw sdpg_error(SDPG_ERR_TOO_LARGE, "small tridiagonalisation limited to n <= 64");
@@ -429,7 +473,8 @@ void k_tridiagonalize_small(int n, mlf<N> *A, mlf<N> *d, mlf<N> *e, cudaStream_t
                                       const mlf<N> *, mlf<N> *, cudaStream_t);                            \
     template void k_lanczos_next<N>(int, const mlf<N> *, const mlf<N> *, mlf<N> *, mlf<N> *, cudaStream_t); \
     template void k_tridiag_min<N>(int, const mlf<N> *, const mlf<N> *, mlf<N> *, int *, cudaStream_t);  \
-    template void k_tridiagonalize_small<N>(int, mlf<N> *, mlf<N> *, mlf<N> *, cudaStream_t);
+    template void k_tridiagonalize_small<N>(int, mlf<N> *, mlf<N> *, mlf<N> *, cudaStream_t);              \
+    template void k_lp_ratio_min<N>(int, const mlf<N> *, const mlf<N> *, mlf<N> *, cudaStream_t);
 SDPG_INST_EIG(8)
 SDPG_INST_EIG(16)
 

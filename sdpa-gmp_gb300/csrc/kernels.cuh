@@ -139,5 +139,8 @@ void k_tridiag_min(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *st
 // d[0..n-1], e[0..n-2].  (Rsytrd 'L', the first stage of Rsyev.)
 template <int N>
 void k_tridiagonalize_small(int n, mlf<N> *A, mlf<N> *d, mlf<N> *e, cudaStream_t s);
+// LP blocks (held as diagonal n x n blocks): out[0] = min_k X[k][k] L[k][k]^2, out[1] = 0.
+template <int N>
+void k_lp_ratio_min(int n, const mlf<N> *X, const mlf<N> *L, mlf<N> *out, cudaStream_t s);
 
 }  // namespace sdpg

@@ -53,6 +53,11 @@ class Solver final : public SolverBase {
         int *f1_owners = nullptr;
         int nF1 = 0;
         int lanczos_kmax = 0;
+        // An LP block of the file (negative size, or size 1), held as a diagonal n x n
+        // block: the same iterates, Schur entries and residuals as the reference's LP
+        // arithmetic, since every product of diagonal matrices stays exactly diagonal;
+        // its step length uses the LP rule instead of Lanczos.
+        bool lp = false;
     };
 
   public:
@@ -182,13 +187,12 @@ class Solver final : public SolverBase {
         std::vector<int> sdp_of_file(P.blockStruct.size(), -1);
         for (size_t l = 0; l < P.blockStruct.size(); ++l) {
             const int bs = P.blockStruct[l];
-            if (bs >= 2) {
-                sdp_of_file[l] = (int)blk_.size();
-                blk_.emplace_back();
-                blk_.back().n = bs;
-            } else {
-                throw sdpg_error(SDPG_ERR_ARG, "LP (diagonal) blocks are not supported by this solver build");
-            }
+            if (bs == 0) throw sdpg_error(SDPG_ERR_ARG, "block size 0");
+            // main, sdpa_main.cpp:113-129: size >= 2 is an SDP block, negative or 1 an LP block
+            sdp_of_file[l] = (int)blk_.size();
+            blk_.emplace_back();
+            blk_.back().n = bs < 0 ? -bs : bs;
+            blk_.back().lp = bs < 2;
         }
         nDim_ = 0;
         for (auto &b : blk_) nDim_ += b.n;
@@ -363,7 +367,9 @@ class Solver final : public SolverBase {
                 B.te[side] = dalloc(std::max(B.lanczos_kmax, n) + 2);
                 B.sl[side] = dalloc(8);
             }
-            if (n <= 20) {
+            if (B.lp) {
+                // no eigenvalue work space: the LP rule reads the diagonals
+            } else if (n <= 20) {
                 B.SW1 = dalloc(nn);
                 B.SW2 = dalloc(nn);
             } else {
@@ -912,7 +918,9 @@ class Solver final : public SolverBase {
                 V *Xm = side == 0 ? B.Dx : B.Dz;
                 cudaStream_t st = side == 0 ? st_ : st2_;
                 Workspace &ws = side == 0 ? ws_ : ws2_;
-                if (B.n > 20) {
+                if (B.lp) {
+                    k_lp_ratio_min<N>(B.n, Xm, L, B.sl[side] + 4, st);
+                } else if (B.n > 20) {
                     Lz t{};
                     t.B = &B;
                     t.side = side;
@@ -934,7 +942,7 @@ class Solver final : public SolverBase {
         // small-block results
         std::vector<V> h(2 * blk_.size());
         for (size_t l = 0; l < blk_.size(); ++l)
-            if (blk_[l].n <= 20)
+            if (blk_[l].n <= 20 || blk_[l].lp)
                 for (int side = 0; side < 2; ++side) {
                     d2h_ += (long long)sizeof(V);
                     SDPG_CUDA(cudaMemcpyAsync(&h[2 * l + side], blk_[l].sl[side] + 4, sizeof(V),
@@ -945,7 +953,7 @@ class Solver final : public SolverBase {
         for (size_t l = 0; l < blk_.size(); ++l) {
             for (int side = 0; side < 2; ++side) {
                 R v;
-                if (blk_[l].n > 20) {
+                if (blk_[l].n > 20 && !blk_[l].lp) {
                     const Lz &t = T[ti++];
                     v = t.min - rabs(t.error * t.beta);
                 } else {
@@ -1552,6 +1560,14 @@ class Solver final : public SolverBase {
             SDPG_CUDA(cudaMemcpyAsync(h.data(), B.*M, h.size() * sizeof(V), cudaMemcpyDeviceToHost, st_));
             SDPG_CUDA(cudaStreamSynchronize(st_));
             auto at = [&](int i, int j) { return ml_format_gmp<N>(fmt, h[i + (size_t)n * j]); };
+            if (B.lp) {  // an LP block prints its diagonal as one braced row
+                fprintf(f, "{");
+                for (int k = 0; k < n; ++k) {
+                    fputs(at(k, k).c_str(), f);
+                    fputs(k + 1 < n ? "," : "}\n", f);
+                }
+                continue;
+            }
             fprintf(f, "{");
             for (int i = 0; i + 1 < n; ++i) {
                 fputs(i == 0 ? " {" : "  {", f);

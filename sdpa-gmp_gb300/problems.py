@@ -184,8 +184,24 @@ def control(m: int = 231, blocks: tuple[int, ...] = (40, 20), seed: int = 0) -> 
     ``min C.X s.t. A_i.X = b_i``.  Written as SDPA data: ``F0 = -C``.
     All sums are exactly rounded, so the file is byte-identical everywhere.
     """
+    return _control(m, blocks, seed)
+
+
+def control_lp(m: int = 30, blocks: tuple[int, ...] = (12,), lp: int = 10, density: float = 0.3,
+               seed: int = 0) -> SDPText:
+    """`control` with an LP block of `lp` nonnegative variables appended (block size
+    -lp in the file): every constraint gets N(0,1) coefficients on a random `density`
+    share of them (at least one); ``x0, z0 ~ U[0.5, 2]`` extend the strictly feasible
+    triple with the same ``y0``.  Sums exactly rounded: byte-identical everywhere."""
+    return _control(m, blocks, seed, lp=lp, density=density)
+
+
+def _control(m, blocks, seed, lp: int = 0, density: float = 0.3) -> SDPText:
     rng = np.random.default_rng(seed)
-    prob = SDPText(f"control m={m} blocks={list(blocks)} seed={seed}", m, list(blocks))
+    if lp:
+        prob = SDPText(f"control_lp m={m} blocks={list(blocks)} lp={lp} seed={seed}", m, list(blocks) + [-lp])
+    else:
+        prob = SDPText(f"control m={m} blocks={list(blocks)} seed={seed}", m, list(blocks))
     scale = float(1 << _DYADIC_BITS)
     A = []  # A[l][i] = list of upper-triangle values, row-major over (a <= b)
     for nb in blocks:
@@ -198,6 +214,15 @@ def control(m: int = 231, blocks: tuple[int, ...] = (40, 20), seed: int = 0) -> 
     X0 = [_spd(nb, rng) for nb in blocks]
     y0 = [float(x) for x in rng.standard_normal(m)]
     Z0 = [_spd(nb, rng) for nb in blocks]
+    coef, x0, z0 = [], [], []
+    if lp:  # drawn after everything `control` draws, so its blocks are unchanged
+        for _ in range(m):
+            mask = rng.random(lp) < density
+            mask[int(rng.integers(0, lp))] = True
+            vals = rng.standard_normal(lp)
+            coef.append({k: round(float(vals[k]) * scale) / scale for k in range(lp) if mask[k]})
+        x0 = [float(v) for v in rng.uniform(0.5, 2.0, lp)]
+        z0 = [float(v) for v in rng.uniform(0.5, 2.0, lp)]
     for i in range(m):
         terms = []
         for l, nb in enumerate(blocks):
@@ -206,6 +231,8 @@ def control(m: int = 231, blocks: tuple[int, ...] = (40, 20), seed: int = 0) -> 
                 for b in range(nb):
                     s_ab = Ai[min(a, b)][max(a, b)]
                     terms.append(s_ab * Xl[a][b])
+        if lp:
+            terms += [a * x0[k] for k, a in coef[i].items()]
         prob.c[i] = _dyadic(math.fsum(terms))
     for l, nb in enumerate(blocks):
         for a in range(nb):
@@ -218,6 +245,14 @@ def control(m: int = 231, blocks: tuple[int, ...] = (40, 20), seed: int = 0) -> 
             for a in range(nb):
                 for b in range(a, nb):
                     prob.add(i + 1, l + 1, a + 1, b + 1, _dyadic(Ai[a][b]))
+    if lp:
+        lpb = len(blocks) + 1
+        for k in range(lp):  # C = z0 + sum_i y0_i a_i on the LP block (F0 = -C)
+            c_k = math.fsum([z0[k]] + [y0[i] * coef[i][k] for i in range(m) if k in coef[i]])
+            prob.add(0, lpb, k + 1, k + 1, _dyadic(-c_k))
+        for i in range(m):
+            for k, a in sorted(coef[i].items()):
+                prob.add(i + 1, lpb, k + 1, k + 1, _dyadic(a))
     return prob
 
 

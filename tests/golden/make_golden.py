@@ -45,6 +45,9 @@ CASES = {
     "maxcut100": ("maxcut", dict(n=100, p=0.1, seed=0), 256),
     "maxcut124pm": ("maxcut", dict(n=124, p=0.1, seed=0, signed=True), 256),
     "control231": ("control", dict(m=231, blocks=(40, 20), seed=0), 256),
+    # LP blocks (a fourth element would hold param_text overrides)
+    "controllp20": ("control_lp", dict(m=20, blocks=(10,), lp=12, seed=5), 256),
+    "controllp40": ("control_lp", dict(m=40, blocks=(24, 8), lp=30, density=0.2, seed=6), 256),
 }
 
 ITER_RE = re.compile(r"^\s*(\d+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s*$")
@@ -143,15 +146,19 @@ def main() -> None:
             with open(os.path.join(HERE, "example1.json"), "w") as f:
                 json.dump(r, f, indent=1)
             print("example1", r["phase"], r["iteration"], r["objValPrimal"])
-        for name, (gen, kw, prec) in CASES.items():
+        for name, case in CASES.items():
             if args.only and name not in args.only:
                 continue
+            gen, kw, prec = case[:3]
+            pkw = case[3] if len(case) > 3 else {}
             dat_text = getattr(problems, gen)(**kw).text()
-            param_text = problems.param_text(precision=prec)
+            param_text = problems.param_text(precision=prec, **pkw)
             r = run_case(binary, dat_text, param_text, work, name)
             r.update(name=name, generator=gen, kwargs={k: (list(v) if isinstance(v, tuple) else v)
                                                          for k, v in kw.items()},
                      precision=prec, sha256=hashlib.sha256(dat_text.encode()).hexdigest())
+            if pkw:
+                r["param"] = pkw
             with open(os.path.join(HERE, name + ".json"), "w") as f:
                 json.dump(r, f, indent=1)
             print(name, r.get("phase"), r.get("iteration"), r.get("objValPrimal"))

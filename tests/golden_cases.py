@@ -27,7 +27,7 @@ def write_inputs(name, directory):
     with open(dat, "w") as f:
         f.write(text)
     with open(par, "w") as f:
-        f.write(problems.param_text(precision=g["precision"]))
+        f.write(problems.param_text(precision=g["precision"], **g.get("param", {})))
     return dat, par, g
 
 

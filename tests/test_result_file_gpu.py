@@ -1,6 +1,7 @@
 """The result file of a whole solve (the reference driver's output: header, iteration
 table, summary, parameters, time table, xVec / xMat / yMat, final times) against the
-reference's own file for its known-answer input example1.dat-s: the same lines once
+reference's own file for its known-answer input example1.dat-s and for a problem with
+an LP block: the same lines once
 numbers, the start time and file names are masked, and the 40-digit solution within
 1e-20 relative to max(1, |x|) (the solves stop at relative gap 1e-30)."""
 import importlib.util
@@ -41,11 +42,14 @@ def _check(text, g, mg):
         assert ok, (key, worst)
 
 
-def test_solve_file_writes_the_reference_layout(sdpg, tmp_path):
-    g = load("example1")
+@pytest.mark.parametrize("name", ["example1", "controllp20"])
+def test_solve_file_writes_the_reference_layout(sdpg, tmp_path, name):
+    """example1 (one SDP block) and a problem with an LP block, whose solution prints
+    as one braced row per LP block."""
+    g = load(name)
     mg = _make_golden()
-    dat, par, _ = write_inputs("example1", str(tmp_path))
-    out = str(tmp_path / "example1.result")
+    dat, par, _ = write_inputs(name, str(tmp_path))
+    out = str(tmp_path / (name + ".result"))
     info = sdpg.solve_file(dat, par, out)
     assert info["phase"] == "pdOPT"
     with open(out) as f:

@@ -21,7 +21,7 @@ from golden_cases import write_inputs
 pytestmark = pytest.mark.gpu
 
 SMALL = ["example1", "maxcut20", "maxcut40", "maxcut40pm", "control20", "control30", "maxcut40_p512",
-         "gpp40"]
+         "gpp40", "controllp20", "controllp40"]
 LARGE = ["gpp60", "maxcut100", "maxcut124pm", "control231"]
 # Graph-partition problems have no strictly feasible primal point (diag(X) = 1 and
 # (11^T).X = 0 force X to be singular), so both solvers end in pFEAS once the step
