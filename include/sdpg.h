@@ -245,9 +245,10 @@ int sdpg_solve_file(const char *data_path, const char *param_path, const char *o
 /* The same with, if print_to_stdout, the iteration table and summary also on stdout:
  * what the command-line driver sdpa_gmp_gb300 calls.  param (may be NULL) gives the
  * parameters directly and param_path is then only echoed in the header; with param NULL
- * a param_path is read as a param.sdpa file, and without either the defaults apply. */
-int sdpg_solve_file_ex(const char *data_path, const sdpg_param *param, const char *param_path, const char *out_path,
-                       int device, int print_to_stdout, double *info12);
+ * a param_path is read as a param.sdpa file, and without either the defaults apply.
+ * init_path (may be NULL): an initial-point file, sparse (-is) or dense (-id) format. */
+int sdpg_solve_file_ex(const char *data_path, const sdpg_param *param, const char *param_path, const char *init_path,
+                       int init_sparse, const char *out_path, int device, int print_to_stdout, double *info12);
 
 /* ---- learned parameter proposal (no reference counterpart) ------------------
  * A fully connected FP32 network (6 inputs, three hidden layers of 64 tanh units,
@@ -282,6 +283,12 @@ int sdpg_policy_gradient(sdpg_policy *p, const float *x, const float *t, const f
  * samples for `epochs` passes; epoch_loss[e] (may be NULL) = mean batch loss of pass e. */
 int sdpg_policy_train(sdpg_policy *p, const float *x, const float *t, const float *mask, int count, int epochs,
                       int batch, float lr, unsigned long long seed, float *epoch_loss);
+/* IO::read of an initial-point file (sdpa_io.cpp:150-276; sparse: the -is format,
+ * otherwise -id): x0 then the user's primal matrix (target 1) and dual matrix (target 2).
+ * The next initialize() starts from it (main, sdpa_main.cpp:237-277): entries not given
+ * keep lambdaStar * I, y = -x0, mu0 = X.Z / n.  SDPG_ERR_NOT_PD from initialize() if a
+ * matrix is not positive definite. */
+int sdpg_solver_read_initial_point(sdpg_solver *h, const char *path, int sparse);
 /* Attach (NULL detaches) a policy to a solver on the same device.  flags: 1 propose the
  * corrector beta each iteration, 2 propose lambdaStar at initialize().  A proposed beta
  * whose step fails the checks (the predicted mu must fall by a factor 1 - min(alphaP,

@@ -123,6 +123,9 @@ def _setup(lib: ctypes.CDLL) -> ctypes.CDLL:
         "sdpg_policy_gradient": (i, [vp, vp, vp, vp, i, vp, vp]),
         "sdpg_policy_train": (i, [vp, vp, vp, vp, i, i, i, c.c_float, c.c_ulonglong, vp]),
         "sdpg_solver_set_policy": (i, [vp, vp, i]),
+        "sdpg_solver_read_initial_point": (i, [vp, c.c_char_p, i]),
+        "sdpg_solve_file_ex": (i, [c.c_char_p, c.POINTER(Param), c.c_char_p, c.c_char_p, i, c.c_char_p, i, i,
+                                   c.POINTER(c.c_double)]),
         "sdpg_solver_policy_stats": (i, [vp, c.POINTER(c.c_double)]),
         "sdpg_solver_features": (i, [vp, vp, i]),
     }
@@ -471,6 +474,10 @@ class Solver:
         a, b = ctypes.c_longlong(), ctypes.c_longlong()
         check(lib().sdpg_solver_io_bytes(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def read_initial_point(self, path: str, sparse: bool = True) -> None:
+        """Start the next initialize() from an -is (sparse) / -id (dense) initial-point file."""
+        check(lib().sdpg_solver_read_initial_point(self.h, path.encode(), 1 if sparse else 0))
 
     def set_policy(self, policy: "Policy | None", beta: bool = True, lam: bool = True) -> None:
         """Attach a learned proposal (the policy must outlive the solver's use of it)."""

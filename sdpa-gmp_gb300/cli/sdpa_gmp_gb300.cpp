@@ -1,9 +1,8 @@
 // Command-line driver with the reference's argument forms (main, sdpa_main.cpp:501-677):
-//   sdpa_gmp_gb300 -ds data.dat-s -o out.result [-p param.sdpa] [-pt 0|1|2]
+//   sdpa_gmp_gb300 -ds data.dat-s -o out.result [-p param.sdpa] [-pt 0|1|2] [-is init | -id init]
 //   sdpa_gmp_gb300 data.dat-s out.result [param.sdpa]
 // It solves on GPU 0 (SDPG_DEVICE selects another) through the library's C ABI and writes
-// the reference's result-file layout.  Dense-format data (-dd) and initial-point files
-// (-id / -is) are not supported and are refused with a message.
+// the reference's result-file layout.  Dense-format data (-dd) is refused with a message.
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -13,7 +12,7 @@
 
 static int usage(const char *prog) {
     fprintf(stderr,
-            "usage: %s -ds data.dat-s -o out.result [-p param.sdpa] [-pt 0|1|2]\n"
+            "usage: %s -ds data.dat-s -o out.result [-p param.sdpa] [-pt 0|1|2] [-is|-id init]\n"
             "       %s data.dat-s out.result [param.sdpa]\n",
             prog, prog);
     return 1;
@@ -24,8 +23,8 @@ int main(int argc, char **argv) {
     const time_t now = time(NULL);
     printf("SDPA-GMP start at    %s", ctime(&now));
     if (argc < 3) return usage(argv[0]);
-    const char *data = NULL, *out = NULL, *par = NULL;
-    int preset = -1;
+    const char *data = NULL, *out = NULL, *par = NULL, *init = NULL;
+    int preset = -1, init_sparse = 0;
     if (argv[1][0] == '-') {
         for (int i = 1; i < argc; ++i) {
             const char *a = argv[i];
@@ -41,9 +40,11 @@ int main(int argc, char **argv) {
                 preset = atoi(argv[++i]);
                 if (preset < 0 || preset > 2) preset = 0;
                 par = NULL;
-            } else if ((!strcmp(a, "-dd") || !strcmp(a, "-id") || !strcmp(a, "-is")) && has) {
-                fprintf(stderr, "%s: option %s is not supported (sparse .dat-s data only, no initial point)\n",
-                        argv[0], a);
+            } else if ((!strcmp(a, "-is") || !strcmp(a, "-id")) && has) {
+                init_sparse = !strcmp(a, "-is");
+                init = argv[++i];
+            } else if (!strcmp(a, "-dd") && has) {
+                fprintf(stderr, "%s: option -dd is not supported (sparse .dat-s data only)\n", argv[0]);
                 return 1;
             } else if (!strcmp(a, "-k") && has) {
                 ++i;  // the F1/F2/F3 cost factor stays at its default of 1.2
@@ -67,9 +68,9 @@ int main(int argc, char **argv) {
             fprintf(stderr, "%s\n", sdpg_last_error());
             return 1;
         }
-        rc = sdpg_solve_file_ex(data, &prm, NULL, out, device, 1, info);
+        rc = sdpg_solve_file_ex(data, &prm, NULL, init, init_sparse, out, device, 1, info);
     } else {
-        rc = sdpg_solve_file_ex(data, NULL, par, out, device, 1, info);
+        rc = sdpg_solve_file_ex(data, NULL, par, init, init_sparse, out, device, 1, info);
     }
     if (rc < 0) {
         fprintf(stderr, "%s: %s\n", argv[0], sdpg_last_error());

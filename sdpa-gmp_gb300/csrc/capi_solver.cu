@@ -101,15 +101,19 @@ SolverBase &S(sdpg_solver *h) {
 // start line, the data file's title/comment lines (IO::read, sdpa_io.cpp:123-134), the
 // file names, "DENSE computation" (Newton::initialize, sdpa_newton.cpp:349-350), the
 // iteration table and summary, then parameters, time table, solution and final times.
-int solve_file_impl(const char *data_path, const Param &q, const char *param_path, const char *out_path, int device,
-                    FILE *display, double *info12) {
+int solve_file_impl(const char *data_path, const Param &q, const char *param_path, const char *init_path,
+                    bool init_sparse, const char *out_path, int device, FILE *display, double *info12) {
     if (!data_path) throw sdpg_error(SDPG_ERR_ARG, "no data file");
     const auto t0 = std::chrono::steady_clock::now();
     std::string err;
     RawProblem P;
     if (!read_sdpa(data_path, false, P, &err)) throw sdpg_error(SDPG_ERR_IO, err);
+    InitPoint ip;
+    const bool has_init = init_path && init_path[0];
+    if (has_init && !read_init(init_path, init_sparse, P.m, P.blockStruct, ip, &err)) throw sdpg_error(SDPG_ERR_IO, err);
     const double read_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     std::unique_ptr<sdpg_solver> h(wrap(P, q, device, nullptr));
+    if (has_init) h->s->set_initial_point(ip);
     FILE *out = nullptr;
     if (out_path && out_path[0]) {
         out = fopen(out_path, "w");
@@ -123,6 +127,7 @@ int solve_file_impl(const char *data_path, const Param &q, const char *param_pat
             fputs(P.title.c_str(), out);
             fprintf(out, "data      is %s\n", data_path);
             if (param_path && param_path[0]) fprintf(out, "parameter is %s\n", param_path);
+            if (has_init) fprintf(out, "initial   is %s\n", init_path);
             fprintf(out, "out       is %s\n", out_path);
             fprintf(out, "DENSE computation\n");
         }
@@ -480,6 +485,18 @@ int sdpg_solver_reset_counters(sdpg_solver *h) {
     });
 }
 
+int sdpg_solver_read_initial_point(sdpg_solver *h, const char *path, int sparse) {
+    return sdpg_guard([&] {
+        SolverBase &s = S(h);
+        InitPoint ip;
+        std::string err;
+        if (!path || !read_init(path, sparse != 0, s.m(), s.block_structure(), ip, &err))
+            throw sdpg_error(SDPG_ERR_IO, path ? err : std::string("no init file"));
+        s.set_initial_point(ip);
+        return SDPG_OK;
+    });
+}
+
 int sdpg_solver_set_policy(sdpg_solver *h, sdpg_policy *p, int flags) {
     return sdpg_guard([&] {
         if (flags < 0 || flags > 3) throw sdpg_error(SDPG_ERR_ARG, "policy flags are 0..3");
@@ -512,19 +529,19 @@ int sdpg_solve_file(const char *data_path, const char *param_path, const char *o
         Param q;
         std::string err;
         if (param_path && param_path[0] && !param_read(q, param_path, &err)) throw sdpg_error(SDPG_ERR_IO, err);
-        return solve_file_impl(data_path, q, param_path, out_path, device, nullptr, info12);
+        return solve_file_impl(data_path, q, param_path, nullptr, false, out_path, device, nullptr, info12);
     });
 }
 
-int sdpg_solve_file_ex(const char *data_path, const sdpg_param *param, const char *param_path, const char *out_path,
-                       int device, int print_to_stdout, double *info12) {
+int sdpg_solve_file_ex(const char *data_path, const sdpg_param *param, const char *param_path, const char *init_path,
+                       int init_sparse, const char *out_path, int device, int print_to_stdout, double *info12) {
     return sdpg_guard([&] {
         Param q = to_param(param);
         std::string err;
         if (!param && param_path && param_path[0] && !param_read(q, param_path, &err))
             throw sdpg_error(SDPG_ERR_IO, err);
-        return solve_file_impl(data_path, q, param_path, out_path, device, print_to_stdout ? stdout : nullptr,
-                               info12);
+        return solve_file_impl(data_path, q, param_path, init_path, init_sparse != 0, out_path, device,
+                               print_to_stdout ? stdout : nullptr, info12);
     });
 }
 

@@ -195,4 +195,81 @@ bool read_sdpa(const char *path, bool dense, RawProblem &P, std::string *err) {
     return true;
 }
 
+// The reference numbers SDP blocks first (l <= number of SDP blocks, in file order) and
+// addresses LP entries by one index running over all LP blocks (sdpa_io.cpp:192-217).
+bool read_init(const char *path, bool sparse, int m, const std::vector<int> &blockStruct, InitPoint &ip,
+               std::string *err) {
+    std::ifstream in(path);
+    if (!in) {
+        if (err) *err = std::string("cannot open init file ") + path;
+        return false;
+    }
+    std::stringstream ss;
+    ss << in.rdbuf();
+    Scanner sc;
+    sc.s = ss.str();
+    auto fail = [&](const std::string &m) {
+        if (err) *err = m + " in init file " + path;
+        return false;
+    };
+    std::vector<int> sdp_blocks, lp_block, lp_local;  // file block of each SDP / LP position
+    for (size_t l = 0; l < blockStruct.size(); ++l) {
+        const int bs = blockStruct[l];
+        if (bs >= 2) {
+            sdp_blocks.push_back((int)l);
+        } else {
+            const int n = bs < 0 ? -bs : bs;
+            for (int k = 0; k < n; ++k) {
+                lp_block.push_back((int)l);
+                lp_local.push_back(k);
+            }
+        }
+    }
+    ip.x0.assign(m, mlf<16>{});
+    for (int k = 0; k < m; ++k)
+        if (!sc.read_num(&ip.x0[k])) return fail("missing x0 entries");
+    ip.entries.clear();
+    if (sparse) {
+        while (true) {
+            int target, l, i, j;
+            mlf<16> v;
+            if (!sc.read_int(&target) || !sc.read_int(&l) || !sc.read_int(&i) || !sc.read_int(&j) || !sc.read_num(&v))
+                break;
+            if (target != 1 && target != 2) return fail("matrix selector not 1 or 2");
+            if (l >= 1 && l <= (int)sdp_blocks.size()) {
+                const int fb = sdp_blocks[l - 1];
+                const int n = blockStruct[fb];
+                if (i < 1 || j < 1 || i > n || j > n) return fail("index out of range");
+                ip.entries.push_back({target, fb, i - 1, j - 1, v});
+            } else if (l > (int)sdp_blocks.size()) {
+                if (i != j) return fail("LP entry off the diagonal");
+                if (i < 1 || i > (int)lp_block.size()) return fail("LP index out of range");
+                ip.entries.push_back({target, lp_block[i - 1], lp_local[i - 1], lp_local[i - 1], v});
+            } else {
+                return fail("block number out of range");
+            }
+        }
+    } else {
+        // dense: Z then X, each as every SDP block in full, then all LP entries; zeros
+        // and the lower triangle are skipped, as the reference skips them
+        for (int target = 1; target <= 2; ++target) {
+            for (int fb : sdp_blocks) {
+                const int n = blockStruct[fb];
+                for (int i = 0; i < n; ++i)
+                    for (int j = 0; j < n; ++j) {
+                        mlf<16> v;
+                        if (!sc.read_num(&v)) return fail("missing matrix entries");
+                        if (i <= j && !ml_is_zero(v)) ip.entries.push_back({target, fb, i, j, v});
+                    }
+            }
+            for (size_t k = 0; k < lp_block.size(); ++k) {
+                mlf<16> v;
+                if (!sc.read_num(&v)) return fail("missing LP entries");
+                if (!ml_is_zero(v)) ip.entries.push_back({target, lp_block[k], lp_local[k], lp_local[k], v});
+            }
+        }
+    }
+    return true;
+}
+
 }  // namespace sdpg

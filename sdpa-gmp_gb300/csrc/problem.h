@@ -49,6 +49,22 @@ struct RawProblem {
 // IO::read for the sparse format (.dat-s); dense .dat when `dense` is true.
 bool read_sdpa(const char *path, bool dense, RawProblem &P, std::string *err);
 
+// An initial point (IO::read of -id / -is files, sdpa_io.cpp:150-276): the first m
+// numbers are x0 (the solver's y = -x0), then entries of the two matrices, target 1
+// the solver's Z (the user's primal matrix) and target 2 its X.  Entries are kept as
+// given, with blocks in the data file's numbering (0-based) and indices within the
+// block; entries not given keep the lambdaStar * I start (as in the reference).
+struct InitEntry {
+    int target, block, i, j;
+    mlf<16> v;
+};
+struct InitPoint {
+    std::vector<mlf<16>> x0;
+    std::vector<InitEntry> entries;
+};
+bool read_init(const char *path, bool sparse, int m, const std::vector<int> &blockStruct, InitPoint &ip,
+               std::string *err);
+
 template <int N>
 inline mlf<N> narrow(const mlf<16> &x) {
     mlf<N> r;

@@ -1252,6 +1252,22 @@ class Solver final : public SolverBase {
         }
     }
 
+    std::vector<int> block_structure() const override {
+        std::vector<int> bs;
+        for (const Blk &B : blk_) bs.push_back(B.lp ? -B.n : B.n);
+        return bs;
+    }
+    void set_initial_point(const InitPoint &ip) override {
+        if ((int)ip.x0.size() != m_) throw sdpg_error(SDPG_ERR_ARG, "initial point: x0 has the wrong length");
+        for (const InitEntry &e : ip.entries)
+            if (e.block < 0 || e.block >= (int)blk_.size() || e.i < 0 || e.j < 0 || e.i >= blk_[e.block].n ||
+                e.j >= blk_[e.block].n || (e.target != 1 && e.target != 2))
+                throw sdpg_error(SDPG_ERR_ARG, "initial point: entry out of range");
+        init_ = ip;
+        has_init_ = true;
+        initialized_ = false;
+    }
+
     void init_point() {
         const R lambda(par_.lambdaStar);
         const R invsq = R(1.0) / rsqrt_(lambda);
@@ -1264,13 +1280,36 @@ class Solver final : public SolverBase {
             k_set_identity<N>(B.n, B.Zinv, inv.v, st_);
         }
         SDPG_CUDA(cudaMemsetAsync(y_, 0, m_ * sizeof(V), st_));
+        if (has_init_) {
+            // main, sdpa_main.cpp:237-251: the file's entries over lambdaStar * I (both
+            // triangles, DenseLinearSpace::setElement_SDP), y = -x0, then the inverses
+            for (size_t l = 0; l < blk_.size(); ++l) {
+                Blk &B = blk_[l];
+                const size_t nn = (size_t)B.n * B.n;
+                std::vector<V> Xh(nn, ml_zero<N>()), Zh(nn, ml_zero<N>());
+                for (int k = 0; k < B.n; ++k) Xh[k + (size_t)B.n * k] = Zh[k + (size_t)B.n * k] = lambda.v;
+                for (const InitEntry &e : init_.entries) {
+                    if (e.block != (int)l) continue;
+                    std::vector<V> &M = e.target == 1 ? Zh : Xh;
+                    M[e.i + (size_t)B.n * e.j] = M[e.j + (size_t)B.n * e.i] = narrow<N>(e.v);
+                }
+                upload(B.X, Xh.data(), nn);
+                upload(B.Z, Zh.data(), nn);
+            }
+            std::vector<V> yh(m_);
+            for (int k = 0; k < m_; ++k) yh[k] = ml_neg(narrow<N>(init_.x0[k]));
+            upload(y_, yh.data(), m_);
+            if (!computeInverse())
+                throw sdpg_error(SDPG_ERR_NOT_PD, "initial point: a matrix is not positive definite");
+        }
         residuals();
         initNormP_ = normP_;
         initNormD_ = normD_;
         aP_ = aD_ = R(0.0);
         betaV_ = R(par_.betaStar);
         reductionOn_ = 1;
-        muInit_ = lambda * lambda;
+        // AverageComplementarity::initialize (sdpa_parts.cpp:633-643)
+        muInit_ = has_init_ ? ip_blocks(&Blk::X, &Blk::Z) / R(nDim_) : lambda * lambda;
         muCur_ = muInit_;
         const R accuracy(par_.epsilonDash);
         thP_ = (initNormP_ < accuracy) ? R(0.0) : R(1.0);
@@ -1706,6 +1745,8 @@ class Solver final : public SolverBase {
     double prof_ms_ = 0;
     long long prof_launches_ = 0, prof_macs_ = 0;
     mutable long long h2d_ = 0, d2h_ = 0;
+    bool has_init_ = false;  // an initial point replaces lambdaStar * I
+    InitPoint init_;
     // learned proposal
     const Policy *policy_ = nullptr;
     int pol_flags_ = 0;

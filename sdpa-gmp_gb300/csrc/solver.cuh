@@ -79,6 +79,10 @@ class SolverBase {
     // bytes copied host->device and device->host since construction (setup included)
     virtual void io_bytes(long long *h2d, long long *d2h) const = 0;
     virtual void sync() = 0;
+    // the data file's block structure (negative: LP block)
+    virtual std::vector<int> block_structure() const = 0;
+    // start from this point instead of lambdaStar * I (the -id / -is files)
+    virtual void set_initial_point(const InitPoint &ip) = 0;
     // the result file after the summary block: parameters, time table, xVec / xMat / yMat
     virtual void print_result_tail(FILE *f, double file_read_seconds) = 0;
     // learned proposal (flags: 1 corrector beta, 2 lambdaStar); null detaches

@@ -100,14 +100,14 @@ def result_layout(text: str) -> list[str]:
     for ln in text.splitlines():
         if ln.startswith("SDPA-GMP start at"):
             ln = "SDPA-GMP start at <time>"
-        for tag in ("data      is ", "parameter is ", "out       is "):
+        for tag in ("data      is ", "parameter is ", "initial   is ", "out       is "):
             if ln.startswith(tag):
                 ln = tag + "<path>"
         out.append(NUM_RE.sub("#", ln))
     return out
 
 
-def run_case(binary: str, dat_text: str, param_text: str, workdir: str, name: str) -> dict:
+def run_case(binary: str, dat_text: str, param_text: str, workdir: str, name: str, extra=()) -> dict:
     dat = os.path.join(workdir, name + ".dat-s")
     par = os.path.join(workdir, name + ".param")
     res = os.path.join(workdir, name + ".result")
@@ -116,7 +116,7 @@ def run_case(binary: str, dat_text: str, param_text: str, workdir: str, name: st
     with open(par, "w") as f:
         f.write(param_text)
     env = dict(os.environ, OMP_NUM_THREADS=str(os.cpu_count() or 1))
-    subprocess.run([binary, "-ds", dat, "-o", res, "-p", par], check=True, env=env,
+    subprocess.run([binary, "-ds", dat, "-o", res, "-p", par, *extra], check=True, env=env,
                    stdout=subprocess.DEVNULL)
     with open(res) as f:
         return parse_result(f.read())
@@ -146,6 +146,17 @@ def main() -> None:
             with open(os.path.join(HERE, "example1.json"), "w") as f:
                 json.dump(r, f, indent=1)
             print("example1", r["phase"], r["iteration"], r["objValPrimal"])
+            # the reference's own initial points for example1: sparse (-is) and dense (-id)
+            for tag, fname, opt in (("is", "example1.ini-s", "-is"), ("id", "example1.ini", "-id")):
+                shutil.copy(os.path.join(args.ref, fname), os.path.join(HERE, fname))
+                r = run_case(binary, dat_text, param_text, work, "example1_" + tag,
+                             extra=(opt, os.path.join(HERE, fname)))
+                r.update(name="example1_" + tag, source=f"reference example1.dat-s + param.sdpa + {fname} ({opt})",
+                         precision=200, sha256=hashlib.sha256(dat_text.encode()).hexdigest(),
+                         init={"file": fname, "sparse": opt == "-is"})
+                with open(os.path.join(HERE, "example1_" + tag + ".json"), "w") as f:
+                    json.dump(r, f, indent=1)
+                print("example1_" + tag, r["phase"], r["iteration"], r["objValPrimal"])
         for name, case in CASES.items():
             if args.only and name not in args.only:
                 continue

@@ -16,7 +16,7 @@ def load(name):
 def write_inputs(name, directory):
     """Write <name>.dat-s and <name>.param for a golden case; returns (dat, param, golden)."""
     g = load(name)
-    if name == "example1":
+    if name.startswith("example1"):  # the reference's own input (and initial points)
         return os.path.join(GOLDEN, "example1.dat-s"), os.path.join(GOLDEN, "example1.param"), g
     problems = importlib.import_module("sdpa-gmp_gb300.problems")
     kw = {k: (tuple(v) if isinstance(v, list) else v) for k, v in g["kwargs"].items()}
@@ -33,3 +33,11 @@ def write_inputs(name, directory):
 
 def fnum(s):
     return float(s)
+
+
+def init_file(g):
+    """(path, sparse) of a golden case's initial-point file, or None."""
+    ini = g.get("init")
+    if not ini:
+        return None
+    return os.path.join(GOLDEN, ini["file"]), bool(ini["sparse"])

@@ -11,7 +11,7 @@ from decimal import Decimal, getcontext
 
 import pytest
 
-from golden_cases import GOLDEN, load, write_inputs
+from golden_cases import GOLDEN, init_file, load, write_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -68,10 +68,20 @@ def test_command_line_driver(sdpg, tmp_path):
     assert "phase.value = pdOPT" in r.stdout
     with open(out) as f:
         _check(f.read(), g, mg)
+    # an initial point (-is / -id), as the reference ran it
+    for name, opt in (("example1_is", "-is"), ("example1_id", "-id")):
+        gi = load(name)
+        path, _ = init_file(gi)
+        outi = str(tmp_path / (name + ".result"))
+        r = subprocess.run([exe, "-ds", dat, "-o", outi, "-p", par, opt, path], capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stderr
+        with open(outi) as f:
+            _check(f.read(), gi, mg)
     # the positional form, and a refused option
     out2 = str(tmp_path / "cli2.result")
     assert subprocess.run([exe, dat, out2, par], capture_output=True, timeout=300).returncode == 0
     with open(out2) as f:
         _check(f.read(), g, mg)
-    assert subprocess.run([exe, "-is", "x", "-ds", dat, "-o", out2], capture_output=True,
+    assert subprocess.run([exe, "-dd", "x", "-ds", dat, "-o", out2], capture_output=True,
                           timeout=60).returncode != 0

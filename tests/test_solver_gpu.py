@@ -16,12 +16,12 @@ import os
 
 import pytest
 
-from golden_cases import write_inputs
+from golden_cases import init_file, write_inputs
 
 pytestmark = pytest.mark.gpu
 
-SMALL = ["example1", "maxcut20", "maxcut40", "maxcut40pm", "control20", "control30", "maxcut40_p512",
-         "gpp40", "controllp20", "controllp40"]
+SMALL = ["example1", "example1_is", "example1_id", "maxcut20", "maxcut40", "maxcut40pm", "control20", "control30",
+         "maxcut40_p512", "gpp40", "controllp20", "controllp40"]
 LARGE = ["gpp60", "maxcut100", "maxcut124pm", "control231"]
 # Graph-partition problems have no strictly feasible primal point (diag(X) = 1 and
 # (11^T).X = 0 force X to be singular), so both solvers end in pFEAS once the step
@@ -45,6 +45,9 @@ def run_case(sdpg, name, tmp_path):
     dat, par, g = write_inputs(name, str(tmp_path))
     prob = sdpg.Problem.read(dat)
     solver = sdpg.Solver(prob, sdpg.Param.read(par))
+    ini = init_file(g)
+    if ini:  # the reference's -is / -id initial point
+        solver.read_initial_point(*ini)
     out = str(tmp_path / (name + ".out"))
     solver.run(out)
     return solver, g
