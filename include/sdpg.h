@@ -246,9 +246,11 @@ int sdpg_solve_file(const char *data_path, const char *param_path, const char *o
  * what the command-line driver sdpa_gmp_gb300 calls.  param (may be NULL) gives the
  * parameters directly and param_path is then only echoed in the header; with param NULL
  * a param_path is read as a param.sdpa file, and without either the defaults apply.
+ * data_dense: the data file is in the dense .dat format (-dd) instead of .dat-s (-ds).
  * init_path (may be NULL): an initial-point file, sparse (-is) or dense (-id) format. */
-int sdpg_solve_file_ex(const char *data_path, const sdpg_param *param, const char *param_path, const char *init_path,
-                       int init_sparse, const char *out_path, int device, int print_to_stdout, double *info12);
+int sdpg_solve_file_ex(const char *data_path, int data_dense, const sdpg_param *param, const char *param_path,
+                       const char *init_path, int init_sparse, const char *out_path, int device, int print_to_stdout,
+                       double *info12);
 
 /* ---- learned parameter proposal (no reference counterpart) ------------------
  * A fully connected FP32 network (6 inputs, three hidden layers of 64 tanh units,

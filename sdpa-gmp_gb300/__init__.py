@@ -124,7 +124,7 @@ def _setup(lib: ctypes.CDLL) -> ctypes.CDLL:
         "sdpg_policy_train": (i, [vp, vp, vp, vp, i, i, i, c.c_float, c.c_ulonglong, vp]),
         "sdpg_solver_set_policy": (i, [vp, vp, i]),
         "sdpg_solver_read_initial_point": (i, [vp, c.c_char_p, i]),
-        "sdpg_solve_file_ex": (i, [c.c_char_p, c.POINTER(Param), c.c_char_p, c.c_char_p, i, c.c_char_p, i, i,
+        "sdpg_solve_file_ex": (i, [c.c_char_p, i, c.POINTER(Param), c.c_char_p, c.c_char_p, i, c.c_char_p, i, i,
                                    c.POINTER(c.c_double)]),
         "sdpg_solver_policy_stats": (i, [vp, c.POINTER(c.c_double)]),
         "sdpg_solver_features": (i, [vp, vp, i]),

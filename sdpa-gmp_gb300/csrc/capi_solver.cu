@@ -101,13 +101,14 @@ SolverBase &S(sdpg_solver *h) {
 // start line, the data file's title/comment lines (IO::read, sdpa_io.cpp:123-134), the
 // file names, "DENSE computation" (Newton::initialize, sdpa_newton.cpp:349-350), the
 // iteration table and summary, then parameters, time table, solution and final times.
-int solve_file_impl(const char *data_path, const Param &q, const char *param_path, const char *init_path,
-                    bool init_sparse, const char *out_path, int device, FILE *display, double *info12) {
+int solve_file_impl(const char *data_path, bool data_dense, const Param &q, const char *param_path,
+                    const char *init_path, bool init_sparse, const char *out_path, int device, FILE *display,
+                    double *info12) {
     if (!data_path) throw sdpg_error(SDPG_ERR_ARG, "no data file");
     const auto t0 = std::chrono::steady_clock::now();
     std::string err;
     RawProblem P;
-    if (!read_sdpa(data_path, false, P, &err)) throw sdpg_error(SDPG_ERR_IO, err);
+    if (!read_sdpa(data_path, data_dense, P, &err)) throw sdpg_error(SDPG_ERR_IO, err);
     InitPoint ip;
     const bool has_init = init_path && init_path[0];
     if (has_init && !read_init(init_path, init_sparse, P.m, P.blockStruct, ip, &err)) throw sdpg_error(SDPG_ERR_IO, err);
@@ -529,19 +530,20 @@ int sdpg_solve_file(const char *data_path, const char *param_path, const char *o
         Param q;
         std::string err;
         if (param_path && param_path[0] && !param_read(q, param_path, &err)) throw sdpg_error(SDPG_ERR_IO, err);
-        return solve_file_impl(data_path, q, param_path, nullptr, false, out_path, device, nullptr, info12);
+        return solve_file_impl(data_path, false, q, param_path, nullptr, false, out_path, device, nullptr, info12);
     });
 }
 
-int sdpg_solve_file_ex(const char *data_path, const sdpg_param *param, const char *param_path, const char *init_path,
-                       int init_sparse, const char *out_path, int device, int print_to_stdout, double *info12) {
+int sdpg_solve_file_ex(const char *data_path, int data_dense, const sdpg_param *param, const char *param_path,
+                       const char *init_path, int init_sparse, const char *out_path, int device, int print_to_stdout,
+                       double *info12) {
     return sdpg_guard([&] {
         Param q = to_param(param);
         std::string err;
         if (!param && param_path && param_path[0] && !param_read(q, param_path, &err))
             throw sdpg_error(SDPG_ERR_IO, err);
-        return solve_file_impl(data_path, q, param_path, init_path, init_sparse != 0, out_path, device,
-                               print_to_stdout ? stdout : nullptr, info12);
+        return solve_file_impl(data_path, data_dense != 0, q, param_path, init_path, init_sparse != 0, out_path,
+                               device, print_to_stdout ? stdout : nullptr, info12);
     });
 }
 

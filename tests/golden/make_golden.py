@@ -157,6 +157,17 @@ def main() -> None:
                 with open(os.path.join(HERE, "example1_" + tag + ".json"), "w") as f:
                     json.dump(r, f, indent=1)
                 print("example1_" + tag, r["phase"], r["iteration"], r["objValPrimal"])
+            # the same problem in the dense data format (-dd example1.dat)
+            shutil.copy(os.path.join(args.ref, "example1.dat"), os.path.join(HERE, "example1.dat"))
+            res = os.path.join(work, "example1_dd.result")
+            subprocess.run([binary, "-dd", os.path.join(HERE, "example1.dat"), "-o", res, "-p",
+                            os.path.join(HERE, "example1.param")], check=True, stdout=subprocess.DEVNULL)
+            with open(res) as f:
+                r = parse_result(f.read())
+            r.update(name="example1_dd", source="reference example1.dat (-dd) + param.sdpa", precision=200)
+            with open(os.path.join(HERE, "example1_dd.json"), "w") as f:
+                json.dump(r, f, indent=1)
+            print("example1_dd", r["phase"], r["iteration"], r["objValPrimal"])
         for name, case in CASES.items():
             if args.only and name not in args.only:
                 continue

@@ -78,10 +78,18 @@ def test_command_line_driver(sdpg, tmp_path):
         assert r.returncode == 0, r.stderr
         with open(outi) as f:
             _check(f.read(), gi, mg)
-    # the positional form, and a refused option
+    # the dense data format (-dd)
+    gd = load("example1_dd")
+    outd = str(tmp_path / "dd.result")
+    r = subprocess.run([exe, "-dd", os.path.join(GOLDEN, "example1.dat"), "-o", outd, "-p", par],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    with open(outd) as f:
+        _check(f.read(), gd, mg)
+    # the positional form, and a call that fails (no such data file)
     out2 = str(tmp_path / "cli2.result")
     assert subprocess.run([exe, dat, out2, par], capture_output=True, timeout=300).returncode == 0
     with open(out2) as f:
         _check(f.read(), g, mg)
-    assert subprocess.run([exe, "-dd", "x", "-ds", dat, "-o", out2], capture_output=True,
+    assert subprocess.run([exe, "-ds", str(tmp_path / "missing.dat-s"), "-o", out2], capture_output=True,
                           timeout=60).returncode != 0
