@@ -32,9 +32,10 @@ constexpr int kMaxTri = 512;
 
 // y[o] = sum_i A[i,o] x[i]  (op 'T': columns of A), tri: 0 all rows, 1 rows i >= o, 2 rows i <= o
 template <int N>
-__global__ void matvec_t_kernel(int n, const mlf<N> *A, int tri, const mlf<N> *x, mlf<N> *y) {
+__global__ void matvec_t_kernel(int n, const mlf<N> *A, int tri, const mlf<N> *x, mlf<N> *y,
+                                const int *gate = nullptr) {
     const int o = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (o >= n) return;
+    if (o >= n || (gate && !*gate)) return;
     const int lo = (tri == 1) ? o : 0;
     const int hi = (tri == 2) ? o + 1 : n;
     const mlf<N> *col = A + (long long)o * n;
@@ -54,9 +55,10 @@ __global__ void matvec_t_kernel(int n, const mlf<N> *A, int tri, const mlf<N> *x
 constexpr int kMvSplit = 4;
 template <int N>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
-    matvec_t_split_kernel(int n, const mlf<N> *A, int tri, const mlf<N> *x, mlf<N> *y) {
+    matvec_t_split_kernel(int n, const mlf<N> *A, int tri, const mlf<N> *x, mlf<N> *y, const int *gate) {
     constexpr int kOut = kWarpsPerBlock / kMvSplit;
     __shared__ mlf<N> part[kWarpsPerBlock];
+    if (gate && !*gate) return;  // a device-controlled Lanczos run that has stopped
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int o = blockIdx.x * kOut + warp / kMvSplit, sp = warp % kMvSplit;
     mlf<N> acc = ml_zero<N>();
@@ -190,11 +192,13 @@ __device__ int newton_level(int k, const mlf<N> *d, const mlf<N> *b2s, mlf<M> &l
 // root of a real-rooted polynomial, Newton increases monotonically towards it).
 // out[1] = |z_k| = sqrt(p_{k-1}(lam) / p_k'(lam)).
 template <int N>
-__global__ void tridiag_min_kernel(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *status) {
+__global__ void tridiag_min_kernel(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *status,
+                                   const int *gate) {
     __shared__ float df[kMaxTri], e2f[kMaxTri];
     __shared__ float bounds[2];
     extern __shared__ uint8_t tri_smem[];  // k diagonal entries, then k - 1 squared off-diagonals
     const int lane = threadIdx.x;
+    if (gate && !*gate) return;  // a device-controlled Lanczos run that has stopped
     if (k <= 0 || k > kMaxTri) {
         if (lane == 0) *status = 1;
         return;
@@ -383,7 +387,8 @@ template <int N>
 void k_matvec(int n, const mlf<N> *A, char op, int tri, const mlf<N> *x, mlf<N> *y, cudaStream_t s) {
     const int g = ceil_div(n, kWarpsPerBlock);
     if ((op == 'T' || op == 't') && n >= 128)
-        matvec_t_split_kernel<N><<<ceil_div(n, kWarpsPerBlock / kMvSplit), 32 * kWarpsPerBlock, 0, s>>>(n, A, tri, x, y);
+        matvec_t_split_kernel<N><<<ceil_div(n, kWarpsPerBlock / kMvSplit), 32 * kWarpsPerBlock, 0, s>>>(n, A, tri, x, y,
+                                                                                                   nullptr);
     else if (op == 'T' || op == 't')
         matvec_t_kernel<N><<<g, 32 * kWarpsPerBlock, 0, s>>>(n, A, tri, x, y);
     else
@@ -405,15 +410,129 @@ void k_lanczos_next(int n, const mlf<N> *r, const mlf<N> *beta, mlf<N> *q, mlf<N
 }
 
 template <int N>
-void k_tridiag_min(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *status, cudaStream_t s) {
+void k_tridiag_min(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *status, cudaStream_t s, const int *gate) {
     if (k > kMaxTri) throw sdpg_error(SDPG_ERR_TOO_LARGE, "tridiagonal larger than 512");
     static std::once_flag once;
     std::call_once(once, [] {
         SDPG_CUDA(cudaFuncSetAttribute(tridiag_min_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(2 * kMaxTri * sizeof(mlf<N>))));
     });
-    tridiag_min_kernel<N><<<1, 32, (size_t)(2 * k) * sizeof(mlf<N>), s>>>(k, d, e, out, status);
+    tridiag_min_kernel<N><<<1, 32, (size_t)(2 * k) * sizeof(mlf<N>), s>>>(k, d, e, out, status, gate);
     SDPG_CHECK_LAUNCH();
+}
+
+// ---- Lanczos steps under device control (the loop of Lal::getMinEigen,
+// sdpa_linear.cpp:27-124, without a host round trip per step) ----
+//
+// Per run: slots sl[0] 1/beta, sl[1] beta, sl[4..5] the tridiagonal solver's output
+// (lambda, z), sl[6] r.r, sl[8] min, sl[9] min_old, sl[10] error; ctl[0] = 1 while the
+// run goes on, ctl[1] = steps done.  Every kernel of a step returns at once when ctl[0]
+// is 0, so the host can enqueue several steps ahead and read the state once.
+
+template <int N>
+__global__ void lz_next_kernel(int n, const mlf<N> *r, const mlf<N> *sl, mlf<N> *q, mlf<N> *qold, const int *ctl) {
+    if (!ctl[0]) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    qold[i] = q[i];
+    q[i] = ml_mul(r[i], sl[0]);  // q = r / beta
+}
+
+// The loop control after step k: the new beta from r.r, the Ritz value of an eigenvalue
+// step, and the loop condition for step k + 1 (Lal::getMinEigen's while test).
+template <int N>
+__device__ void lz_control(mlf<N> *sl, mlf<N> *te, int *ctl, int k, int eig, int n, int kgo, int kmax) {
+    if (eig) {
+        sl[9] = sl[8];
+        sl[8] = sl[4];
+        sl[10] = sl[5];
+    }
+    const mlf<N> beta = ml_sqrt(sl[6]);
+    te[k] = beta;
+    sl[1] = beta;
+    sl[0] = ml_is_zero(beta) ? ml_zero<N>() : ml_div(ml_one<N>(), beta);
+    ctl[1] = k + 1;
+    const int kn = k + 1;
+    const mlf<N> mn = sl[8], mo = sl[9], er = sl[10];
+    bool go = kn < n && kn < kgo && ml_cmp(beta, ml_from_double<N>(1.0e-16)) > 0;
+    if (go) {
+        const mlf<N> amin = ml_abs(mn);
+        const bool c1 = ml_cmp(ml_abs(ml_sub(mn, mo)),
+                               ml_add(ml_mul(ml_from_double<N>(1.0e-5), amin), ml_from_double<N>(1.0e-8))) > 0;
+        const bool c2 = ml_cmp(ml_abs(ml_mul(er, beta)),
+                               ml_add(ml_mul(ml_from_double<N>(1.0e-2), amin), ml_from_double<N>(1.0e-4))) > 0;
+        go = c1 || c2;
+    }
+    if (kn + 1 >= kmax) go = false;
+    ctl[0] = go ? 1 : 0;
+}
+
+// alpha = q.w (into the tridiagonal's diagonal td[k]), r = (w - alpha q) - beta qold, and
+// r.r in one CTA of 256 threads (the strided pairs and block sum of the dot kernel);
+// without an eigenvalue solve at this step also the loop control.
+template <int N>
+__global__ void __launch_bounds__(256) lz_update_kernel(int n, const mlf<N> *w, const mlf<N> *q, const mlf<N> *qold,
+                                                        mlf<N> *td, mlf<N> *te, mlf<N> *sl, mlf<N> *r, int *ctl,
+                                                        int k, int eig, int kgo, int kmax) {
+    __shared__ mlf<N> alpha_s;
+    if (!ctl[0]) return;
+    const int stride = blockDim.x;
+    mlf<N> a0 = ml_zero<N>(), a1 = ml_zero<N>();
+    int i = threadIdx.x;
+    for (; i + stride < n; i += 2 * stride) {
+        a0 = ml_add(a0, ml_mul(q[i], w[i]));
+        a1 = ml_add(a1, ml_mul(q[i + stride], w[i + stride]));
+    }
+    if (i < n) a0 = ml_add(a0, ml_mul(q[i], w[i]));
+    const mlf<N> alpha = ml_block_sum(ml_add(a0, a1));
+    if (threadIdx.x == 0) {
+        alpha_s = alpha;
+        td[k] = alpha;
+    }
+    __syncthreads();
+    const mlf<N> al = alpha_s, be = sl[1];
+    for (int j = threadIdx.x; j < n; j += stride) r[j] = ml_sub(ml_sub(w[j], ml_mul(q[j], al)), ml_mul(qold[j], be));
+    __syncthreads();
+    a0 = ml_zero<N>();
+    a1 = ml_zero<N>();
+    i = threadIdx.x;
+    for (; i + stride < n; i += 2 * stride) {
+        a0 = ml_add(a0, ml_mul(r[i], r[i]));
+        a1 = ml_add(a1, ml_mul(r[i + stride], r[i + stride]));
+    }
+    if (i < n) a0 = ml_add(a0, ml_mul(r[i], r[i]));
+    const mlf<N> rr = ml_block_sum(ml_add(a0, a1));
+    if (threadIdx.x == 0) {
+        sl[6] = rr;
+        if (!eig) lz_control(sl, te, ctl, k, 0, n, kgo, kmax);
+    }
+}
+
+template <int N>
+__global__ void lz_control_kernel(mlf<N> *sl, mlf<N> *te, int *ctl, int k, int n, int kgo, int kmax) {
+    if (!ctl[0]) return;
+    lz_control(sl, te, ctl, k, 1, n, kgo, kmax);
+}
+
+template <int N>
+void k_lanczos_step(int n, const mlf<N> *M, mlf<N> *r, mlf<N> *q, mlf<N> *qold, mlf<N> *w, mlf<N> *td, mlf<N> *te,
+                    mlf<N> *sl, int *ctl, int *status, int k, int eig, int kgo, int kmax, cudaStream_t s) {
+    lz_next_kernel<N><<<ceil_div(n, 128), 128, 0, s>>>(n, r, sl, q, qold, ctl);
+    SDPG_CHECK_LAUNCH();
+    if (n >= 128) {
+        matvec_t_split_kernel<N><<<ceil_div(n, kWarpsPerBlock / kMvSplit), 32 * kWarpsPerBlock, 0, s>>>(n, M, 0, q, w,
+                                                                                                   ctl);
+    } else {
+        matvec_t_kernel<N><<<ceil_div(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(n, M, 0, q, w, ctl);
+    }
+    SDPG_CHECK_LAUNCH();
+    lz_update_kernel<N><<<1, 256, 0, s>>>(n, w, q, qold, td, te, sl, r, ctl, k, eig, kgo, kmax);
+    SDPG_CHECK_LAUNCH();
+    if (eig) {
+        k_tridiag_min<N>(k + 1, td, te, sl + 4, status, s, ctl);
+        lz_control_kernel<N><<<1, 1, 0, s>>>(sl, te, ctl, k, n, kgo, kmax);
+        SDPG_CHECK_LAUNCH();
+    }
 }
 
 // The LP rule of Jal::getMinEigen (sdpa_jordan.cpp:79-85): min over k of
@@ -472,7 +591,10 @@ void k_tridiagonalize_small(int n, mlf<N> *A, mlf<N> *d, mlf<N> *e, cudaStream_t
     template void k_lanczos_update<N>(int, const mlf<N> *, const mlf<N> *, const mlf<N> *, const mlf<N> *, \
                                       const mlf<N> *, mlf<N> *, cudaStream_t);                            \
     template void k_lanczos_next<N>(int, const mlf<N> *, const mlf<N> *, mlf<N> *, mlf<N> *, cudaStream_t); \
-    template void k_tridiag_min<N>(int, const mlf<N> *, const mlf<N> *, mlf<N> *, int *, cudaStream_t);  \
+    template void k_tridiag_min<N>(int, const mlf<N> *, const mlf<N> *, mlf<N> *, int *, cudaStream_t,     \
+                                   const int *);                                                          \
+    template void k_lanczos_step<N>(int, const mlf<N> *, mlf<N> *, mlf<N> *, mlf<N> *, mlf<N> *, mlf<N> *, \
+                                    mlf<N> *, mlf<N> *, int *, int *, int, int, int, int, cudaStream_t);   \
     template void k_tridiagonalize_small<N>(int, mlf<N> *, mlf<N> *, mlf<N> *, cudaStream_t);              \
     template void k_lp_ratio_min<N>(int, const mlf<N> *, const mlf<N> *, mlf<N> *, cudaStream_t);
 SDPG_INST_EIG(8)

@@ -134,7 +134,17 @@ void k_lanczos_next(int n, const mlf<N> *r, const mlf<N> *beta, mlf<N> *q, mlf<N
 // Smallest eigenvalue of the symmetric tridiagonal (diag d[0..k-1], offdiag e[0..k-2]) and
 // the last component of its unit eigenvector (sign arbitrary): out[0] = lambda, out[1] = z_{k-1}.
 template <int N>
-void k_tridiag_min(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *status, cudaStream_t s);
+void k_tridiag_min(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *status, cudaStream_t s,
+                   const int *gate = nullptr);
+// One Lanczos step k on the operator M (its columns read as rows) under device control:
+// q = r / beta, w = M q, alpha = q.w -> td[k], r = w - alpha q - beta qold, beta' =
+// sqrt(r.r) -> te[k], with the tridiagonal eigenvalue solve when `eig`, then the loop
+// test for step k + 1 (k + 1 < n, k + 1 < kgo, beta' > 1e-16, the Ritz value or its
+// error bound still moving, k + 2 < kmax).  Slots and flags in sl / ctl as described in
+// eig.cu; every kernel of the step does nothing once ctl[0] is 0.
+template <int N>
+void k_lanczos_step(int n, const mlf<N> *M, mlf<N> *r, mlf<N> *q, mlf<N> *qold, mlf<N> *w, mlf<N> *td, mlf<N> *te,
+                    mlf<N> *sl, int *ctl, int *status, int k, int eig, int kgo, int kmax, cudaStream_t s);
 // Householder tridiagonalisation of a dense symmetric n x n (n <= 64) in place; writes
 // d[0..n-1], e[0..n-2].  (Rsytrd 'L', the first stage of Rsyev.)
 template <int N>

@@ -47,6 +47,7 @@ class Solver final : public SolverBase {
         // Lanczos vectors and tridiagonal storage, one set per side (0: X, 1: Z)
         V *q[2], *qold[2], *r[2], *w[2], *tmp[2], *td[2], *te[2], *sl[2];
         V *Mop[2] = {nullptr, nullptr}, *Mtmp[2] = {nullptr, nullptr};  // L X L^T of a Lanczos run (n > 20)
+        int *lzctl[2] = {nullptr, nullptr};  // device loop flags of a Lanczos run: [0] going on, [1] steps done
         V *SW1 = nullptr, *SW2 = nullptr;  // Z-side work matrices of the small-block eigenvalue path
         BlockDev<N> cons;
         std::vector<int> f1_owners_h;
@@ -365,7 +366,8 @@ class Solver final : public SolverBase {
                 B.tmp[side] = dalloc(n);
                 B.td[side] = dalloc(std::max(B.lanczos_kmax, n) + 2);
                 B.te[side] = dalloc(std::max(B.lanczos_kmax, n) + 2);
-                B.sl[side] = dalloc(8);
+                B.sl[side] = dalloc(16);
+                B.lzctl[side] = (int *)dalloc_raw(16);
             }
             if (B.lp) {
                 // no eigenvalue work space: the LP rule reads the diagonals
@@ -786,110 +788,104 @@ class Solver final : public SolverBase {
     // ---------------------------------------------------------------- eigenvalues (sdpa_jordan.cpp, sdpa_linear.cpp)
 
     // One Lanczos run (Lal::getMinEigen, sdpa_linear.cpp:27-124) on L Xm L^T for one block
-    // and side; the host keeps the reference's loop control, the device does the rest.
+    // and side.  The steps and the loop test run on the device (k_lanczos_step); the host
+    // enqueues a few steps ahead and reads the loop flags once per batch.
     struct Lz {
         Blk *B;
-        int side, n, k, kk;
+        int side, n, k, kgo;
         V *L, *Xm, *Lt;
         cudaStream_t st;
         Workspace *ws;
-        V *hp;  // 8 pinned slots: 0 rb, 1 beta, 2 te[k], 4 lambda, 5 z, 6 r.r
-        R min, min_old, error, beta, sq_n, sq_n9;
-        bool active, issued, eig;
+        V *hp;  // 16 pinned slots: the run's state slots, flags at 12
+        R min, error, beta;
+        std::vector<int> eig;  // steps with a tridiagonal eigenvalue solve
+        bool active;
     };
+    static constexpr int kLanczosBatch = 4;
 
-    void lanczos_issue(Lz &t) {
-        Blk &B = *t.B;
-        const int n = t.n, s = t.side;
-        V *sl = B.sl[s];
-        t.hp[0] = (R(1) / t.beta).v;  // value = MONE / beta
-        t.hp[1] = t.beta.v;
-        h2d_ += 2 * (long long)sizeof(V);
-        SDPG_CUDA(cudaMemcpyAsync(sl + 0, t.hp + 0, 2 * sizeof(V), cudaMemcpyHostToDevice, t.st));
-        k_lanczos_next<N>(n, B.r[s], sl + 0, B.q[s], B.qold[s], t.st);  // qold = q; q = r / beta
-        k_matvec<N>(n, B.Mop[s], 'T', 0, B.q[s], B.w[s], t.st);         // w = (L X L^T) q
-        {
-            const size_t mark = t.ws->used;
-            k_dot<N>(n, B.q[s], B.w[s], B.td[s] + t.k, *t.ws, t.st);  // alpha = q . w -> diagVec[k]
-            t.ws->used = mark;
-        }
-        k_lanczos_update<N>(n, B.w[s], B.q[s], B.qold[s], B.td[s] + t.k, sl + 1, B.r[s], t.st);
-        t.eig = R(t.kk) >= rsqrt_(R(t.k)) || t.k == n - 1 || R(t.k) > t.sq_n9;
-        if (t.eig) {
-            t.kk = 0;
-            k_tridiag_min<N>(t.k + 1, B.td[s], B.te[s], sl + 4, status_, t.st);
-        }
-        {
-            const size_t mark = t.ws->used;
-            k_dot<N>(n, B.r[s], B.r[s], sl + 6, *t.ws, t.st);  // value = r . r
-            t.ws->used = mark;
-        }
-        d2h_ += 3 * (long long)sizeof(V);
-        SDPG_CUDA(cudaMemcpyAsync(t.hp + 4, sl + 4, 3 * sizeof(V), cudaMemcpyDeviceToHost, t.st));
-        t.issued = true;
-    }
-
-    void lanczos_finish_step(Lz &t) {
-        Blk &B = *t.B;
-        if (t.eig) {
-            t.min_old = t.min;
-            t.min = R(t.hp[4]);
-            t.error = R(t.hp[5]);
-        }
-        t.beta = rsqrt_(R(t.hp[6]));
-        t.hp[2] = t.beta.v;
-        h2d_ += (long long)sizeof(V);
-        SDPG_CUDA(cudaMemcpyAsync(B.te[t.side] + t.k, t.hp + 2, sizeof(V), cudaMemcpyHostToDevice, t.st));  // diagVec2[k]
-        ++t.k;
-        ++t.kk;
-        t.issued = false;
-    }
-
-    // all Lanczos runs advance in lockstep: one host synchronisation per step for all of them
+    // all runs advance together: one host synchronisation per batch of steps for all of them
     void lanczos_all(std::vector<Lz> &T) {
-        if (8 * T.size() > (size_t)kPinned - 4) throw sdpg_error(SDPG_ERR_TOO_LARGE, "too many Lanczos runs at once");
+        if (16 * T.size() > (size_t)kPinned - 4) throw sdpg_error(SDPG_ERR_TOO_LARGE, "too many Lanczos runs at once");
         for (size_t i = 0; i < T.size(); ++i) {
             Lz &t = T[i];
             Blk &B = *t.B;
-            t.hp = pinned_ + 8 * i;
+            const int s = t.side;
+            t.hp = pinned_ + 16 * i;
             // the Lanczos operator L X L^T, formed once per run (symmetric up to rounding;
             // its columns are read as rows)
-            mm_on(t.st, *t.ws, t.n, B.Mtmp[t.side], t.Xm, 'N', t.L, 'T');
-            mm_on(t.st, *t.ws, t.n, B.Mop[t.side], t.L, 'N', B.Mtmp[t.side], 'N');
-            k_fill<N>(t.n, B.r[t.side], ml_one<N>(), t.st);
-            SDPG_CUDA(cudaMemsetAsync(B.q[t.side], 0, t.n * sizeof(V), t.st));
-            t.min = R(1.0e+51);
-            t.min_old = R(1.0e+52);
-            t.error = R(1.0e+10);
-            t.beta = rsqrt_(R(t.n));  // norm of r
-            t.sq_n = t.beta;
-            t.sq_n9 = rsqrt_(R(t.n) + R(9));
-            t.k = t.kk = 0;
-            t.active = true;
-            t.issued = false;
+            mm_on(t.st, *t.ws, t.n, B.Mtmp[s], t.Xm, 'N', t.L, 'T');
+            mm_on(t.st, *t.ws, t.n, B.Mop[s], t.L, 'N', B.Mtmp[s], 'N');
+            k_fill<N>(t.n, B.r[s], ml_one<N>(), t.st);
+            SDPG_CUDA(cudaMemsetAsync(B.q[s], 0, t.n * sizeof(V), t.st));
+            // the loop's initial state (sdpa_linear.cpp:33-56): r = 1, beta = |r|,
+            // min = 1e51, min_old = 1e52, error = 1e10
+            const R beta = rsqrt_(R(t.n));
+            const R sq_n = beta, sq_n9 = rsqrt_(R(t.n) + R(9));
+            for (int q = 0; q < 12; ++q) t.hp[q] = ml_zero<N>();
+            t.hp[0] = (R(1) / beta).v;
+            t.hp[1] = beta.v;
+            t.hp[8] = R(1.0e+51).v;
+            t.hp[9] = R(1.0e+52).v;
+            t.hp[10] = R(1.0e+10).v;
+            int *flags = reinterpret_cast<int *>(t.hp + 12);
+            flags[0] = 1;
+            flags[1] = 0;
+            h2d_ += 12 * (long long)sizeof(V) + 2 * (long long)sizeof(int);
+            SDPG_CUDA(cudaMemcpyAsync(B.sl[s], t.hp, 12 * sizeof(V), cudaMemcpyHostToDevice, t.st));
+            SDPG_CUDA(cudaMemcpyAsync(B.lzctl[s], flags, 2 * sizeof(int), cudaMemcpyHostToDevice, t.st));
+            // the loop bound k < sqrt(n) + 10 as a step count, and the static schedule of
+            // the eigenvalue solves (kk >= sqrt(k) || k == n - 1 || k > sqrt(n + 9))
+            t.kgo = 0;
+            while (R(t.kgo) < sq_n + R(10)) ++t.kgo;
+            const int kmax = B.lanczos_kmax;
+            t.eig.assign(kmax + 1, 0);
+            int kk = 0;
+            for (int k = 0; k <= kmax; ++k, ++kk) {
+                t.eig[k] = (R(kk) >= rsqrt_(R(k)) || k == t.n - 1 || R(k) > sq_n9) ? 1 : 0;
+                if (t.eig[k]) kk = 0;
+            }
+            t.k = 0;
+            t.active = t.n > 0 && kmax > 1;
         }
+        // (the pinned slots are next written by stream-ordered copies, after the uploads)
         while (true) {
             bool any = false;
             for (Lz &t : T) {
                 if (!t.active) continue;
-                const bool go = t.k < t.n && R(t.k) < t.sq_n + R(10) && t.beta > R(1.0e-16) &&
-                                (rabs(t.min - t.min_old) > R(1.0e-5) * rabs(t.min) + R(1.0e-8) ||
-                                 rabs(t.error * t.beta) > R(1.0e-2) * rabs(t.min) + R(1.0e-4));
-                if (!go || t.k + 1 >= t.B->lanczos_kmax) {
-                    t.active = false;
-                    continue;
+                Blk &B = *t.B;
+                const int s = t.side;
+                for (int b = 0; b < kLanczosBatch; ++b) {
+                    const int k = t.k + b;
+                    if (k >= t.n || k + 1 >= B.lanczos_kmax) break;
+                    k_lanczos_step<N>(t.n, B.Mop[s], B.r[s], B.q[s], B.qold[s], B.w[s], B.td[s], B.te[s], B.sl[s],
+                                      B.lzctl[s], status_, k, t.eig[k], t.kgo, B.lanczos_kmax, t.st);
                 }
-                lanczos_issue(t);
+                int *flags = reinterpret_cast<int *>(t.hp + 12);
+                d2h_ += 2 * (long long)sizeof(int);
+                SDPG_CUDA(cudaMemcpyAsync(flags, B.lzctl[s], 2 * sizeof(int), cudaMemcpyDeviceToHost, t.st));
                 any = true;
             }
             if (!any) break;
             SDPG_CUDA(cudaStreamSynchronize(st_));
             SDPG_CUDA(cudaStreamSynchronize(st2_));
-            for (Lz &t : T)
-                if (t.issued) lanczos_finish_step(t);
+            for (Lz &t : T) {
+                if (!t.active) continue;
+                const int *flags = reinterpret_cast<const int *>(t.hp + 12);
+                t.k = flags[1];
+                if (!flags[0] || t.k >= t.n || t.k + 1 >= t.B->lanczos_kmax) t.active = false;
+            }
+        }
+        for (Lz &t : T) {
+            d2h_ += 11 * (long long)sizeof(V);
+            SDPG_CUDA(cudaMemcpyAsync(t.hp, t.B->sl[t.side], 11 * sizeof(V), cudaMemcpyDeviceToHost, t.st));
         }
         SDPG_CUDA(cudaStreamSynchronize(st_));
         SDPG_CUDA(cudaStreamSynchronize(st2_));
+        for (Lz &t : T) {
+            t.beta = R(t.hp[1]);
+            t.min = R(t.hp[8]);
+            t.error = R(t.hp[10]);
+        }
     }
 
     // Lal::getMinEigenValue on L*X*L^T for blocks of size <= 20 (sdpa_jordan.cpp:63-68):
