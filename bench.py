@@ -43,7 +43,7 @@ UNIT = "iters/s"
 RESIDUE_MODULI = 70  # primes of the 256-bit residue GEMM (csrc/crt_tables.h)
 # DRAM bytes (read + write) per launch of tc_modgemm_kernel for a 500^3 product, from
 # the ncu capture summarised in profiles/tc_modgemm_kernel_gemm500_256bit.md
-TC_TRAFFIC_BYTES = 83.0e6
+TC_TRAFFIC_BYTES = 81.8e6
 
 
 def workload(precision: int):
