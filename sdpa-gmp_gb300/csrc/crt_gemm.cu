@@ -27,6 +27,7 @@ namespace sdpg {
 namespace {
 
 __constant__ int c_moduli[kCrtL];
+__constant__ float c_minv[kCrtL];  // 1.0f / m_l, correctly rounded (as the division would give)
 __constant__ int c_pow16[kCrtL][kCrtPowChunks];
 __constant__ uint32_t c_inv[kCrtL][kCrtInvWords];
 __constant__ uint32_t c_mtot[8];
@@ -48,6 +49,9 @@ CrtDevice crt_device() {
     std::lock_guard<std::mutex> lock(mu);
     if (!ready[dev]) {
         SDPG_CUDA(cudaMemcpyToSymbol(c_moduli, kCrtModuli, sizeof(kCrtModuli)));
+        float minv[kCrtL];
+        for (int l = 0; l < kCrtL; ++l) minv[l] = 1.0f / (float)kCrtModuli[l];
+        SDPG_CUDA(cudaMemcpyToSymbol(c_minv, minv, sizeof(minv)));
         SDPG_CUDA(cudaMemcpyToSymbol(c_pow16, kCrtPow16, sizeof(kCrtPow16)));
         SDPG_CUDA(cudaMemcpyToSymbol(c_inv, kCrtInv, sizeof(kCrtInv)));
         SDPG_CUDA(cudaMemcpyToSymbol(c_mtot, kCrtMtotMant, sizeof(kCrtMtotMant)));
@@ -152,7 +156,7 @@ __global__ void __launch_bounds__(256) crt_residue_kernel(CrtOperands<N> ops, in
         int acc = 0;  // < 18 * 65535 * 511 < 2^31
 #pragma unroll
         for (int c = 0; c < kCrtPowChunks; ++c) acc += (int)chunk[c] * c_pow16[l][c];
-        int r = acc - (int)((float)acc * (1.0f / (float)m)) * m;
+        int r = acc - (int)((float)acc * c_minv[l]) * m;
         if (r < 0) r += m;
         if (r >= m) r -= m;
         if (2 * r > m) r -= m;  // balanced: |r| <= (m - 1) / 2
