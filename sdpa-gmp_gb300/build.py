@@ -2,7 +2,9 @@
 
 Every ``csrc/*.cu`` translation unit is compiled in parallel into
 ``_build/`` and linked into ``sdpa-gmp_gb300/libsdpg.so``.  Only one
-``-gencode`` (compute_103a / sm_103a) is emitted.
+``-gencode`` (compute_103a / sm_103a) is emitted.  The command-line driver
+``sdpa-gmp_gb300/sdpa_gmp_gb300`` (``cli/sdpa_gmp_gb300.cpp``) is linked
+against it with g++.
 """
 from __future__ import annotations
 

@@ -97,24 +97,6 @@ __global__ void matvec_n_kernel(int n, const mlf<N> *A, int tri, const mlf<N> *x
     if (lane == 0) y[o] = acc;
 }
 
-template <int N>
-__global__ void lanczos_update_kernel(int n, const mlf<N> *w, const mlf<N> *q, const mlf<N> *qold,
-                                      const mlf<N> *alpha, const mlf<N> *beta, mlf<N> *r) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    // r = w - q*alpha; r = r - qold*beta   (Lal::let(r,'=',w,'-',q,&alpha) then (r,'-',qold,&beta))
-    mlf<N> t = ml_sub(w[i], ml_mul(q[i], *alpha));
-    r[i] = ml_sub(t, ml_mul(qold[i], *beta));
-}
-
-template <int N>
-__global__ void lanczos_next_kernel(int n, const mlf<N> *r, const mlf<N> *rbeta, mlf<N> *q, mlf<N> *qold) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    qold[i] = q[i];
-    q[i] = ml_mul(r[i], *rbeta);
-}
-
 // Number of eigenvalues of the (scaled, single-precision) tridiagonal below x: the
 // negative pivots of the LDL^T factorisation of T - x I (Sturm sequence).
 __device__ int sturm_count_f(int k, const float *d, const float *e2, float x) {
@@ -397,19 +379,6 @@ void k_matvec(int n, const mlf<N> *A, char op, int tri, const mlf<N> *x, mlf<N> 
 }
 
 template <int N>
-void k_lanczos_update(int n, const mlf<N> *w, const mlf<N> *q, const mlf<N> *qold, const mlf<N> *alpha,
-                      const mlf<N> *beta, mlf<N> *r, cudaStream_t s) {
-    lanczos_update_kernel<N><<<ceil_div(n, 128), 128, 0, s>>>(n, w, q, qold, alpha, beta, r);
-    SDPG_CHECK_LAUNCH();
-}
-
-template <int N>
-void k_lanczos_next(int n, const mlf<N> *r, const mlf<N> *beta, mlf<N> *q, mlf<N> *qold, cudaStream_t s) {
-    lanczos_next_kernel<N><<<ceil_div(n, 128), 128, 0, s>>>(n, r, beta, q, qold);
-    SDPG_CHECK_LAUNCH();
-}
-
-template <int N>
 void k_tridiag_min(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *status, cudaStream_t s, const int *gate) {
     if (k > kMaxTri) throw sdpg_error(SDPG_ERR_TOO_LARGE, "tridiagonal larger than 512");
     static std::once_flag once;
@@ -588,9 +557,6 @@ void k_tridiagonalize_small(int n, mlf<N> *A, mlf<N> *d, mlf<N> *e, cudaStream_t
 
 #define SDPG_INST_EIG(N)                                                                                  \
     template void k_matvec<N>(int, const mlf<N> *, char, int, const mlf<N> *, mlf<N> *, cudaStream_t);   \
-    template void k_lanczos_update<N>(int, const mlf<N> *, const mlf<N> *, const mlf<N> *, const mlf<N> *, \
-                                      const mlf<N> *, mlf<N> *, cudaStream_t);                            \
-    template void k_lanczos_next<N>(int, const mlf<N> *, const mlf<N> *, mlf<N> *, mlf<N> *, cudaStream_t); \
     template void k_tridiag_min<N>(int, const mlf<N> *, const mlf<N> *, mlf<N> *, int *, cudaStream_t,     \
                                    const int *);                                                          \
     template void k_lanczos_step<N>(int, const mlf<N> *, mlf<N> *, mlf<N> *, mlf<N> *, mlf<N> *, mlf<N> *, \

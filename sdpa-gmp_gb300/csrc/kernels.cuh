@@ -124,13 +124,6 @@ int *ml_potrs_status(int n, mlf<N> *Dinv);
 template <int N>
 void k_matvec(int n, const mlf<N> *A, char op, int tri, const mlf<N> *x, mlf<N> *y, cudaStream_t s);
 // r = w - alpha*q - beta*qold (alpha, beta device scalars); also writes dots:
-// out[0] = q.w must be computed before (k_dot); after this, out2 = r.r
-template <int N>
-void k_lanczos_update(int n, const mlf<N> *w, const mlf<N> *q, const mlf<N> *qold, const mlf<N> *alpha,
-                      const mlf<N> *beta, mlf<N> *r, cudaStream_t s);
-// q = r / beta (device scalar), qold = previous q
-template <int N>
-void k_lanczos_next(int n, const mlf<N> *r, const mlf<N> *beta, mlf<N> *q, mlf<N> *qold, cudaStream_t s);
 // Smallest eigenvalue of the symmetric tridiagonal (diag d[0..k-1], offdiag e[0..k-2]) and
 // the last component of its unit eigenvector (sign arbitrary): out[0] = lambda, out[1] = z_{k-1}.
 template <int N>
