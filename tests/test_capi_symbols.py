@@ -28,3 +28,12 @@ def test_exports(sdpg):
     exported = set(re.findall(r" T (sdpg_[a-z0-9_]+)", out))
     assert declared <= exported, sorted(declared - exported)
     assert lib.sdpg_version() == 100
+
+
+def test_command_line_driver_usage(sdpg):
+    """The driver is built with the library and answers a call without data (no GPU use)."""
+    exe = os.path.join(os.path.dirname(sdpg.LIB_PATH), "sdpa_gmp_gb300")
+    assert os.path.exists(exe)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
+    assert "usage:" in r.stderr and "-ds" in r.stderr and "-is" in r.stderr
