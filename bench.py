@@ -364,7 +364,7 @@ def bench_reference(args) -> None:
 
 
 def bench_batch(args) -> None:
-    """Batched mode (cfg4 shape): control/LMI instances with m ~ U[20, 350] and two
+    """Batched mode: control/LMI instances with m ~ U[20, 350] and two
     blocks of sizes ~ U[15, 90] (seeds 0 .. batch-1) solved by sdpg_solve_batch with
     --concurrency solvers in flight, against the same solver run one problem at a time
     on the first --serial instances; prints solves/s for both."""
@@ -404,7 +404,7 @@ def bench_batch(args) -> None:
 
 
 def bench_learned(args) -> None:
-    """Learned mode (cfg5 family): the committed lambdaStar / beta policy against the
+    """Learned mode (signed MaxCut, n = 124): the committed lambdaStar / beta policy against the
     default parameters on held-out MaxCut instances (n = 124, p ~ U[0.02, 0.2], edge
     weights +-1); prints mean iterations of both and the largest objective difference
     from the default solve, which judges the learned path's error."""
