@@ -83,6 +83,10 @@ int sdpg_ml_host_op(int limbs, int op, long long n, const void *a, const void *b
  * (sdpa_linear.cpp:856-875).  transa/transb: 'N' or 'T'. */
 int sdpg_rgemm(int limbs, char transa, char transb, int m, int n, int k, const void *alpha, const void *A,
                int lda, const void *B, int ldb, const void *beta, void *C, int ldc);
+/* Scratch: the library keeps one device workspace per (calling host thread, current
+ * device, stream) and grows it on demand (cudaMalloc / cudaFree, which wait for the
+ * device).  Calls on one stream reuse it in stream order; calls on different streams
+ * or devices, or from different threads, never share scratch. */
 int sdpg_rgemm_device(int limbs, char transa, char transb, int m, int n, int k, const void *alpha,
                       const void *A, int lda, const void *B, int ldb, const void *beta, void *C, int ldc,
                       void *stream);
@@ -224,7 +228,10 @@ unsigned long long sdpg_launch_count(void);
  * Returns the previous method.  Both paths meet the same error bound. */
 int sdpg_set_gemm_method(int method);
 /* *flag = non-zero if a tensor-core GEMM kernel on `device` ever gave up a bounded wait
- * (its results are then invalid); solvers check it every iteration. */
+ * (its results are then invalid).  The flag is sticky: it is never cleared, for the life
+ * of the process.  Each solver also has its own word, cleared when it is created and
+ * checked every iteration (a time-out there fails that solver with SDPG_ERR_TIMEOUT,
+ * not the other solvers on the device). */
 int sdpg_tensor_error(int device, int *flag);
 /* Measured throughput of signed 32x32->64 multiply-adds (IMAD.WIDE) on one GPU, the
  * instruction the multi-limb GEMM is built from; the plain path's roofline denominator. */

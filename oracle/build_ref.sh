@@ -16,10 +16,11 @@
 #   * libgmpxx's stream inserters come from oracle/gmpxx_streams.cpp.
 # Flags follow Makefile.am:56 (-O2 -fopenmp -DUseMETIS=0) minus -march=native.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_DIR]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_DIR]
+#   (default: $SDPG_REFERENCE_DIR, else /root/reference)
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${SDPG_REFERENCE_DIR:-/root/reference}}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/sdpa_main.cpp" ]; then
     echo "build_ref: reference sources not found at $REF" >&2

@@ -181,7 +181,7 @@ int sdpg_rgemm_device(int limbs, char transa, char transb, int m, int n, int k, 
             memcpy(&p.beta, beta, sizeof(mlf<N>));
             p.lower_only = 0;
             if (m == 0 || n == 0) return (int)SDPG_OK;
-            Workspace &ws = thread_workspace();
+            Workspace &ws = thread_workspace((cudaStream_t)stream);
             ws.reset();
             ws.reserve(gemm_workspace_bytes(p) + 512);
             ml_gemm<N>(p, ws, (cudaStream_t)stream);
@@ -240,7 +240,7 @@ int sdpg_rpotrf(int limbs, int n, void *A, int lda, int *info) {
             constexpr int N = decltype(tag)::value;
             DeviceBuffer dinfo(sizeof(int));
             int rc = with_device_copy(limbs, (size_t)lda * n, A, true, A, [&](void *dA) {
-                Workspace &ws = thread_workspace();
+                Workspace &ws = thread_workspace(nullptr);
                 ws.reset();
                 GemmProblem<N> p{};
                 p.M = n;
@@ -264,7 +264,7 @@ int sdpg_inv_lower(int limbs, int n, const void *L, int ldl, void *Linv) {
             constexpr int N = decltype(tag)::value;
             DeviceBuffer dout((size_t)n * n * sizeof(mlf<N>));
             int rc = with_device_copy(limbs, (size_t)ldl * n, L, false, nullptr, [&](void *dL) {
-                Workspace &ws = thread_workspace();
+                Workspace &ws = thread_workspace(nullptr);
                 ws.reset();
                 ws.reserve(ml_trtri_workspace_bytes<N>(n) + (1 << 20));
                 ml_trtri_lower<N>(n, (const mlf<N> *)dL, ldl, (mlf<N> *)dout.p, ws, nullptr);
@@ -284,7 +284,7 @@ int sdpg_solve_systems(int limbs, int n, const void *L, int ldl, void *x) {
             DeviceBuffer dx((size_t)n * sizeof(mlf<N>));
             SDPG_CUDA(cudaMemcpy(dx.p, x, (size_t)n * sizeof(mlf<N>), cudaMemcpyHostToDevice));
             int rc = with_device_copy(limbs, (size_t)ldl * n, L, false, nullptr, [&](void *dL) {
-                Workspace &ws = thread_workspace();
+                Workspace &ws = thread_workspace(nullptr);
                 ws.reset();
                 ws.reserve(ml_potrs_prepare_bytes<N>(n) + (1 << 20));
                 mlf<N> *Dinv = (mlf<N> *)ws.carve(ml_potrs_prepare_bytes<N>(n));

@@ -1,8 +1,10 @@
 // Helpers shared by the C-ABI translation units: exception-to-error-code
 // guard, limb-count dispatch, RAII device buffers and a per-thread workspace.
 #pragma once
+#include <memory>
 #include <string>
 #include <type_traits>
+#include <vector>
 
 #include "common.cuh"
 
@@ -53,9 +55,34 @@ struct DeviceBuffer {
     }
 };
 
-inline Workspace &thread_workspace() {
-    thread_local Workspace ws;
-    return ws;
+// Scratch of the standalone entry points: one workspace per (host thread, current
+// device, stream).  Calls on one stream are ordered by that stream, so they can reuse
+// its workspace; calls on other streams or devices get workspaces of their own, so no
+// two calls that may overlap on the GPU share scratch.  Workspaces are plain cudaMalloc
+// memory (freed with cudaFree, which waits for the device), and a thread that has used
+// more than kMaxWorkspaces (device, stream) pairs releases them all before going on.
+inline Workspace &thread_workspace(cudaStream_t stream) {
+    constexpr size_t kMaxWorkspaces = 16;
+    struct Entry {
+        int device;
+        cudaStream_t stream;
+        std::unique_ptr<Workspace> ws;
+    };
+    thread_local std::vector<Entry> table;
+    int dev = 0;
+    SDPG_CUDA(cudaGetDevice(&dev));
+    for (auto &e : table)
+        if (e.device == dev && e.stream == stream) return *e.ws;
+    if (table.size() >= kMaxWorkspaces) {
+        for (auto &e : table) {
+            SDPG_CUDA(cudaSetDevice(e.device));
+            e.ws->release();
+        }
+        table.clear();
+        SDPG_CUDA(cudaSetDevice(dev));
+    }
+    table.push_back(Entry{dev, stream, std::unique_ptr<Workspace>(new Workspace())});
+    return *table.back().ws;
 }
 
 }  // namespace sdpg

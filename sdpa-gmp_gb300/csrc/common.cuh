@@ -45,6 +45,9 @@ struct Workspace {
     size_t cap = 0;
     size_t used = 0;
     cudaStream_t stream = nullptr;
+    // device word that tensor-core GEMMs run out of this workspace set when one of their
+    // bounded waits gives up (null: only the device-wide flag of crt_error_word())
+    int *error = nullptr;
     ~Workspace() { release(); }
     void release() {
         if (base) {

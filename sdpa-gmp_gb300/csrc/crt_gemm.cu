@@ -367,7 +367,8 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
             t.kpitch = L.Kpad;
             t.lower_only = p.lower_only;
             t.moduli = dev.moduli;
-            t.error = dev.error;
+            t.error = p.error ? p.error : dev.error;
+            t.sticky = dev.error;
             if (p.ev_before) SDPG_CUDA(cudaEventRecord(p.ev_before, s));
             // K beyond the tensor memory's four exact accumulators runs in chunks whose
             // residues are added modulo each prime in the epilogue
@@ -385,7 +386,7 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
     }
 }
 
-// device word set by the tensor-core kernel when one of its bounded waits timed out
+// device-wide sticky word: set by every tensor-core kernel that gave up a bounded wait
 int *crt_error_word() { return crt_device().error; }
 
 template bool crt_gemm_applies<8>(const GemmProblem<8> &);

@@ -327,7 +327,13 @@ void ml_gemm(const GemmProblem<N> &p, Workspace &ws, cudaStream_t stream) {
     if (p.M <= 0 || p.Nn <= 0 || p.batch <= 0) return;
     if (crt_gemm_applies<N>(p)) {
         void *s = ws.carve(crt_gemm_workspace_bytes<N>(p));
-        crt_gemm<N>(p, s, stream);
+        if (!p.error && ws.error) {
+            GemmProblem<N> q = p;
+            q.error = ws.error;
+            crt_gemm<N>(q, s, stream);
+        } else {
+            crt_gemm<N>(p, s, stream);
+        }
         return;
     }
     void *s = ws.carve(gemm_bfp_workspace_bytes<N>(p));

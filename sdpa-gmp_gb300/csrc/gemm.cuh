@@ -47,6 +47,9 @@ struct GemmProblem {
     long long ldc, sc;
     mlf<N> alpha, beta;
     int lower_only;  // 1: only entries with i >= j are written (SYRK-style update)
+    // device word set non-zero when a tensor-core kernel of this product gives up a
+    // bounded wait (null: the workspace's word, else only the device-wide flag)
+    int *error = nullptr;
     // optional: events recorded immediately before / after the digit-GEMM kernel launch
     cudaEvent_t ev_before = nullptr, ev_after = nullptr;
 };
@@ -91,7 +94,8 @@ template <int N>
 size_t crt_gemm_workspace_bytes(const GemmProblem<N> &p);
 template <int N>
 void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t stream);
-// device word that the tensor-core kernel sets when a bounded wait timed out
+// Device-wide sticky flag: set (and never cleared) when any tensor-core kernel on the
+// current device gave up a bounded wait, in addition to the product's own error word.
 int *crt_error_word();
 
 }  // namespace sdpg

@@ -399,6 +399,10 @@ class Solver final : public SolverBase {
         max_ws = std::max(max_ws, ml_trtri_workspace_bytes<N>(m_));
         ws_.reserve(max_ws + (64u << 20));
         ws2_.reserve(max_ws + (64u << 20));
+        // this solver's own tensor-core time-out word (zeroed by dalloc_raw): a wait that
+        // gives up in another solver on the device does not fail this one
+        tc_error_ = (int *)dalloc_raw(sizeof(int));
+        ws_.error = ws2_.error = tc_error_;
         SDPG_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
         SDPG_CUDA(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
         SDPG_CUDA(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
@@ -1398,7 +1402,7 @@ class Solver final : public SolverBase {
             int st = 0;
             if (N == 8 && g_gemm_method != 1) {
                 d2h_ += (long long)sizeof(int);
-                SDPG_CUDA(cudaMemcpyAsync(&st, crt_error_word(), sizeof(int), cudaMemcpyDeviceToHost, st_));
+                SDPG_CUDA(cudaMemcpyAsync(&st, tc_error_, sizeof(int), cudaMemcpyDeviceToHost, st_));
                 SDPG_CUDA(cudaStreamSynchronize(st_));
                 if (st != 0) throw sdpg_error(SDPG_ERR_TIMEOUT, "tensor-core GEMM: a bounded wait timed out");
             }
@@ -1713,6 +1717,7 @@ class Solver final : public SolverBase {
     int dev_;
     cudaStream_t st_;
     Workspace ws_, ws2_;  // ws2_ serves work issued on the second stream
+    int *tc_error_ = nullptr;  // device word: a tensor-core GEMM of this solver gave up a bounded wait
 
     cudaStream_t st2_ = nullptr;
     cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;

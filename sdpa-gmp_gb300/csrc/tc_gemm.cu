@@ -55,6 +55,12 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return true;
 }
 
+// a bounded wait gave up: the caller's word and the device-wide flag record it
+__device__ __forceinline__ void record_error(const TcModGemm &p, int code) {
+    atomicExch(p.error, code);
+    if (p.sticky && p.sticky != p.error) atomicExch(p.sticky, code);
+}
+
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
     asm volatile(
         "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
@@ -186,7 +192,7 @@ __global__ void __launch_bounds__(128, 1)
             ++issued;
         }
         if (!ok) {
-            atomicExch(p.error, 1);
+            record_error(p, 1);
             abort_flag = 1;
             // let the copies already issued land before the CTA goes away
             for (int kb = (issued > kStages ? issued - kStages : 0); kb < issued; ++kb)
@@ -214,14 +220,14 @@ __global__ void __launch_bounds__(128, 1)
             tc_commit(smem_u32(&empty[s]));
         }
         if (!ok) {
-            atomicExch(p.error, 2);
+            record_error(p, 2);
             abort_flag = 1;
         }
         tc_commit(smem_u32(done));  // arrives once every product issued above has completed
     }
     __syncwarp();
     if (!mbar_wait(smem_u32(done), 0)) {
-        atomicExch(p.error, 3);
+        record_error(p, 3);
         abort_flag = 1;
     }
     __syncthreads();

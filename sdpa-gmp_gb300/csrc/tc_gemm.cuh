@@ -34,7 +34,8 @@ struct TcModGemm {
     int accumulate;        // 1: Y = (Y + new) mod m (a later K chunk of the same product)
     int lower_only;        // 1: skip tiles strictly above the diagonal (their Y is not written)
     const int *moduli;     // device, L entries
-    int *error;            // device word: set non-zero if a bounded wait timed out
+    int *error;            // device word of the caller: set non-zero if a bounded wait timed out
+    int *sticky;           // device-wide flag, also set (may equal error or be null)
 };
 
 // Y planes for all (b, l); grid (Npad/128, Mpad/128, batch*L), 128 threads, one tile each.

@@ -258,10 +258,12 @@ def _control(m, blocks, seed, lp: int = 0, density: float = 0.3) -> SDPText:
 
 def param_text(precision: int = 256, max_iteration: int = 200, epsilon_star: str = "1.0E-30",
                lambda_star: str = "1.0E4", beta_star: str = "0.1", beta_bar: str = "0.3",
-               gamma_star: str = "0.9", epsilon_dash: str = "1.0E-30") -> str:
+               gamma_star: str = "0.9", epsilon_dash: str = "1.0E-30", print_format: str = "%+50.40Fe") -> str:
     """A ``param.sdpa`` file in the reference's 15-line positional layout
     (Parameter::readFile, sdpa_parts.cpp:188-225); defaults are the reference's
-    default parameter set (sdpa_parts.cpp:163-176) except ``precision``."""
+    default parameter set (sdpa_parts.cpp:163-176) except ``precision``.
+    ``print_format`` is the GMP format of xVec / xMat / yMat (lines 12-14; at most
+    29 characters, the reference's buffer)."""
     return (f"{max_iteration}\tunsigned int maxIteration;\n"
             f"{epsilon_star}\tdouble 0.0 < epsilonStar;\n"
             f"{lambda_star}   double 0.0 < lambdaStar;\n"
@@ -273,9 +275,9 @@ def param_text(precision: int = 256, max_iteration: int = 200, epsilon_star: str
             f"{gamma_star}     double 0.0 < gammaStar  <  1.0;\n"
             f"{epsilon_dash}\tdouble 0.0 < epsilonDash;\n"
             f"{precision}     precision\n"
-            "%+50.40Fe     char*  xPrint   (default %+8.3e,   NOPRINT skips printout)\n"
-            "%+50.40Fe     char*  XPrint   (default %+8.3e,   NOPRINT skips printout)\n"
-            "%+50.40Fe     char*  YPrint   (default %+8.3e,   NOPRINT skips printout)\n"
+            f"{print_format}     char*  xPrint   (default %+8.3e,   NOPRINT skips printout)\n"
+            f"{print_format}     char*  XPrint   (default %+8.3e,   NOPRINT skips printout)\n"
+            f"{print_format}     char*  YPrint   (default %+8.3e,   NOPRINT skips printout)\n"
             "%+50.40Fe     char*  infPrint (default %+10.16e, NOPRINT skips printout)\n")
 
 

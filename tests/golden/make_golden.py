@@ -12,7 +12,8 @@ Each fixture records what the reference prints: the per-iteration table
 (phase, iteration count, mu, gaps, objectives, feasibility errors) and the
 final primal vector ``xVec`` to 40 significant digits (``%+50.40Fe``).
 
-Usage: python tests/golden/make_golden.py [--only NAME ...] [--ref DIR]
+Usage: python tests/golden/make_golden.py [--only NAME ...] [--ref DIR] [--precise]
+(--ref defaults to $SDPG_REFERENCE_DIR, else /root/reference)
 """
 from __future__ import annotations
 
@@ -26,6 +27,7 @@ import shutil
 import subprocess
 import sys
 import tempfile
+import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
@@ -49,6 +51,26 @@ CASES = {
     "controllp20": ("control_lp", dict(m=20, blocks=(10,), lp=12, seed=5), 256),
     "controllp40": ("control_lp", dict(m=40, blocks=(24, 8), lp=30, density=0.2, seed=6), 256),
 }
+
+# High-precision cases: the reference prints xVec / xMat / yMat with `print_format`
+# (param.sdpa lines 12-14), so its final iterate is known to far below 2^-p.  The
+# fixture keeps xVec, the objectives recomputed exactly from the printed solution
+# (c.x and F0.Y), and for large blocks only the first column and diagonal of xMat /
+# yMat.  max_iteration < 200 stops the reference after that many iterations, which
+# gives fixed-iteration comparisons of the same run.
+P80 = "%+.80Fe"
+P160 = "%+.160Fe"
+PRECISE = {
+    "gpp500_hp": ("gpp", dict(n=500, p=0.02, seed=0), 256, dict(print_format=P80)),
+    "gpp500_it5": ("gpp", dict(n=500, p=0.02, seed=0), 256, dict(print_format=P80, max_iteration=5)),
+    "gpp500_it10": ("gpp", dict(n=500, p=0.02, seed=0), 256, dict(print_format=P80, max_iteration=10)),
+    "gpp500_it20": ("gpp", dict(n=500, p=0.02, seed=0), 256, dict(print_format=P80, max_iteration=20)),
+    "gpp500_p512_it10": ("gpp", dict(n=500, p=0.02, seed=0), 512, dict(print_format=P160, max_iteration=10)),
+    "control231_hp": ("control", dict(m=231, blocks=(40, 20), seed=0), 256, dict(print_format=P80)),
+    "maxcut124pm_hp": ("maxcut", dict(n=124, p=0.1, seed=0, signed=True), 256, dict(print_format=P80)),
+    "maxcut100_hp": ("maxcut", dict(n=100, p=0.1, seed=0), 256, dict(print_format=P80)),
+}
+FULL_MATRIX_LIMIT = 4000  # larger solutions keep only a digest
 
 ITER_RE = re.compile(r"^\s*(\d+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)\s*$")
 FINAL_KEYS = ["mu", "relative gap", "gap", "digits", "objValPrimal", "objValDual",
@@ -107,6 +129,53 @@ def result_layout(text: str) -> list[str]:
     return out
 
 
+def precise_fields(r: dict, prob) -> None:
+    """Replace r's xMat / yMat by a digest when large and add the objectives computed
+    exactly (decimal, 200 digits) from the printed solution: objValPrimal = c.xVec and
+    objValDual = F0.yMat (SDPA's printed primal / dual, sdpa_io.cpp:1095-1109, 1166-1173),
+    and the relative gap |P - D| / max(1, (|P| + |D|) / 2) (sdpa_io.cpp:1001-1003)."""
+    from decimal import Decimal, getcontext
+    getcontext().prec = 200
+    x = [Decimal(v) for v in r["xVec"]]
+    objp = sum(Decimal(c) * xi for c, xi in zip(prob.c, x))
+    sizes = [abs(b) for b in prob.block_struct]
+    offs, o = [], 0
+    for b, nb in zip(prob.block_struct, sizes):
+        offs.append(o)
+        o += nb * nb if b > 0 else nb
+    ymat = r["yMat"]
+    assert len(ymat) == o, (len(ymat), o)
+
+    def y(block, i, j):  # 1-based entry of block `block` of yMat
+        b = prob.block_struct[block - 1]
+        if b < 0:
+            return Decimal(ymat[offs[block - 1] + i - 1]) if i == j else Decimal(0)
+        return Decimal(ymat[offs[block - 1] + (i - 1) * sizes[block - 1] + (j - 1)])
+
+    objd = Decimal(0)
+    for k, blk, i, j, v in prob.entries:
+        if k == 0:
+            objd += Decimal(v) * y(blk, i, j) * (1 if i == j else 2)
+    gap = abs(objp - objd) / max(Decimal(1), (abs(objp) + abs(objd)) / 2)
+    r["objValPrimal_hp"] = format(objp, ".90e")
+    r["objValDual_hp"] = format(objd, ".90e")
+    r["relgap_hp"] = format(gap, ".40e")
+    if len(ymat) > FULL_MATRIX_LIMIT:
+        dig = {}
+        for key in ("xMat", "yMat"):
+            vals = r.pop(key)
+            d = {"diag": [], "col0": []}
+            for blk, (b, nb) in enumerate(zip(prob.block_struct, sizes)):
+                if b < 0:
+                    continue
+                base = offs[blk]
+                d["diag"].append([vals[base + i * nb + i] for i in range(nb)])
+                d["col0"].append([vals[base + i * nb] for i in range(nb)])
+            dig[key] = d
+        r["digest"] = dig
+    r["layout"] = [ln for ln in r["layout"] if not ln.startswith("{")][:400]
+
+
 def run_case(binary: str, dat_text: str, param_text: str, workdir: str, name: str, extra=()) -> dict:
     dat = os.path.join(workdir, name + ".dat-s")
     par = os.path.join(workdir, name + ".param")
@@ -125,7 +194,8 @@ def run_case(binary: str, dat_text: str, param_text: str, workdir: str, name: st
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", nargs="*")
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("SDPG_REFERENCE_DIR", "/root/reference"))
+    ap.add_argument("--precise", action="store_true", help="also run the high-precision cases")
     args = ap.parse_args()
     binary = os.path.join(ROOT, "oracle", "_ref", "sdpa_gmp")
     subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh"), args.ref], check=True,
@@ -184,6 +254,23 @@ def main() -> None:
             with open(os.path.join(HERE, name + ".json"), "w") as f:
                 json.dump(r, f, indent=1)
             print(name, r.get("phase"), r.get("iteration"), r.get("objValPrimal"))
+        for name, (gen, kw, prec, pkw) in PRECISE.items():
+            if not args.precise or (args.only and name not in args.only):
+                continue
+            prob = getattr(problems, gen)(**kw)
+            dat_text = prob.text()
+            param_text = problems.param_text(precision=prec, **pkw)
+            t0 = time.time()
+            r = run_case(binary, dat_text, param_text, work, name)
+            precise_fields(r, prob)
+            r.update(name=name, generator=gen, kwargs={k: (list(v) if isinstance(v, tuple) else v)
+                                                         for k, v in kw.items()},
+                     precision=prec, sha256=hashlib.sha256(dat_text.encode()).hexdigest(), param=pkw,
+                     reference_seconds=round(time.time() - t0, 1))
+            with open(os.path.join(HERE, name + ".json"), "w") as f:
+                json.dump(r, f, indent=0)
+            print(name, r.get("phase"), r.get("iteration"), r["objValPrimal_hp"][:30], r["reference_seconds"], "s",
+                  flush=True)
     finally:
         shutil.rmtree(work, ignore_errors=True)
 
