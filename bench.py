@@ -41,9 +41,17 @@ sys.path.insert(0, ROOT)
 METRIC = "256-bit IPM iters/s (gpp n=500 m=501)"
 UNIT = "iters/s"
 RESIDUE_MODULI = 70  # primes of the 256-bit residue GEMM (csrc/crt_tables.h)
-# DRAM bytes (read + write) per launch of tc_modgemm_kernel for a 500^3 product, from
-# the ncu capture summarised in profiles/tc_modgemm_kernel_gemm500_256bit.md
+# DRAM bytes (read + write) per algorithmic byte (or per launch for the tensor kernel),
+# from the ncu captures of a 500^3 product summarised in
+# profiles/tc_modgemm_kernel_gemm500_256bit.md: crt_residue_kernel 20.0 + 51.1 MB against
+# 20.0 + 70.0 MB algorithmic; crt_reconstruct_kernel 35.9 MB against 45.0 MB;
+# tc_modgemm_kernel 81.8 MB per launch.
 TC_TRAFFIC_BYTES = 81.8e6
+TRAFFIC_PER_ALG_BYTE = {"crt_residue_kernel": 71.1 / 90.0, "crt_reconstruct_kernel": 35.9 / 45.0}
+# Kernel families with an algorithmic-work figure (sdpg_kernel_times' work column):
+# roofline bound and the unit of that work.
+FAMILY_BOUND = {"crt_residue_kernel": "hbm", "crt_exp_kernel": "hbm", "crt_reconstruct_kernel": "hbm",
+                "lz_matvec_kernel": "hbm", "tc_modgemm_kernel": "tensor"}
 
 
 def workload(precision: int):
@@ -143,6 +151,74 @@ def run_cpu_port(dat: str, par_dir: str, precision: int, iters: int) -> tuple[li
                        check=True)
     times = [float(m.group(2)) for m in re.finditer(r"^ITER (\d+) ([0-9.eE+-]+)$", r.stderr, re.M)]
     return times, threads
+
+
+def kernel_families(sdpg, new_solver, steps: int, warmup: int, peaks: dict) -> tuple[list, float]:
+    """A second pass over the same workload: `steps` iterations after `warmup`, every kernel
+    bracketed by CUDA events on its own stream (captured graphs run as plain launches).
+    Returns per-kernel rows sorted by time and the summed kernel milliseconds per step."""
+    import torch
+    s = new_solver()
+    for _ in range(warmup):
+        if not s.iterate():
+            s = new_solver()
+    torch.cuda.synchronize()
+    sdpg.kernel_times()  # drop anything recorded before
+    sdpg.kernel_timing(True)
+    try:
+        k = 0
+        while k < steps:
+            if s.iterate():
+                k += 1
+            else:
+                s = new_solver()
+        torch.cuda.synchronize()
+        times = sdpg.kernel_times()
+    finally:
+        sdpg.kernel_timing(False)
+    s.close()
+    total = sum(v[1] for v in times.values())
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    tflops = peaks.get("bf16_tflops_sustained") or 1700.0
+    rows = []
+    for name, (launches, ms, work) in sorted(times.items(), key=lambda kv: -kv[1][1]):
+        row = {"kernel": name, "launches_per_step": launches / steps, "ms_per_step": ms / steps,
+               "share": ms / total if total else None, "avg_launch_us": 1e3 * ms / max(1, launches)}
+        bound = FAMILY_BOUND.get(name)
+        if bound and work > 0 and ms > 0:
+            if bound == "hbm":
+                ach = work / (ms * 1e-3) / 1e9
+                row.update(bound="hbm", achieved=ach, peak=hbm, unit="GB/s", frac=ach / hbm,
+                           algorithmic_bytes_per_launch=work / launches)
+            else:
+                ach = work / (ms * 1e-3) / 1e12
+                row.update(bound="tensor", achieved=ach, peak=tflops, unit="TFLOP/s", frac=ach / tflops,
+                           algorithmic_flops_per_launch=work / launches)
+        else:
+            row["bound"] = "latency"
+        rows.append(row)
+    return rows, total / steps
+
+
+def reference_errors(sdpg, solver, name: str) -> dict | None:
+    """log2 relative errors against a high-precision golden (tests/golden/<name>.json)."""
+    gpath = os.path.join(ROOT, "tests", "golden", name + ".json")
+    if not os.path.exists(gpath):
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    precise = importlib.import_module("precise")
+    with open(gpath) as f:
+        g = json.load(f)
+    info = solver.info()
+    out = {"golden": name, "reference_phase": g["phase"], "reference_iterations": g["iteration"],
+           "phase": info["phase"], "iterations": info["iteration"]}
+    if info["iteration"] != g["iteration"]:
+        out["note"] = "different iteration counts: final iterates not comparable"
+        return out
+    e = precise.errors(sdpg, solver, g)
+    out["log2_rel_error"] = {k: round(e[k + "_log2"], 1) for k in ("objValPrimal", "objValDual", "relgap", "xVec",
+                                                                  "xMat", "yMat")}
+    return out
 
 
 def dist_setup(n_gpus: int):
@@ -259,6 +335,31 @@ def bench_ours(args) -> None:
                                    "integer-pipe figure)",
                     "imad_wide_per_mac": imad_per_mac, "traffic": None, **common}
 
+    # every kernel family of the same iterations, timed per launch in a second pass
+    families, kernel_ms_per_step = kernel_families(sdpg, new_solver, args.steps, args.warmup, measured_peaks()) \
+        if not args.no_families else ([], None)
+    dominant = None
+    for fam in families:  # the dominant kernel with a roofline bound (hbm or tensor)
+        if fam.get("bound") in ("hbm", "tensor"):
+            dominant = fam
+            break
+    if dominant is not None:
+        traffic = None
+        if dominant["kernel"] in TRAFFIC_PER_ALG_BYTE:
+            traffic = TRAFFIC_PER_ALG_BYTE[dominant["kernel"]] * dominant["algorithmic_bytes_per_launch"]
+        elif dominant["kernel"] == "tc_modgemm_kernel":
+            traffic = TC_TRAFFIC_BYTES
+        roofline_dom = {"bound": dominant["bound"], "kernel": dominant["kernel"], "achieved": dominant["achieved"],
+                        "peak": dominant["peak"], "unit": dominant["unit"], "frac": dominant["frac"],
+                        "traffic": traffic, "share_of_kernel_time": dominant["share"],
+                        "avg_launch_us": dominant["avg_launch_us"],
+                        "peak_source": ("hbm_gbs" if dominant["bound"] == "hbm" else "bf16_tflops_sustained")
+                                       + " of measured (MEASURED_PEAKS.json)",
+                        "timing": "per-launch CUDA events on the launching stream, second pass of the same "
+                                  f"{args.steps} iterations after {args.warmup} warm-up"}
+    else:
+        roofline_dom = None
+
     # the same iterations with every product on the integer digit GEMM (the plain
     # multi-limb path): the tensor-core path's speed-up at equal accuracy
     plain = None
@@ -301,10 +402,27 @@ def bench_ours(args) -> None:
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         h2d, d2h = s2.io_bytes()
+        err_full = reference_errors(sdpg, s2, "gpp500_hp" if args.precision <= 256 else "")
         e2e = {"value": its / (t1 - t0), "unit": UNIT, "iterations": its, "seconds": t1 - t0,
                "h2d_bytes_per_step": int(h2d / max(1, its)), "d2h_bytes_per_step": int((d2h + x.nbytes) / max(1, its)),
                "phase": s2.info()["phase"], "scope": "Problem.read + Solver + run() + xvec(), host file to host result"}
         s2.close()
+    # error against the reference's own 80-digit (160 at 512 bits) output: the full solve
+    # (above) and the first 10 iterations of the same problem
+    errs = {}
+    if not args.no_e2e and err_full:
+        errs["full_solve"] = err_full
+    pref = "gpp500_it10" if args.precision <= 256 else "gpp500_p512_it10"
+    par10 = os.path.join(d, "it10.param")
+    with open(par10, "w") as f:
+        f.write(importlib.import_module("sdpa-gmp_gb300.problems").param_text(precision=args.precision,
+                                                                              max_iteration=10))
+    s3 = sdpg.Solver(sdpg.Problem.read(dat), sdpg.Param.read(par10), device=local, stream=stream.cuda_stream)
+    s3.run()
+    e10 = reference_errors(sdpg, s3, pref)
+    if e10:
+        errs["first_10_iterations"] = e10
+    s3.close()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -325,7 +443,12 @@ def bench_ours(args) -> None:
                 "scaling": "weak", "vs_baseline": None, "dtype": f"u32x{8 if args.precision <= 256 else 16} multi-limb",
                 "data": "synthetic (seeded generator standing in for SDPLIB gpp500)",
                 "config": config(args.precision, ws_mb),
-                "impl": "ours", "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+                "impl": "ours", "e2e": e2e, "gpu_launches": launches, "roofline": roofline_dom or roofline,
+                "roofline_gemm": roofline, "kernel_families": families[:12],
+                "kernel_ms_per_step": kernel_ms_per_step,
+                "dominant_kernel": ({"kernel": families[0]["kernel"], "share": families[0]["share"],
+                                     "bound": families[0]["bound"]} if families else None),
+                "error_vs_reference": errs or None, "cpu_baseline": cpu,
                 "plain_path": plain,
                 "clocks": clk, "phase_ms": {k: round(v, 3) for k, v in timers.items()},
                 "restarts": restarts, "peaks": {k: measured_peaks().get(k) for k in ("hbm_gbs", "bf16_tflops")}}
@@ -483,6 +606,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the digit-GEMM (plain path) comparison")
+    ap.add_argument("--no-families", action="store_true", help="skip the per-kernel timing pass")
     ap.add_argument("--workload", choices=["ipm", "batch", "learned"], default="ipm",
                     help="batch: many small control/LMI solves at once (solves/s); learned: the committed "
                          "lambdaStar/beta policy against the defaults (mean iterations) on --batch held-out seeds")

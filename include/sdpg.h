@@ -75,6 +75,8 @@ int sdpg_ml_to_double(int limbs, const void *v, long long n, double *out);
 int sdpg_ml_from_mpf(int limbs, const sdpg_mpf_t *src, long long n, void *out);
 /* dst[i]._mp_d must hold _mp_prec + 1 limbs (as GMP allocates). */
 int sdpg_ml_to_mpf(int limbs, const void *v, long long n, sdpg_mpf_t *dst);
+/* *result = -1, 0 or 1 as a < b, a == b, a > b (exact); mpf_cmp's role. */
+int sdpg_ml_compare(int limbs, const void *a, const void *b, int *result);
 /* Elementwise host arithmetic in the ml format (SDPG_OP_*); b is ignored for SQRT. */
 int sdpg_ml_host_op(int limbs, int op, long long n, const void *a, const void *b, void *out);
 
@@ -178,6 +180,37 @@ int sdpg_solver_run(sdpg_solver *h, const char *out_path, int print_to_stdout);
  * sdpa_main.cpp:294-384): returns 1 when an iteration was made, 0 once the loop has
  * stopped (phase decided, iteration limit, Schur Cholesky failure, or cannot move). */
 int sdpg_solver_iterate(sdpg_solver *h);
+/* pinpal's main loop one step at a time (sdpa_main.cpp:294-398), in its order; the C++
+ * classes of sdpa_gb300.hpp (Phase, DirectionParameter, StepLength, Solutions, ...) call
+ * these.  sdpg_solver_iterate is the sequence predictor-direction .. after-update.
+ *   sdpg_loop_phase_check     Phase::updateCheck (sdpa_parts.cpp:932-1011): 1 go on, 0 stop
+ *                             (initialises the solver on its first call)
+ *   sdpg_loop_direction       corrector 0: Switch::MehrotraPredictor and
+ *                             DirectionParameter::MehrotraPredictor (sdpa_parts.cpp:543-553,
+ *                             605-612); 1: DirectionParameter::MehrotraCorrector (:555-586)
+ *   sdpg_loop_corrector_break 1 if the phase is pdFEAS and (beta > 5 or objValPrimal <
+ *                             objValDual): the loop's break before the corrector
+ *                             (sdpa_main.cpp:335-339)
+ *   sdpg_loop_record          IO::printOneIteration (sdpa_io.cpp:764-796) to out_file and
+ *                             display_file (FILE *, either may be NULL); records the row
+ *   sdpg_loop_update          Solutions::update (sdpa_dataset.cpp:120-143); SDPG_ERR_NOT_PD
+ *                             when the step is too short ("cannot move")
+ *   sdpg_loop_after_update    RatioInitResCurrentRes::update, AverageComplementarity::update,
+ *                             Residuals::update, RatioInitResCurrentRes::update_exact,
+ *                             SolveInfo::update, and the iteration count (sdpa_main.cpp:374-382)
+ *   sdpg_loop_finish          Residuals::compute, Phase::reverse and IO::printLastInfo
+ *                             (sdpa_main.cpp:387-398) to out_file / display_file
+ *   sdpg_loop_values          the phase (as the loop sees it, not reversed), the iteration
+ *                             count and 9 ml values: beta, objValPrimal (C.X), objValDual
+ *                             (b.y), mu, initial mu, alphaP, alphaD, thetaP, thetaD */
+int sdpg_loop_phase_check(sdpg_solver *h);
+int sdpg_loop_direction(sdpg_solver *h, int corrector);
+int sdpg_loop_corrector_break(sdpg_solver *h);
+int sdpg_loop_record(sdpg_solver *h, void *out_file, void *display_file);
+int sdpg_loop_update(sdpg_solver *h);
+int sdpg_loop_after_update(sdpg_solver *h);
+int sdpg_loop_finish(sdpg_solver *h, void *out_file, void *display_file);
+int sdpg_loop_values(sdpg_solver *h, int *phase, int *iteration, void *out_ml9);
 /* Newton::Mehrotra (sdpa_newton.cpp:1375-1414); direction 0 predictor, 1 corrector.
  * Returns SDPG_ERR_NOT_PD when the Schur Cholesky fails (the reference's FAILURE). */
 int sdpg_newton(sdpg_solver *h, int direction);
@@ -233,6 +266,27 @@ int sdpg_set_gemm_method(int method);
  * checked every iteration (a time-out there fails that solver with SDPG_ERR_TIMEOUT,
  * not the other solvers on the device). */
 int sdpg_tensor_error(int device, int *flag);
+/* Per-kernel timing (no reference counterpart; the reference's ComputeTime times whole
+ * phases).  While enabled, every kernel the library launches outside a stream capture is
+ * bracketed by a pair of CUDA events on its own stream, and the solvers run their
+ * captured sequences as plain launches.  sdpg_kernel_timing returns the previous state.
+ * sdpg_kernel_times waits for the recorded kernels, writes one line per kernel name,
+ * "name launches milliseconds work", sorted by name, into buf, forgets the records and
+ * returns the number of lines (SDPG_ERR_TOO_LARGE if cap is too small).  `work` is the
+ * launches' summed algorithmic work where the library states one: for
+ * crt_residue_kernel, crt_exp_kernel, crt_reconstruct_kernel and lz_matvec_kernel the
+ * bytes the kernel must move (multi-limb entries read, residue planes written, ...), for
+ * tc_modgemm_kernel the fp16 tensor flops 2 M N K per residue GEMM; 0 elsewhere. */
+int sdpg_kernel_timing(int enable);
+int sdpg_kernel_times(char *buf, int cap);
+/* Test hook (no reference counterpart): the budget, in GPU clock cycles, of the
+ * tensor-core GEMM kernel's primary waits (TMA data arriving, ring stages freed);
+ * cycles <= 0 restores the default of about one second.  With a budget shorter than a
+ * copy takes, those waits give up: the kernel records the time-out in the caller's
+ * error word and the sticky device flag (sdpg_tensor_error), waits with the full
+ * budget for the copies and products it already issued, frees its tensor memory and
+ * returns; a solver then fails with SDPG_ERR_TIMEOUT.  Returns the previous setting. */
+long long sdpg_set_tensor_wait_budget(long long cycles);
 /* Measured throughput of signed 32x32->64 multiply-adds (IMAD.WIDE) on one GPU, the
  * instruction the multi-limb GEMM is built from; the plain path's roofline denominator. */
 int sdpg_probe_imad_wide(int device, double *ops_per_second);

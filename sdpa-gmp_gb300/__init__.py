@@ -113,6 +113,9 @@ def _setup(lib: ctypes.CDLL) -> ctypes.CDLL:
         "sdpg_launch_count": (c.c_ulonglong, []),
         "sdpg_set_gemm_method": (i, [i]),
         "sdpg_tensor_error": (i, [i, c.POINTER(i)]),
+        "sdpg_set_tensor_wait_budget": (ll, [ll]),
+        "sdpg_kernel_timing": (i, [i]),
+        "sdpg_kernel_times": (i, [c.c_char_p, i]),
         "sdpg_probe_imad_wide": (i, [i, c.POINTER(c.c_double)]),
         "sdpg_solve_file": (i, [c.c_char_p, c.c_char_p, c.c_char_p, i, c.POINTER(c.c_double)]),
         "sdpg_policy_create": (i, [i, c.POINTER(vp)]),
@@ -587,6 +590,28 @@ def tensor_error(device: int = 0) -> int:
     flag = ctypes.c_int(0)
     check(lib().sdpg_tensor_error(device, ctypes.byref(flag)))
     return flag.value
+
+
+def set_tensor_wait_budget(cycles: int) -> int:
+    """Test hook: budget (clock cycles) of the tensor-core kernel's primary waits; 0 restores
+    the default.  Returns the previous setting."""
+    return int(lib().sdpg_set_tensor_wait_budget(cycles))
+
+
+def kernel_timing(enable: bool) -> bool:
+    """Per-kernel CUDA-event timing on (graphs become plain launches) or off; returns the old state."""
+    return bool(lib().sdpg_kernel_timing(1 if enable else 0))
+
+
+def kernel_times() -> dict:
+    """{kernel name: (launches, milliseconds, algorithmic work)} recorded since the last call."""
+    buf = ctypes.create_string_buffer(1 << 16)
+    check(lib().sdpg_kernel_times(buf, len(buf)))
+    out = {}
+    for ln in buf.value.decode().splitlines():
+        name, cnt, ms, work = ln.split()
+        out[name] = (int(cnt), float(ms), float(work))
+    return out
 
 
 def solve_batch(problems, param: Param | None = None, device: int = 0, concurrency: int = 16):

@@ -155,6 +155,21 @@ int sdpg_ml_host_op(int limbs, int op, long long n, const void *a, const void *b
     });
 }
 
+int sdpg_ml_compare(int limbs, const void *a, const void *b, int *result) {
+    return sdpg_guard([&] {
+        if (!a || !b || !result) throw sdpg_error(SDPG_ERR_ARG, "null operand");
+        return dispatch_limbs(limbs, [&](auto tag) {
+            constexpr int N = decltype(tag)::value;
+            mlf<N> x, y;
+            memcpy(&x, a, sizeof x);
+            memcpy(&y, b, sizeof y);
+            const int c = ml_cmp(x, y);
+            *result = c < 0 ? -1 : c > 0 ? 1 : 0;
+            return (int)SDPG_OK;
+        });
+    });
+}
+
 int sdpg_rgemm_device(int limbs, char transa, char transb, int m, int n, int k, const void *alpha,
                       const void *A, int lda, const void *B, int ldb, const void *beta, void *C, int ldc,
                       void *stream) {

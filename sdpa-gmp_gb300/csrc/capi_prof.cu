@@ -3,6 +3,7 @@
 #include "capi_util.cuh"
 #include "gemm.cuh"
 #include "sdpg.h"
+#include "tc_gemm.cuh"
 
 #include <map>
 #include <mutex>
@@ -93,6 +94,12 @@ int sdpg_set_gemm_method(int method) {
     });
 }
 
+long long sdpg_set_tensor_wait_budget(long long cycles) {
+    const long long old = g_tc_wait_cycles;
+    g_tc_wait_cycles = cycles > 0 ? cycles : 0;
+    return old;
+}
+
 int sdpg_tensor_error(int device, int *flag) {
     return sdpg_guard([&] {
         if (!flag) throw sdpg_error(SDPG_ERR_ARG, "null output");
@@ -133,6 +140,133 @@ int sdpg_probe_imad_wide(int device, double *ops_per_second) {
         cudaEventDestroy(b);
         *ops_per_second = (double)blocks * threads * iters * 16.0 / (best * 1e-3);
         return (int)SDPG_OK;
+    });
+}
+
+}  // extern "C"
+
+// ---- per-kernel timing ------------------------------------------------------------
+
+namespace sdpg {
+
+std::atomic<bool> g_kt_on{false};
+
+namespace kt_detail {
+
+struct KtPair {
+    const char *name;
+    int device;
+    cudaEvent_t a, b;
+    double work;
+};
+
+std::mutex g_kt_mu;
+std::vector<KtPair> g_kt_pairs;           // recorded, not yet read
+std::vector<std::pair<int, cudaEvent_t>> g_kt_free;  // (device, event) ready for reuse
+thread_local std::vector<std::pair<cudaStream_t, cudaEvent_t>> t_kt_open;  // begun, not ended
+
+cudaEvent_t kt_event(int dev) {
+    {
+        std::lock_guard<std::mutex> lock(g_kt_mu);
+        for (size_t i = 0; i < g_kt_free.size(); ++i)
+            if (g_kt_free[i].first == dev) {
+                cudaEvent_t e = g_kt_free[i].second;
+                g_kt_free[i] = g_kt_free.back();
+                g_kt_free.pop_back();
+                return e;
+            }
+    }
+    cudaEvent_t e;
+    SDPG_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+bool capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone;
+}
+
+}  // namespace kt_detail
+
+using namespace kt_detail;
+
+void kt_begin(cudaStream_t s) {
+    if (capturing(s)) return;
+    int dev = 0;
+    SDPG_CUDA(cudaGetDevice(&dev));
+    cudaEvent_t e = kt_event(dev);
+    SDPG_CUDA(cudaEventRecord(e, s));
+    t_kt_open.emplace_back(s, e);
+}
+
+void kt_end(const char *name, cudaStream_t s, double work) {
+    for (size_t i = t_kt_open.size(); i-- > 0;) {
+        if (t_kt_open[i].first != s) continue;
+        cudaEvent_t a = t_kt_open[i].second;
+        t_kt_open.erase(t_kt_open.begin() + (long)i);
+        int dev = 0;
+        SDPG_CUDA(cudaGetDevice(&dev));
+        cudaEvent_t b = kt_event(dev);
+        SDPG_CUDA(cudaEventRecord(b, s));
+        std::lock_guard<std::mutex> lock(g_kt_mu);
+        g_kt_pairs.push_back(KtPair{name, dev, a, b, work});
+        return;
+    }
+}
+
+}  // namespace sdpg
+
+extern "C" {
+
+int sdpg_kernel_timing(int enable) {
+    const bool old = sdpg::g_kt_on.exchange(enable != 0);
+    return old ? 1 : 0;
+}
+
+int sdpg_kernel_times(char *buf, int cap) {
+    using namespace sdpg::kt_detail;
+    return sdpg_guard([&] {
+        if (!buf || cap <= 0) throw sdpg_error(SDPG_ERR_ARG, "null buffer");
+        std::vector<KtPair> pairs;
+        {
+            std::lock_guard<std::mutex> lock(g_kt_mu);
+            pairs.swap(g_kt_pairs);
+        }
+        struct Agg {
+            long long launches = 0;
+            double ms = 0, work = 0;
+        };
+        std::map<std::string, Agg> agg;
+        int dev0 = 0;
+        SDPG_CUDA(cudaGetDevice(&dev0));
+        for (const KtPair &p : pairs) {
+            SDPG_CUDA(cudaSetDevice(p.device));
+            SDPG_CUDA(cudaEventSynchronize(p.b));
+            float ms = 0;
+            SDPG_CUDA(cudaEventElapsedTime(&ms, p.a, p.b));
+            Agg &v = agg[p.name];
+            v.launches += 1;
+            v.ms += ms;
+            v.work += p.work;
+        }
+        SDPG_CUDA(cudaSetDevice(dev0));
+        {
+            std::lock_guard<std::mutex> lock(g_kt_mu);
+            for (const KtPair &p : pairs) {
+                g_kt_free.emplace_back(p.device, p.a);
+                g_kt_free.emplace_back(p.device, p.b);
+            }
+        }
+        std::string out;
+        for (const auto &kv : agg) {
+            char line[256];
+            snprintf(line, sizeof line, "%s %lld %.6f %.6e\n", kv.first.c_str(), kv.second.launches, kv.second.ms,
+                     kv.second.work);
+            out += line;
+        }
+        if ((int)out.size() + 1 > cap) throw sdpg_error(SDPG_ERR_TOO_LARGE, "buffer too small");
+        memcpy(buf, out.c_str(), out.size() + 1);
+        return (int)agg.size();
     });
 }
 

@@ -344,6 +344,54 @@ int sdpg_step_length(sdpg_solver *h, int direction) {
     });
 }
 
+int sdpg_loop_phase_check(sdpg_solver *h) {
+    return sdpg_guard([&] { return S(h).loop_phase_check() ? 1 : 0; });
+}
+
+int sdpg_loop_direction(sdpg_solver *h, int corrector) {
+    return sdpg_guard([&] {
+        S(h).loop_direction(corrector);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_loop_corrector_break(sdpg_solver *h) {
+    return sdpg_guard([&] { return S(h).loop_corrector_break() ? 1 : 0; });
+}
+
+int sdpg_loop_record(sdpg_solver *h, void *out_file, void *display_file) {
+    return sdpg_guard([&] {
+        S(h).loop_record((FILE *)out_file, (FILE *)display_file);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_loop_update(sdpg_solver *h) {
+    return sdpg_guard([&] { return S(h).loop_update() ? (int)SDPG_OK : (int)SDPG_ERR_NOT_PD; });
+}
+
+int sdpg_loop_after_update(sdpg_solver *h) {
+    return sdpg_guard([&] {
+        S(h).loop_after_update();
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_loop_finish(sdpg_solver *h, void *out_file, void *display_file) {
+    return sdpg_guard([&] {
+        S(h).loop_finish((FILE *)out_file, (FILE *)display_file);
+        return (int)SDPG_OK;
+    });
+}
+
+int sdpg_loop_values(sdpg_solver *h, int *phase, int *iteration, void *out_ml9) {
+    return sdpg_guard([&] {
+        if (!phase || !iteration || !out_ml9) throw sdpg_error(SDPG_ERR_ARG, "null output");
+        S(h).loop_values(phase, iteration, out_ml9);
+        return (int)SDPG_OK;
+    });
+}
+
 int sdpg_update(sdpg_solver *h) {
     return sdpg_guard([&] { return S(h).update() ? (int)SDPG_OK : (int)SDPG_ERR_NOT_PD; });
 }

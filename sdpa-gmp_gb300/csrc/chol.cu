@@ -451,12 +451,14 @@ void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t 
             ml_gemm<N>(p, ws, s);
             ws.used = m2;
         }
+        SDPG_KT_BEGIN(s);
         potf2_cluster_kernel<N><<<kPotf2Cluster, kPotf2ClusterThreads, 0, s>>>(Akk, lda, kb, k0, info, rinv, Lsc);
-        SDPG_CHECK_LAUNCH();
+        SDPG_CHECK_LAUNCH_KT("potf2_cluster_kernel", s);
         if (rows <= 0) break;
+        SDPG_KT_BEGIN(s);
         panel_trsm_kernel<N><<<ceil_div((long long)rows * 32, 256), 256, 0, s>>>(Lsc, Akk + kb, lda, kb, rows, info,
                                                                                rinv);
-        SDPG_CHECK_LAUNCH();
+        SDPG_CHECK_LAUNCH_KT("panel_trsm_kernel", s);
     }
     ws.used = mark;
 }
@@ -519,11 +521,13 @@ void ml_trtri_lower(int n, const mlf<N> *L, int ldl, mlf<N> *Linv, Workspace &ws
     mlf<N> *Lp = (mlf<N> *)ws.carve(pp * sizeof(mlf<N>));
     mlf<N> *Xp = (mlf<N> *)ws.carve(pp * sizeof(mlf<N>));
     mlf<N> *W = (mlf<N> *)ws.carve(pp / 2 * sizeof(mlf<N>));
+    SDPG_KT_BEGIN(s);
     pad_lower_kernel<N><<<ceil_div(pp, 256), 256, 0, s>>>(n, P, L, ldl, Lp);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("pad_lower_kernel", s);
     SDPG_CUDA(cudaMemsetAsync(Xp, 0, pp * sizeof(mlf<N>), s));
+    SDPG_KT_BEGIN(s);
     trtri_diag_kernel<N><<<P / NB, kPotf2Threads, 0, s>>>(Lp, P, Xp, P, P);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("trtri_diag_kernel", s);
     const mlf<N> one = ml_one<N>(), zero = ml_zero<N>(), mone = ml_from_int<N>(-1);
     for (int b = 2 * NB; b <= P; b *= 2) {
         const int h = b / 2, nodes = P / b;
@@ -560,8 +564,9 @@ void ml_trtri_lower(int n, const mlf<N> *L, int ldl, mlf<N> *Linv, Workspace &ws
             ws.used = m2;
         }
     }
+    SDPG_KT_BEGIN(s);
     unpad_kernel<N><<<ceil_div((long long)n * n, 256), 256, 0, s>>>(n, P, Xp, Linv);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("unpad_kernel", s);
     ws.used = mark;
 }
 
@@ -575,11 +580,13 @@ size_t ml_potrs_prepare_bytes(int n) {
 
 template <int N>
 void ml_potrs_prepare(int n, const mlf<N> *L, int ldl, mlf<N> *Dinv, cudaStream_t s) {
+    SDPG_KT_BEGIN(s);
     trtri_diag_packed_kernel<N><<<ceil_div(n, NB), 256, 0, s>>>(L, ldl, Dinv, n);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("trtri_diag_packed_kernel", s);
     mlf<N> *LT = Dinv + (size_t)ceil_div(n, NB) * NB * NB;
+    SDPG_KT_BEGIN(s);
     transpose_lower_kernel<N><<<dim3(ceil_div(n, 32), ceil_div(n, 32)), dim3(32, 8), 0, s>>>(n, L, ldl, LT);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("transpose_lower_kernel", s);
 }
 
 template <int N>
@@ -589,10 +596,12 @@ void ml_potrs_solve(int n, const mlf<N> *L, int ldl, const mlf<N> *Dinv, mlf<N> 
     int *sync = (int *)(((uintptr_t)(LT + (size_t)n * n) + 255) & ~(uintptr_t)255);
     int *status = sync + 2 * (nblk + 1);
     SDPG_CUDA(cudaMemsetAsync(sync, 0, (2 * (nblk + 1) + 1) * sizeof(int), s));
+    SDPG_KT_BEGIN(s);
     trsv_wavefront_kernel<N><<<nblk, kTrsvThreads, 0, s>>>(n, L, ldl, Dinv, x, sync, status, 0);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("trsv_wavefront_kernel", s);
+    SDPG_KT_BEGIN(s);
     trsv_wavefront_kernel<N><<<nblk, kTrsvThreads, 0, s>>>(n, LT, n, Dinv, x, sync + nblk + 1, status, 1);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("trsv_wavefront_kernel", s);
 }
 
 template <int N>

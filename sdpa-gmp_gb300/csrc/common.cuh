@@ -36,6 +36,28 @@ extern std::atomic<unsigned long long> g_kernel_launches;
         SDPG_CUDA(cudaGetLastError());                                              \
     } while (0)
 
+// Per-kernel timing (sdpg_kernel_timing): while on, every launch site brackets its
+// kernel with a pair of CUDA events on the launching stream (none inside a stream
+// capture) and the pairs are summed per kernel name when read.
+extern std::atomic<bool> g_kt_on;
+void kt_begin(cudaStream_t s);
+void kt_end(const char *name, cudaStream_t s, double work = 0);
+#define SDPG_KT_BEGIN(s)                                                            \
+    do {                                                                            \
+        if (::sdpg::g_kt_on.load(std::memory_order_relaxed)) ::sdpg::kt_begin(s);   \
+    } while (0)
+#define SDPG_CHECK_LAUNCH_KT(name, s)                                                   \
+    do {                                                                                \
+        SDPG_CHECK_LAUNCH();                                                            \
+        if (::sdpg::g_kt_on.load(std::memory_order_relaxed)) ::sdpg::kt_end(name, s);   \
+    } while (0)
+// the same, with the launch's algorithmic work (bytes or flops, per kernel) recorded
+#define SDPG_CHECK_LAUNCH_KTW(name, s, work)                                                  \
+    do {                                                                                      \
+        SDPG_CHECK_LAUNCH();                                                                  \
+        if (::sdpg::g_kt_on.load(std::memory_order_relaxed)) ::sdpg::kt_end(name, s, work);   \
+    } while (0)
+
 // Device scratch that only grows; one per problem handle (or per C-ABI call).  With an
 // allocation stream set, memory comes from the device's stream-ordered pool
 // (cudaMallocAsync / cudaFreeAsync), so creating and destroying solvers does not

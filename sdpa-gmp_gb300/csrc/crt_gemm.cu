@@ -344,15 +344,22 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
             ops.Q[0] = QA;
             ops.Q[1] = QB;
             const int opad = max(L.Mpad, L.Npad);
+            // algorithmic work of the conversions: every entry of the operands read once
+            // (multi-limb), its kCrtL residues written once (fp16); exponents 4 bytes a row
+            const double entries = ((double)ops.cnt[0] * p.M + (double)ops.cnt[1] * p.Nn) * p.K;
+            const double rows = (double)ops.cnt[0] * p.M + (double)ops.cnt[1] * p.Nn;
             if (ops.cnt[0] + ops.cnt[1] > 0) {
+                SDPG_KT_BEGIN(s);
                 crt_exp_kernel<N><<<dim3(ceil_div(opad, kExpWarps), ops.cnt[0] + ops.cnt[1]), 32 * kExpWarps, 0, s>>>(
                     ops, p.K);
-                SDPG_CHECK_LAUNCH();
+                SDPG_CHECK_LAUNCH_KTW("crt_exp_kernel", s, entries * sizeof(mlf<N>) + rows * 4);
                 const int lg = residue_groups((long long)(L.Kpad / 32) * (opad / 8) * (ops.cnt[0] + ops.cnt[1]));
                 ops.lg[0] = ops.lg[1] = lg;
+                SDPG_KT_BEGIN(s);
                 crt_residue_kernel<N><<<dim3(L.Kpad / 32, opad / 8, (ops.cnt[0] + ops.cnt[1]) * lg), dim3(32, 8), 0,
                                         s>>>(ops, p.K, L.Kpad);
-                SDPG_CHECK_LAUNCH();
+                SDPG_CHECK_LAUNCH_KTW("crt_residue_kernel", s,
+                                      entries * (sizeof(mlf<N>) + 2.0 * kCrtL) + rows * 4);
             }
             TcModGemm t{};
             t.A = QA;
@@ -376,12 +383,18 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
                 t.k0 = k0;
                 t.Kpad = min(kTcMaxK, L.Kpad - k0);
                 t.accumulate = k0 > 0;
+                t.alg_flops = 2.0 * kCrtL * G * (double)p.M * p.Nn * min(kTcMaxK, p.K - k0) *
+                              (p.lower_only ? 0.5 : 1.0);
                 tc_modgemm(t, s);
             }
             if (p.ev_after) SDPG_CUDA(cudaEventRecord(p.ev_after, s));
+            SDPG_KT_BEGIN(s);
             crt_reconstruct_kernel<N><<<dim3(ceil_div((long long)p.M * ((p.Nn + 1) / 2), 128), G), 128, 0, s>>>(
                 Y, L.Mpad, L.Npad, EA, EB, ab ? L.Mpad : 0, bb ? L.Npad : 0, b0, alpha_one, p);
-            SDPG_CHECK_LAUNCH();
+            // every output: its kCrtL residues read, the result written, C read when beta != 0
+            SDPG_CHECK_LAUNCH_KTW("crt_reconstruct_kernel", s,
+                                  (double)G * p.M * p.Nn * (p.lower_only ? 0.5 : 1.0) *
+                                      (2.0 * kCrtL + sizeof(mlf<N>) * (ml_is_zero(p.beta) ? 1 : 2)));
         }
     }
 }

@@ -275,8 +275,9 @@ void k_axpby(long long n, const mlf<N> &a, const mlf<N> *x, const mlf<N> &b, con
              cudaStream_t s) {
     if (n <= 0) return;
     const int b_mode = (ml_is_zero(b) || y == nullptr) ? 0 : (is_one(b) ? 1 : 2);
+    SDPG_KT_BEGIN(s);
     axpby_kernel<N><<<grid1(n), kThreads, 0, s>>>(n, a, x, b, y, out, is_one(a) ? 1 : 0, b_mode);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("axpby_kernel", s);
 }
 
 template <int N>
@@ -288,35 +289,40 @@ void k_copy(long long n, const mlf<N> *x, mlf<N> *out, cudaStream_t s) {
 template <int N>
 void k_fill(long long n, mlf<N> *x, const mlf<N> &v, cudaStream_t s) {
     if (n <= 0) return;
+    SDPG_KT_BEGIN(s);
     fill_kernel<N><<<grid1(n), kThreads, 0, s>>>(n, x, v);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("fill_kernel", s);
 }
 
 template <int N>
 void k_set_identity(int n, mlf<N> *A, const mlf<N> &v, cudaStream_t s) {
+    SDPG_KT_BEGIN(s);
     identity_kernel<N><<<grid1((long long)n * n), kThreads, 0, s>>>(n, A, v);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("identity_kernel", s);
 }
 
 template <int N>
 void k_symmetrize(int n, mlf<N> *A, cudaStream_t s) {
     dim3 blk(16, 16), g(ceil_div(n, 16), ceil_div(n, 16));
+    SDPG_KT_BEGIN(s);
     symmetrize_kernel<N><<<g, blk, 0, s>>>(n, A);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("symmetrize_kernel", s);
 }
 
 template <int N>
 void k_transpose(int n, const mlf<N> *A, mlf<N> *At, cudaStream_t s) {
     dim3 blk(16, 16), g(ceil_div(n, 16), ceil_div(n, 16));
+    SDPG_KT_BEGIN(s);
     transpose_kernel<N><<<g, blk, 0, s>>>(n, A, At);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("transpose_kernel", s);
 }
 
 template <int N>
 void k_zero_strict_upper(int n, mlf<N> *A, cudaStream_t s) {
     dim3 blk(16, 16), g(ceil_div(n, 16), ceil_div(n, 16));
+    SDPG_KT_BEGIN(s);
     zero_upper_kernel<N><<<g, blk, 0, s>>>(n, A);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("zero_upper_kernel", s);
 }
 
 template <int N>
@@ -328,10 +334,12 @@ void k_dot_batched(long long n, const mlf<N> *x, const long long *xoff, const ml
     if (G > 64) G = 64;
     mlf<N> *partial = (mlf<N> *)ws.carve((size_t)G * batch * sizeof(mlf<N>));
     dim3 g(G, batch);
+    SDPG_KT_BEGIN(s);
     dot_partial_kernel<N><<<g, kThreads, 0, s>>>(n, x, xoff, y, yoff, partial);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("dot_partial_kernel", s);
+    SDPG_KT_BEGIN(s);
     sum_partials_kernel<N><<<batch, 64, 0, s>>>(G, partial, out);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("sum_partials_kernel", s);
 }
 
 template <int N>
@@ -345,40 +353,47 @@ void k_maxabs(long long n, const mlf<N> *x, mlf<N> *out, Workspace &ws, cudaStre
     if (G < 1) G = 1;
     if (G > 64) G = 64;
     mlf<N> *partial = (mlf<N> *)ws.carve((size_t)G * sizeof(mlf<N>));
+    SDPG_KT_BEGIN(s);
     maxabs_partial_kernel<N><<<G, kThreads, 0, s>>>(n, x, partial);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("maxabs_partial_kernel", s);
+    SDPG_KT_BEGIN(s);
     maxabs_final_kernel<N><<<1, 64, 0, s>>>(G, partial, out);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("maxabs_final_kernel", s);
 }
 
 template <int N>
 void k_trace(int n, const mlf<N> *A, mlf<N> *out, cudaStream_t s) {
+    SDPG_KT_BEGIN(s);
     trace_kernel<N><<<1, kThreads, 0, s>>>(n, A, out);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("trace_kernel", s);
 }
 
 template <int N>
 void k_constraint_inner(const BlockDev<N> &B, const mlf<N> *M, mlf<N> *g, Workspace &ws, cudaStream_t s) {
     if (B.nc == 0) return;
+    SDPG_KT_BEGIN(s);
     constraint_inner_sparse_kernel<N><<<grid1((long long)B.nc * 32), kThreads, 0, s>>>(B, M, g);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("constraint_inner_sparse_kernel", s);
     if (B.ndense > 0) {
         const long long nn = (long long)B.n * B.n;
         mlf<N> *tmp = (mlf<N> *)ws.carve((size_t)B.ndense * sizeof(mlf<N>));
         k_dot_batched<N>(nn, B.dense, B.dn_off, M, nullptr, B.ndense, tmp, ws, s);
+        SDPG_KT_BEGIN(s);
         add_slots_kernel<N><<<grid1(B.ndense), kThreads, 0, s>>>(B.ndense, B.dn_cid, tmp, g);
-        SDPG_CHECK_LAUNCH();
+        SDPG_CHECK_LAUNCH_KT("add_slots_kernel", s);
     }
 }
 
 template <int N>
 void k_constraint_plus(const BlockDev<N> &B, const mlf<N> *y, mlf<N> *M, cudaStream_t s) {
     const long long nn = (long long)B.n * B.n;
+    SDPG_KT_BEGIN(s);
     constraint_plus_dense_kernel<N><<<grid1(nn), kThreads, 0, s>>>(B, y, M);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("constraint_plus_dense_kernel", s);
     if (B.npos > 0) {
+        SDPG_KT_BEGIN(s);
         constraint_plus_sparse_kernel<N><<<grid1(B.npos), kThreads, 0, s>>>(B, y, M);
-        SDPG_CHECK_LAUNCH();
+        SDPG_CHECK_LAUNCH_KT("constraint_plus_sparse_kernel", s);
     }
 }
 
@@ -386,8 +401,9 @@ template <int N>
 void k_schur_f3(const BlockDev<N> &B, const mlf<N> *X, const mlf<N> *Zinv, mlf<N> *bMat, int m, cudaStream_t s) {
     if (B.nc == 0) return;
     dim3 blk(32, 8), g(ceil_div(B.nc, 32), ceil_div(B.nc, 8));
+    SDPG_KT_BEGIN(s);
     schur_f3_kernel<N><<<g, blk, 0, s>>>(B, X, Zinv, bMat, m);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("schur_f3_kernel", s);
 }
 
 template <int N>
@@ -396,10 +412,12 @@ void k_densify(const BlockDev<N> &B, const int *owners, int cnt, mlf<N> *out, cu
     const long long nn = (long long)B.n * B.n;
     int gx = grid1(nn);
     if (gx > 256) gx = 256;
+    SDPG_KT_BEGIN(s);
     densify_kernel<N><<<dim3(gx, cnt), kThreads, 0, s>>>(B, owners, cnt, out);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("densify_kernel", s);
+    SDPG_KT_BEGIN(s);
     densify_scatter_kernel<N><<<dim3(gx, cnt), kThreads, 0, s>>>(B, owners, cnt, out);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("densify_scatter_kernel", s);
 }
 
 template <int N>
@@ -407,8 +425,9 @@ void k_schur_f1_sparse(const BlockDev<N> &B, const int *owners, int cnt, const m
                        cudaStream_t s) {
     if (cnt <= 0 || B.nc == 0) return;
     dim3 blk(32, 8), g(ceil_div(B.nc, 32), ceil_div(cnt, 8));
+    SDPG_KT_BEGIN(s);
     schur_f1_sparse_kernel<N><<<g, blk, 0, s>>>(B, owners, cnt, G, bMat, m);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("schur_f1_sparse_kernel", s);
 }
 
 template <int N>
@@ -416,8 +435,9 @@ void k_schur_f1_dense_scatter(const BlockDev<N> &B, const int *owners, int cnt, 
                               int m, cudaStream_t s) {
     if (cnt <= 0 || B.ndense == 0) return;
     dim3 blk(32, 8), g(ceil_div(B.ndense, 32), ceil_div(cnt, 8));
+    SDPG_KT_BEGIN(s);
     schur_f1_dense_scatter_kernel<N><<<g, blk, 0, s>>>(B, owners, cnt, P, bMat, m, B.dn_local);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("schur_f1_dense_scatter_kernel", s);
 }
 
 #define SDPG_INST_DENSE(N)                                                                                   \

@@ -368,6 +368,7 @@ __global__ void tridiagonalize_kernel(int n, mlf<N> *A, mlf<N> *dout, mlf<N> *eo
 template <int N>
 void k_matvec(int n, const mlf<N> *A, char op, int tri, const mlf<N> *x, mlf<N> *y, cudaStream_t s) {
     const int g = ceil_div(n, kWarpsPerBlock);
+    SDPG_KT_BEGIN(s);
     if ((op == 'T' || op == 't') && n >= 128)
         matvec_t_split_kernel<N><<<ceil_div(n, kWarpsPerBlock / kMvSplit), 32 * kWarpsPerBlock, 0, s>>>(n, A, tri, x, y,
                                                                                                    nullptr);
@@ -375,7 +376,7 @@ void k_matvec(int n, const mlf<N> *A, char op, int tri, const mlf<N> *x, mlf<N> 
         matvec_t_kernel<N><<<g, 32 * kWarpsPerBlock, 0, s>>>(n, A, tri, x, y);
     else
         matvec_n_kernel<N><<<g, 32 * kWarpsPerBlock, 0, s>>>(n, A, tri, x, y);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("matvec_kernel", s);
 }
 
 template <int N>
@@ -386,8 +387,9 @@ void k_tridiag_min(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *st
         SDPG_CUDA(cudaFuncSetAttribute(tridiag_min_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(2 * kMaxTri * sizeof(mlf<N>))));
     });
+    SDPG_KT_BEGIN(s);
     tridiag_min_kernel<N><<<1, 32, (size_t)(2 * k) * sizeof(mlf<N>), s>>>(k, d, e, out, status, gate);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("tridiag_min_kernel", s);
 }
 
 // ---- Lanczos steps under device control (the loop of Lal::getMinEigen,
@@ -486,21 +488,26 @@ __global__ void lz_control_kernel(mlf<N> *sl, mlf<N> *te, int *ctl, int k, int n
 template <int N>
 void k_lanczos_step(int n, const mlf<N> *M, mlf<N> *r, mlf<N> *q, mlf<N> *qold, mlf<N> *w, mlf<N> *td, mlf<N> *te,
                     mlf<N> *sl, int *ctl, int *status, int k, int eig, int kgo, int kmax, cudaStream_t s) {
+    SDPG_KT_BEGIN(s);
     lz_next_kernel<N><<<ceil_div(n, 128), 128, 0, s>>>(n, r, sl, q, qold, ctl);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("lz_next_kernel", s);
     if (n >= 128) {
+        SDPG_KT_BEGIN(s);
         matvec_t_split_kernel<N><<<ceil_div(n, kWarpsPerBlock / kMvSplit), 32 * kWarpsPerBlock, 0, s>>>(n, M, 0, q, w,
                                                                                                    ctl);
     } else {
+        SDPG_KT_BEGIN(s);
         matvec_t_kernel<N><<<ceil_div(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(n, M, 0, q, w, ctl);
     }
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KTW("lz_matvec_kernel", s, ((double)n * n + 2.0 * n) * sizeof(mlf<N>));
+    SDPG_KT_BEGIN(s);
     lz_update_kernel<N><<<1, 256, 0, s>>>(n, w, q, qold, td, te, sl, r, ctl, k, eig, kgo, kmax);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("lz_update_kernel", s);
     if (eig) {
         k_tridiag_min<N>(k + 1, td, te, sl + 4, status, s, ctl);
+        SDPG_KT_BEGIN(s);
         lz_control_kernel<N><<<1, 1, 0, s>>>(sl, te, ctl, k, n, kgo, kmax);
-        SDPG_CHECK_LAUNCH();
+        SDPG_CHECK_LAUNCH_KT("lz_control_kernel", s);
     }
 }
 
@@ -544,15 +551,17 @@ __global__ void lp_ratio_min_kernel(int n, const mlf<N> *X, const mlf<N> *L, mlf
 
 template <int N>
 void k_lp_ratio_min(int n, const mlf<N> *X, const mlf<N> *L, mlf<N> *out, cudaStream_t s) {
+    SDPG_KT_BEGIN(s);
     lp_ratio_min_kernel<N><<<1, 256, 0, s>>>(n, X, L, out);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("lp_ratio_min_kernel", s);
 }
 
 template <int N>
 void k_tridiagonalize_small(int n, mlf<N> *A, mlf<N> *d, mlf<N> *e, cudaStream_t s) {
     if (n > 64) throw sdpg_error(SDPG_ERR_TOO_LARGE, "small tridiagonalisation limited to n <= 64");
+    SDPG_KT_BEGIN(s);
     tridiagonalize_kernel<N><<<1, 128, 0, s>>>(n, A, d, e);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("tridiagonalize_kernel", s);
 }
 
 #define SDPG_INST_EIG(N)                                                                                  \

@@ -290,21 +290,25 @@ void ml_gemm_scratch(const GemmProblem<N> &p, void *scratch, cudaStream_t stream
     // exponents
     {
         dim3 g(ceil_div(L.Mpad, kQuantWarps), L.batchA);
+        SDPG_KT_BEGIN(stream);
         bfp_exp_kernel<N><<<g, 32 * kQuantWarps, 0, stream>>>(p.A, p.M, p.K, L.Mpad, EA);
-        SDPG_CHECK_LAUNCH();
+        SDPG_CHECK_LAUNCH_KT("bfp_exp_kernel", stream);
         dim3 g2(ceil_div(L.Npad, kQuantWarps), L.batchB);
+        SDPG_KT_BEGIN(stream);
         bfp_exp_kernel<N><<<g2, 32 * kQuantWarps, 0, stream>>>(p.B, p.Nn, p.K, L.Npad, EB);
-        SDPG_CHECK_LAUNCH();
+        SDPG_CHECK_LAUNCH_KT("bfp_exp_kernel", stream);
     }
     // digits
     {
         dim3 blk(32, 8);
         dim3 g(ceil_div(L.Mpad, 32), ceil_div(L.Kpad, 8), L.batchA);
+        SDPG_KT_BEGIN(stream);
         bfp_digits_kernel<N><<<g, blk, 0, stream>>>(p.A, p.M, p.K, L.Mpad, L.Kpad, EA, Aq);
-        SDPG_CHECK_LAUNCH();
+        SDPG_CHECK_LAUNCH_KT("bfp_digits_kernel", stream);
         dim3 g2(ceil_div(L.Npad, 32), ceil_div(L.Kpad, 8), L.batchB);
+        SDPG_KT_BEGIN(stream);
         bfp_digits_kernel<N><<<g2, blk, 0, stream>>>(p.B, p.Nn, p.K, L.Npad, L.Kpad, EB, Bq);
-        SDPG_CHECK_LAUNCH();
+        SDPG_CHECK_LAUNCH_KT("bfp_digits_kernel", stream);
     }
     constexpr int D = Bfp<N>::D;
     const long long sAq = (p.A.sb == 0) ? 0 : (long long)D * L.Kpad * L.Mpad;
@@ -316,9 +320,10 @@ void ml_gemm_scratch(const GemmProblem<N> &p, void *scratch, cudaStream_t stream
     const mlf<N> one = ml_one<N>();
     const int alpha_one = memcmp(&one, &p.alpha, sizeof(one)) == 0;
     if (p.ev_before) SDPG_CUDA(cudaEventRecord(p.ev_before, stream));
+    SDPG_KT_BEGIN(stream);
     bfp_gemm_kernel<N, T::BM, T::BN, T::BK, T::TM, T::TN><<<grid, threads, 0, stream>>>(
         Aq, Bq, EA, EB, L.Mpad, L.Npad, L.Kpad, sAq, sBq, sEA, sEB, alpha_one, p);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("bfp_gemm_kernel", stream);
     if (p.ev_after) SDPG_CUDA(cudaEventRecord(p.ev_after, stream));
 }
 

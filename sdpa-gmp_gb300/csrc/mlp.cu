@@ -246,9 +246,10 @@ void ensure_smem(int device) {
 void launch(const Policy &p, const float *X, const float *T, const float *M, const int *perm, int first, int count,
             float inv_batch, float *Y, float *G, float *loss, cudaStream_t s) {
     ensure_smem(p.device);
+    SDPG_KT_BEGIN(s);
     policy_kernel<<<(count + kTile - 1) / kTile, kThreads, kSmemBytes, s>>>(p.params, p.scale, X, T, M, perm, first,
                                                                          count, inv_batch, Y, G, loss);
-    SDPG_CHECK_LAUNCH();
+    SDPG_CHECK_LAUNCH_KT("policy_kernel", s);
 }
 
 Policy &get(sdpg_policy *h) {
@@ -434,9 +435,10 @@ int sdpg_policy_train(sdpg_policy *h, const float *x, const float *t, const floa
                     ++p.adam_step;
                     const float bc1 = (float)(1.0 - pow((double)b1, (double)p.adam_step));
                     const float bc2 = (float)(1.0 - pow((double)b2, (double)p.adam_step));
+                    SDPG_KT_BEGIN(s);
                     policy_adam_kernel<<<(kPolParams + 255) / 256, 256, 0, s>>>(p.params, p.grad, p.m1, p.m2,
                                                                                kPolParams, lr, b1, b2, eps, bc1, bc2);
-                    SDPG_CHECK_LAUNCH();
+                    SDPG_CHECK_LAUNCH_KT("policy_adam_kernel", s);
                 }
                 // the host permutation is rewritten next epoch: wait for its copy
                 SDPG_CUDA(cudaStreamSynchronize(s));

@@ -453,6 +453,10 @@ class Solver final : public SolverBase {
     };
     template <class F>
     void graphed(GraphSlot &g, cudaStream_t st, F &&f) {
+        if (g_kt_on.load(std::memory_order_relaxed)) {  // per-kernel timing: plain launches
+            f();
+            return;
+        }
         if (g.exec) {
             SDPG_CUDA(cudaGraphLaunch(g.exec, st));
             g_kernel_launches.fetch_add(g.launches, std::memory_order_relaxed);
@@ -1366,8 +1370,33 @@ class Solver final : public SolverBase {
         fflush(trace_);
     }
 
-    // one pass of pinpal's main loop body, sdpa_main.cpp:294-384
+    // SDPG_ERR_TIMEOUT if a tensor-core GEMM of this solver gave up a bounded wait (its
+    // products, and everything computed from them, are then invalid)
+    void check_tensor_timeout() {
+        if (N != 8 || !tc_error_) return;
+        int st = 0;
+        d2h_ += (long long)sizeof(int);
+        SDPG_CUDA(cudaMemcpyAsync(&st, tc_error_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+        SDPG_CUDA(cudaStreamSynchronize(st_));
+        if (st != 0) throw sdpg_error(SDPG_ERR_TIMEOUT, "tensor-core GEMM: a bounded wait timed out");
+    }
+
+    // A time-out takes precedence over whatever the invalid products made happen next
+    // (a failed factorisation, a stop, a non-converged eigenvalue).
     int iterate(FILE *out) override {
+        int r = 0;
+        try {
+            r = iterate_body(out);
+        } catch (const sdpg_error &e) {
+            if (e.code != SDPG_ERR_TIMEOUT) check_tensor_timeout();
+            throw;
+        }
+        if (r == 0) check_tensor_timeout();
+        return r;
+    }
+
+    // one pass of pinpal's main loop body, sdpa_main.cpp:294-384
+    int iterate_body(FILE *out) {
         if (!initialized_) initialize();
         if (stopped_) return 0;
         if (!(phase_updateCheck() && iter_ < par_.maxIteration)) return stop();
@@ -1397,16 +1426,8 @@ class Solver final : public SolverBase {
                 step_length(1);
             }
         }
-        {
-            // the tensor-core GEMMs' bounded waits (step_length has synchronised the streams)
-            int st = 0;
-            if (N == 8 && g_gemm_method != 1) {
-                d2h_ += (long long)sizeof(int);
-                SDPG_CUDA(cudaMemcpyAsync(&st, tc_error_, sizeof(int), cudaMemcpyDeviceToHost, st_));
-                SDPG_CUDA(cudaStreamSynchronize(st_));
-                if (st != 0) throw sdpg_error(SDPG_ERR_TIMEOUT, "tensor-core GEMM: a bounded wait timed out");
-            }
-        }
+        // the tensor-core GEMMs' bounded waits (step_length has synchronised the streams)
+        if (g_gemm_method != 1) check_tensor_timeout();
         record_iteration();
         feats_.push_back(feat);
         lastAP_ = aP_;
@@ -1417,25 +1438,70 @@ class Solver final : public SolverBase {
             cannot_move_ = true;
             return stop();
         }
-        // RatioInitResCurrentRes::update (:692-698)
-        if (reductionOn_) {
-            thP_ = rabs((R(1.0) - aP_) * thP_);
-            thD_ = rabs((R(1.0) - aD_) * thD_);
-        }
-        // AverageComplementarity::update (:647-651)
-        muCur_ = ip_blocks(&Blk::X, &Blk::Z) / R(nDim_);
-        residuals();
-        // RatioInitResCurrentRes::update_exact (:700-708)
-        thP_ = (initNormP_ > R(1.0e-10)) ? normP_ / initNormP_ : R(0.0);
-        thD_ = (initNormD_ > R(1.0e-10)) ? normD_ / initNormD_ : R(0.0);
-        solveInfo_update();
-        ++iter_;
+        loop_after_update();
         return 1;
     }
 
     int stop() {
         stopped_ = true;
         return 0;
+    }
+
+    // ---------------------------------------------------------------- main-loop steps
+    // (the C++ drop-in classes drive the loop through these, in pinpal's order)
+    bool loop_phase_check() override {
+        if (!initialized_) initialize();
+        return phase_updateCheck();
+    }
+    void loop_direction(int corrector) override {
+        if (corrector) direction_corrector();
+        else direction_predictor();
+    }
+    bool loop_corrector_break() const override { return phase_ == pdFEAS && (betaV_ > R(5) || objP_ < objD_); }
+    void loop_record(FILE *out, FILE *display) override {
+        if (g_gemm_method != 1) check_tensor_timeout();
+        record_iteration();
+        feats_.push_back(policy_features(betaV_));
+        lastAP_ = aP_;
+        lastAD_ = aD_;
+        print_iteration(out);
+        if (display) print_iteration_row(display, hist_.size() - 1);
+    }
+    bool loop_update() override {
+        if (!update()) {
+            cannot_move_ = true;
+            return false;
+        }
+        return true;
+    }
+    void loop_after_update() override {
+        // RatioInitResCurrentRes::update (sdpa_parts.cpp:692-698)
+        if (reductionOn_) {
+            thP_ = rabs((R(1.0) - aP_) * thP_);
+            thD_ = rabs((R(1.0) - aD_) * thD_);
+        }
+        // AverageComplementarity::update (:647-651), Residuals::update
+        muCur_ = ip_blocks(&Blk::X, &Blk::Z) / R(nDim_);
+        residuals();
+        // RatioInitResCurrentRes::update_exact (:700-708), SolveInfo::update
+        thP_ = (initNormP_ > R(1.0e-10)) ? normP_ / initNormP_ : R(0.0);
+        thD_ = (initNormD_ > R(1.0e-10)) ? normD_ / initNormD_ : R(0.0);
+        solveInfo_update();
+        ++iter_;
+    }
+    void loop_values(int *phase, int *iteration, void *out9) const override {
+        *phase = phase_;
+        *iteration = iter_;
+        V *o = (V *)out9;
+        const R vals[9] = {betaV_, objP_, objD_, muCur_, muInit_, aP_, aD_, thP_, thD_};
+        for (int i = 0; i < 9; ++i) o[i] = vals[i].v;
+    }
+    void loop_finish(FILE *out, FILE *display) override {
+        if (cannot_move_ && display) fprintf(display, "cannot move\n");
+        residuals();
+        final_phase_ = reverse_phase(phase_);
+        print_last(out);
+        print_last(display);
     }
 
     // pinpal's main loop, sdpa_main.cpp:294-385

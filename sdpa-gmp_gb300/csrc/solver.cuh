@@ -49,6 +49,19 @@ class SolverBase {
     // One pass of the main-loop body (sdpa_main.cpp:294-384): 1 = iterated, 0 = the loop
     // condition or a break stopped it (phase decided, Cholesky failure, cannot move).
     virtual int iterate(FILE *out) = 0;
+    // The main loop's steps one at a time, in the order pinpal calls them
+    // (sdpa_main.cpp:294-398); run() / iterate() are these steps in sequence.
+    virtual bool loop_phase_check() = 0;                    // Phase::updateCheck
+    virtual void loop_direction(int corrector) = 0;         // Switch + DirectionParameter::Mehrotra*
+    virtual bool loop_corrector_break() const = 0;          // the pdFEAS stopping rule (:337)
+    virtual void loop_record(FILE *out, FILE *display) = 0;  // IO::printOneIteration
+    virtual bool loop_update() = 0;                          // Solutions::update ("cannot move")
+    virtual void loop_after_update() = 0;  // theta, mu, Residuals::update, SolveInfo::update, iteration
+    virtual void loop_finish(FILE *out, FILE *display) = 0;  // Residuals::compute, Phase::reverse, printLastInfo
+    // the loop's state as the reference's objects hold it: the phase (not reversed), the
+    // iteration count, and 9 ml values: beta, objValPrimal (C.X), objValDual (b.y), mu,
+    // initial mu, alphaP, alphaD, thetaP, thetaD
+    virtual void loop_values(int *phase, int *iteration, void *out9) const = 0;
     virtual bool newton(int corrector) = 0;                 // Newton::Mehrotra
     virtual void step_length(int corrector) = 0;            // StepLength::Mehrotra{Predictor,Corrector}
     virtual bool update() = 0;                              // Solutions::update

@@ -47,11 +47,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
-// false if the phase with the given parity has not completed within the budget
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// false if the phase with the given parity has not completed within `budget` cycles
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long budget = kWaitCycles) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > budget) return false;
     return true;
 }
 
@@ -174,13 +174,16 @@ __global__ void __launch_bounds__(128, 1)
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
+    // The producer's and the MMA issuer's waits use the primary budget p.wait_cycles;
+    // the waits that drain work already issued (products before tensor memory is freed,
+    // copies before the CTA exits) always use the full budget.
+    int issued = 0;  // TMA stages issued (producer thread)
     if (threadIdx.x == 0) {
         // producer: TMA into the stage ring
-        int issued = 0;
         bool ok = true;
         for (int kb = 0; kb < nk; ++kb) {
             const int s = kb % kStages;
-            if (kb >= kStages && !mbar_wait(smem_u32(&empty[s]), ((kb / kStages) - 1) & 1)) {
+            if (kb >= kStages && !mbar_wait(smem_u32(&empty[s]), ((kb / kStages) - 1) & 1, p.wait_cycles)) {
                 ok = false;
                 break;
             }
@@ -194,16 +197,13 @@ __global__ void __launch_bounds__(128, 1)
         if (!ok) {
             record_error(p, 1);
             abort_flag = 1;
-            // let the copies already issued land before the CTA goes away
-            for (int kb = (issued > kStages ? issued - kStages : 0); kb < issued; ++kb)
-                mbar_wait(smem_u32(&full[kb % kStages]), (kb / kStages) & 1);
         }
     } else if (threadIdx.x == 32) {
         // MMA issuer
         bool ok = true;
         for (int kb = 0; kb < nk; ++kb) {
             const int s = kb % kStages;
-            if (!mbar_wait(smem_u32(&full[s]), (kb / kStages) & 1)) {
+            if (!mbar_wait(smem_u32(&full[s]), (kb / kStages) & 1, p.wait_cycles)) {
                 ok = false;
                 break;
             }
@@ -229,6 +229,14 @@ __global__ void __launch_bounds__(128, 1)
     if (!mbar_wait(smem_u32(done), 0)) {
         record_error(p, 3);
         abort_flag = 1;
+    }
+    __syncthreads();
+    if (abort_flag && threadIdx.x == 0) {
+        // let the copies already issued land before the CTA goes away: a stage's last
+        // issued copy is among the last kStages (an earlier one was consumed before its
+        // stage was refilled)
+        for (int kb = (issued > kStages ? issued - kStages : 0); kb < issued; ++kb)
+            mbar_wait(smem_u32(&full[kb % kStages]), (kb / kStages) & 1);
     }
     __syncthreads();
     tc_fence_after();
@@ -328,6 +336,8 @@ CUtensorMap make_map(const __half *base, long long rows, int cols) {
 
 }  // namespace
 
+long long g_tc_wait_cycles = 0;
+
 void tc_modgemm(const TcModGemm &p, cudaStream_t s) {
     if (p.Mpad % kTcBM || p.Npad % kTcBN || p.Kpad % kTcBK || p.Kpad <= 0 || p.Kpad > kTcMaxK || p.L <= 0 ||
         p.batch <= 0 || p.k0 % kTcBK || p.k0 < 0 || p.kpitch % kTcBK || p.k0 + p.Kpad > p.kpitch)
@@ -343,8 +353,11 @@ void tc_modgemm(const TcModGemm &p, cudaStream_t s) {
     const CUtensorMap ma = make_map(p.A, arows, p.kpitch);
     const CUtensorMap mb = make_map(p.B, brows, p.kpitch);
     dim3 grid(p.Npad / kTcBN, p.Mpad / kTcBM, p.batch * p.L);
-    tc_modgemm_kernel<<<grid, 128, kSmemBytes, s>>>(ma, mb, p);
-    SDPG_CHECK_LAUNCH();
+    TcModGemm q = p;
+    q.wait_cycles = g_tc_wait_cycles > 0 ? g_tc_wait_cycles : kWaitCycles;
+    SDPG_KT_BEGIN(s);
+    tc_modgemm_kernel<<<grid, 128, kSmemBytes, s>>>(ma, mb, q);
+    SDPG_CHECK_LAUNCH_KTW("tc_modgemm_kernel", s, p.alg_flops);
 }
 
 }  // namespace sdpg

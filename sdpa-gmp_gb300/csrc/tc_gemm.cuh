@@ -36,7 +36,14 @@ struct TcModGemm {
     const int *moduli;     // device, L entries
     int *error;            // device word of the caller: set non-zero if a bounded wait timed out
     int *sticky;           // device-wide flag, also set (may equal error or be null)
+    long long wait_cycles; // budget of the producer's and MMA issuer's waits (set by tc_modgemm)
+    double alg_flops;      // algorithmic fp16 flops of this call (per-kernel timing only)
 };
+
+// Budget in clock cycles of the tensor-core kernel's primary waits (TMA data, free
+// stages); 0 = the default of about one second.  Shortening it is a test hook that makes
+// those waits give up; the drains after a give-up keep the full budget.
+extern long long g_tc_wait_cycles;
 
 // Y planes for all (b, l); grid (Npad/128, Mpad/128, batch*L), 128 threads, one tile each.
 void tc_modgemm(const TcModGemm &p, cudaStream_t s);

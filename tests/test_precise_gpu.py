@@ -36,7 +36,7 @@ BOUNDS = {
     "gpp500_hp": (-150, -100, -100),
     "control231_hp": (-150, -100, -100),
     "maxcut124pm_hp": (-150, -100, -100),
-    "maxcut100_hp": (-150, -100, -100),
+    "maxcut100_hp": (-120, -85, -70),
 }
 # the full graph-partition solve stops in pFEAS when the step collapses (no strictly
 # feasible primal point); where exactly depends on rounding, so its iteration count
