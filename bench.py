@@ -493,30 +493,59 @@ def bench_batch(args) -> None:
     on the first --serial instances; prints solves/s for both."""
     import numpy as np
     import torch
+    world, rank, local, dist = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
     sdpg = importlib.import_module("sdpa-gmp_gb300")
     problems = importlib.import_module("sdpa-gmp_gb300.problems")
+    shard = importlib.import_module("sdpa-gmp_gb300.shard")
+    # instances are partitioned over the ranks by estimated cost (sum n_b^3 + m^3); each
+    # rank builds and solves only its own, and rank 0 gathers the per-instance results
+    sizes = [problems.batch_instance_size(seed) for seed in range(args.batch)]
+    costs = [shard.instance_cost(m, bl) for m, bl in sizes]
+    mine = shard.partition(costs, world)[rank]
     t0 = time.perf_counter()
-    probs = [sdpg.Problem.from_dense(*problems.batch_instance(seed)) for seed in range(args.batch)]
+    probs = {seed: sdpg.Problem.from_dense(*problems.batch_instance(seed)) for seed in mine}
     gen_s = time.perf_counter() - t0
     param = sdpg.Param.default()
     param.precision = args.precision
     # warm-up: one small solve (library set-up, tensor-core tables)
-    sdpg.solve_batch(probs[:1], param, concurrency=1)
+    if mine:
+        sdpg.solve_batch([probs[mine[0]]], param, device=local, concurrency=1)
     torch.cuda.synchronize()
+    barrier(dist)
     t0 = time.perf_counter()
-    its, info = sdpg.solve_batch(probs, param, concurrency=args.concurrency)
-    torch.cuda.synchronize()
-    batched_s = time.perf_counter() - t0
+
+    def solve_mine(seeds):
+        if not seeds:
+            return []
+        its_, info_ = sdpg.solve_batch([probs[s] for s in seeds], param, device=local,
+                                       concurrency=args.concurrency)
+        torch.cuda.synchronize()
+        return [(int(a), [float(v) for v in b]) for a, b in zip(its_, info_)]
+
+    gathered = shard.solve_sharded(list(range(args.batch)), costs, solve_mine, rank, world, dist)
+    batched_s = max_over_ranks(dist, time.perf_counter() - t0)
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    its = np.array([g[0] for g in gathered])
+    info = np.array([g[1] for g in gathered])
     ns = min(args.serial, args.batch)
+    serial_probs = [probs[s] if s in probs else sdpg.Problem.from_dense(*problems.batch_instance(s))
+                    for s in range(ns)]
     t0 = time.perf_counter()
-    its_s, info_s = sdpg.solve_batch(probs[:ns], param, concurrency=1)
+    its_s, info_s = sdpg.solve_batch(serial_probs, param, device=local, concurrency=1)
     torch.cuda.synchronize()
     serial_s = time.perf_counter() - t0
     phases = [sdpg.PHASES[int(x)] for x in info[:, 0]]
     line = {"metric": f"batched solves/s ({args.precision}-bit control/LMI SDPs, m~U[20,350], two blocks ~U[15,90])",
-            "value": args.batch / batched_s, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+            "value": args.batch / batched_s, "unit": "solves/s", "n_gpus": world, "higher_is_better": True,
+            "scaling": "strong",
             "config": {"workload": f"{args.batch} instances, seeds 0..{args.batch - 1}",
-                       "concurrency": args.concurrency, "precision_bits": args.precision},
+                       "concurrency": args.concurrency, "precision_bits": args.precision,
+                       "sharding": f"instances partitioned over {world} rank(s) by sum n_b^3 + m^3, "
+                                   "results gathered on rank 0"},
             "serial": {"value": ns / serial_s, "unit": "solves/s", "instances": ns},
             "speedup_vs_serial": (args.batch / batched_s) / (ns / serial_s),
             "iterations_mean": float(np.mean(its)), "pdOPT": sum(p == "pdOPT" for p in phases),
@@ -524,6 +553,8 @@ def bench_batch(args) -> None:
             "identical_to_serial": bool(np.array_equal(info[:ns], info_s)),
             "generation_s": gen_s, "data": "synthetic (seeded generator)"}
     print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
 
 
 def bench_learned(args) -> None:
@@ -536,13 +567,20 @@ def bench_learned(args) -> None:
     pol = sdpg.Policy.load(learned.POLICY_FILE)
     seeds = range(learned.HOLDOUT_BASE, learned.HOLDOUT_BASE + args.batch)
     t0 = time.perf_counter()
-    ev = learned.evaluate(pol, seeds, workers=args.concurrency)
+    ev = learned.evaluate(pol, seeds, workers=args.concurrency, constant=learned.BEST_CONSTANT)
     secs = time.perf_counter() - t0
     line = {"metric": "mean IPM iterations to pdOPT, learned lambdaStar/beta vs default (MaxCut n=124, +-1)",
             "value": ev["mean_iterations_learned"], "unit": "iterations", "n_gpus": 1, "higher_is_better": False,
             "config": {"workload": f"{args.batch} held-out seeds from {learned.HOLDOUT_BASE}",
                        "precision_bits": learned.PRECISION, "policy": os.path.basename(learned.POLICY_FILE)},
             "default_iterations": ev["mean_iterations_default"], "iteration_reduction": ev["iteration_reduction"],
+            "ablation": {"default": ev["mean_iterations_default"], "best_constant": ev["mean_iterations_constant"],
+                         "policy": ev["mean_iterations_learned"], "constant": ev["constant"],
+                         "constant_reduction_vs_default": ev["constant_reduction"],
+                         "policy_reduction_vs_constant": ev["learned_vs_constant"],
+                         "seeds_policy_better": ev["seeds_learned_better"],
+                         "seeds_constant_better": ev["seeds_constant_better"],
+                         "max_constant_objective_rel_error": ev["max_constant_objective_rel_error"]},
             "fallback_solves": ev["fallback_solves"], "beta_fallback_rate": ev["beta_fallback_rate"],
             "mean_lambda_star": ev["mean_lambda"], "max_objective_rel_error": ev["max_objective_rel_error"],
             "seconds": secs, "data": "synthetic (seeded generator)"}

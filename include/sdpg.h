@@ -130,7 +130,10 @@ int sdpg_solve_systems(int limbs, int n, const void *L, int ldl, void *x);
  * Lal::getMinEigen reads from Rsteqr (sdpa_linear.cpp:65-112). */
 int sdpg_tridiag_min(int limbs, int k, const void *d, const void *e, void *out2);
 /* Smallest eigenvalue of a dense symmetric n x n (n <= 64, lower triangle read) --
- * replaces Lal::getMinEigenValue (sdpa_linear.cpp:126-158, Rsyev 'N' 'L'). */
+ * replaces Lal::getMinEigenValue (sdpa_linear.cpp:126-158, Rsyev 'N' 'L').
+ * SDPG_ERR_NOCONV (out still written) when the Newton iteration on the characteristic
+ * polynomial did not reach full precision within its step limit, as happens for a
+ * tight cluster of smallest eigenvalues (a nearly singular matrix). */
 int sdpg_sym_min_eigen(int limbs, int n, const void *A, void *out);
 
 /* ---- the interior-point solver ------------------------------------------------ */
@@ -290,6 +293,13 @@ long long sdpg_set_tensor_wait_budget(long long cycles);
 /* Measured throughput of signed 32x32->64 multiply-adds (IMAD.WIDE) on one GPU, the
  * instruction the multi-limb GEMM is built from; the plain path's roofline denominator. */
 int sdpg_probe_imad_wide(int device, double *ops_per_second);
+/* Measured throughput of one tensor instruction on one GPU, in multiply-add operations
+ * (2 per MAC) per second, from fixed operands with no memory traffic (no reference
+ * counterpart: it records why the residue GEMM uses fp16 products).  kind 0:
+ * tcgen05.mma kind::f16 (fp16 x fp16 -> fp32, M = 128, N = 256, one CTA per SM);
+ * 1: mma.sync m16n8k32 s8 x s8 -> s32 (tcgen05.mma kind::i8 does not exist for sm_103a);
+ * 2: mma.sync m16n8k16 f16 x f16 -> f32. */
+int sdpg_probe_tensor_rate(int device, int kind, double *ops_per_second);
 /* Batched solves (no reference counterpart; the reference solves one problem per
  * process): `count` problems with one parameter set (NULL: defaults), up to
  * `concurrency` solvers in flight at once, one host thread and its own CUDA streams

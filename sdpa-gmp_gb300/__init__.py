@@ -117,6 +117,7 @@ def _setup(lib: ctypes.CDLL) -> ctypes.CDLL:
         "sdpg_kernel_timing": (i, [i]),
         "sdpg_kernel_times": (i, [c.c_char_p, i]),
         "sdpg_probe_imad_wide": (i, [i, c.POINTER(c.c_double)]),
+        "sdpg_probe_tensor_rate": (i, [i, i, c.POINTER(c.c_double)]),
         "sdpg_solve_file": (i, [c.c_char_p, c.c_char_p, c.c_char_p, i, c.POINTER(c.c_double)]),
         "sdpg_policy_create": (i, [i, c.POINTER(vp)]),
         "sdpg_policy_destroy": (None, [vp]),
@@ -636,6 +637,19 @@ def probe_imad_wide(device: int = 0) -> float:
     """Measured IMAD.WIDE (signed 32x32->64 multiply-add) operations per second."""
     out = ctypes.c_double()
     check(lib().sdpg_probe_imad_wide(device, ctypes.byref(out)))
+    return out.value
+
+
+TENSOR_PROBE_KINDS = {0: "tcgen05.mma kind::f16 (fp16 x fp16 -> fp32), M128 N256",
+                      1: "mma.sync m16n8k32 s8 x s8 -> s32",
+                      2: "mma.sync m16n8k16 f16 x f16 -> f32"}
+
+
+def probe_tensor_rate(kind: int, device: int = 0) -> float:
+    """Measured multiply-add operations (2 per MAC) per second of one tensor instruction
+    (TENSOR_PROBE_KINDS) from fixed operands, no memory traffic."""
+    out = ctypes.c_double()
+    check(lib().sdpg_probe_tensor_rate(device, kind, ctypes.byref(out)))
     return out.value
 
 

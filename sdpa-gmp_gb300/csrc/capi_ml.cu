@@ -347,7 +347,10 @@ int sdpg_sym_min_eigen(int limbs, int n, const void *A, void *out) {
             k_tridiagonalize_small<N>(n, (mlf<N> *)dA.p, (mlf<N> *)dd.p, (mlf<N> *)de.p, nullptr);
             k_tridiag_min<N>(n, (const mlf<N> *)dd.p, (const mlf<N> *)de.p, (mlf<N> *)dout.p, (int *)dst.p, nullptr);
             SDPG_CUDA(cudaDeviceSynchronize());
+            int st = 0;
+            SDPG_CUDA(cudaMemcpy(&st, dst.p, sizeof(int), cudaMemcpyDeviceToHost));
             SDPG_CUDA(cudaMemcpy(out, dout.p, eb, cudaMemcpyDeviceToHost));
+            if (st != 0) throw sdpg_error(SDPG_ERR_NOCONV, "smallest eigenvalue: Newton iteration did not converge");
             return (int)SDPG_OK;
         });
     });

@@ -4,7 +4,9 @@
 #include "gemm.cuh"
 #include "sdpg.h"
 #include "tc_gemm.cuh"
+#include "tcgen05.cuh"
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -79,11 +81,184 @@ __global__ void imad_wide_probe_kernel(const int *in, long long *out, int iters)
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// ---- tensor-instruction throughput probes -------------------------------------------
+//
+// Which tensor instruction carries the residue GEMM was settled by these rates.
+// sdpg_probe_tensor_rate(kind):
+//   0  tcgen05.mma kind::f16 (fp16 x fp16 -> fp32 in tensor memory), the residue GEMM's
+//      instruction: one CTA per SM; one thread issues `rounds` x 4 products of
+//      M = 128, N = 256, K = 16 into one accumulator from fixed shared-memory operands
+//      (no memory traffic), then waits for them on an mbarrier (bounded).
+//   1  mma.sync m16n8k32 s8 x s8 -> s32, the 8-bit integer tensor instruction this target
+//      accepts (ptxas rejects tcgen05.mma kind::i8 for sm_103a).
+//   2  mma.sync m16n8k16 f16 x f16 -> f32, the legacy form of kind 0.
+constexpr int kProbeN = 256;
+constexpr int kProbeTileA = 128 * 128;  // 128 rows of one 128-byte swizzle row
+constexpr int kProbeTileB = kProbeN * 128;
+constexpr int kProbeSmem = kProbeTileA + kProbeTileB + 1024 + 64;
+constexpr int kProbeRounds = 2048;
+// shared memory requested per CTA: more than half the SM's, so each SM holds one CTA
+constexpr int kProbeSmemLaunch = 120 * 1024;
+static_assert(kProbeSmem <= kProbeSmemLaunch, "probe shared memory");
+
+__global__ void __launch_bounds__(128, 1) tc_f16_rate_probe_kernel(int rounds, int *status) {
+    using namespace tc;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *tA = smem, *tB = smem + kProbeTileA;
+    uint64_t *bar = (uint64_t *)(tB + kProbeTileB);
+    uint32_t *slot = (uint32_t *)(bar + 1);
+    const int t = threadIdx.x;
+    // operands: fp16 ones and zeros (the values do not matter for the rate)
+    for (int i = t; i < (kProbeTileA + kProbeTileB) / 16; i += blockDim.x)
+        reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0x3C003C00u, 0u, 0x00003C00u, 0u);
+    if (t == 0) {
+        mbar_init(smem_u32(bar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (t < 32) {
+        tmem_alloc(smem_u32(slot), kProbeN);
+        tmem_relinquish();
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *slot;
+    if (t == 0) {
+        const uint64_t ad = sw128_kmajor_desc(smem_u32(tA)), bd = sw128_kmajor_desc(smem_u32(tB));
+        constexpr uint32_t idesc = idesc_f16_f32(128, kProbeN);
+        for (int r = 0; r < rounds; ++r) {
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+                tc_mma(tmem, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), idesc, (r | kk) ? 1u : 0u);
+        }
+        tc_commit(smem_u32(bar));
+        // the products are issued: wait for them with the full budget, and once more if
+        // that ran out, so none is in flight when the tensor memory is freed
+        if (!mbar_wait(smem_u32(bar), 0)) {
+            atomicExch(status, 1);
+            mbar_wait(smem_u32(bar), 0);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (t < 32) {
+        tc_fence_after();
+        tmem_dealloc(tmem, kProbeN);
+    }
+}
+
+// Eight independent accumulator chains per warp; each mma depends on its own previous
+// result only, so the loop cannot be folded.
+template <bool kInt8>
+__global__ void mma_sync_rate_probe_kernel(int iters, uint32_t seed, uint32_t *out) {
+    const uint32_t x = seed ^ (threadIdx.x * 0x9E3779B9u) ^ blockIdx.x;
+    const uint32_t a0 = x & 0x3F3F3F3Fu, a1 = (x >> 3) & 0x3F3F3F3Fu, a2 = (x >> 5) & 0x3F3F3F3Fu,
+                   a3 = (x >> 7) & 0x3F3F3F3Fu;
+    const uint32_t b0 = (x * 3u) & 0x3F3F3F3Fu, b1 = (x * 5u) & 0x3F3F3F3Fu;
+    uint32_t acc[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[j][q] = 0u;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if constexpr (kInt8) {
+                asm volatile(
+                    "mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+                    "{%8, %9}, {%0, %1, %2, %3};"
+                    : "+r"(acc[j][0]), "+r"(acc[j][1]), "+r"(acc[j][2]), "+r"(acc[j][3])
+                    : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+            } else {
+                // fp16 operands: the low bits of x as normal numbers in [0.5, 1)
+                asm volatile(
+                    "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+                    "{%8, %9}, {%0, %1, %2, %3};"
+                    : "+r"(acc[j][0]), "+r"(acc[j][1]), "+r"(acc[j][2]), "+r"(acc[j][3])
+                    : "r"((a0 & 0x03FF03FFu) | 0x38003800u), "r"((a1 & 0x03FF03FFu) | 0x38003800u),
+                      "r"((a2 & 0x03FF03FFu) | 0x38003800u), "r"((a3 & 0x03FF03FFu) | 0x38003800u),
+                      "r"((b0 & 0x03FF03FFu) | 0x38003800u), "r"((b1 & 0x03FF03FFu) | 0x38003800u));
+            }
+        }
+    }
+    uint32_t s = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s ^= acc[j][q];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace
 
 extern "C" {
 
 unsigned long long sdpg_launch_count(void) { return g_kernel_launches.load(); }
+
+int sdpg_probe_tensor_rate(int device, int kind, double *ops_per_second) {
+    return sdpg_guard([&] {
+        if (!ops_per_second) throw sdpg_error(SDPG_ERR_ARG, "null output");
+        if (kind < 0 || kind > 2) throw sdpg_error(SDPG_ERR_ARG, "kind must be 0, 1 or 2");
+        SDPG_CUDA(cudaSetDevice(device));
+        int sms = 0;
+        SDPG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        cudaEvent_t a, b;
+        SDPG_CUDA(cudaEventCreate(&a));
+        SDPG_CUDA(cudaEventCreate(&b));
+        float best = 1e30f;
+        double ops = 0;
+        if (kind == 0) {
+            DeviceBuffer st(sizeof(int));
+            SDPG_CUDA(cudaMemset(st.p, 0, sizeof(int)));
+            SDPG_CUDA(cudaFuncSetAttribute(tc_f16_rate_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           kProbeSmemLaunch));
+            tc_f16_rate_probe_kernel<<<sms, 128, kProbeSmemLaunch>>>(64, (int *)st.p);  // warm-up
+            SDPG_CHECK_LAUNCH();
+            for (int rep = 0; rep < 3; ++rep) {
+                SDPG_CUDA(cudaEventRecord(a));
+                tc_f16_rate_probe_kernel<<<sms, 128, kProbeSmemLaunch>>>(kProbeRounds, (int *)st.p);
+                SDPG_CHECK_LAUNCH();
+                SDPG_CUDA(cudaEventRecord(b));
+                SDPG_CUDA(cudaEventSynchronize(b));
+                float ms = 0;
+                SDPG_CUDA(cudaEventElapsedTime(&ms, a, b));
+                best = std::min(best, ms);
+            }
+            int h = 0;
+            SDPG_CUDA(cudaMemcpy(&h, st.p, sizeof(int), cudaMemcpyDeviceToHost));
+            if (h) throw sdpg_error(SDPG_ERR_TIMEOUT, "tensor-rate probe: a bounded wait gave up");
+            ops = (double)sms * kProbeRounds * 4 * (2.0 * 128 * kProbeN * 16);
+        } else {
+            const int blocks = sms * 4, threads = 256, iters = 4096;
+            DeviceBuffer out((size_t)blocks * threads * sizeof(uint32_t));
+            auto launch = [&](int it) {
+                if (kind == 1)
+                    mma_sync_rate_probe_kernel<true><<<blocks, threads>>>(it, 12345u, (uint32_t *)out.p);
+                else
+                    mma_sync_rate_probe_kernel<false><<<blocks, threads>>>(it, 12345u, (uint32_t *)out.p);
+                SDPG_CHECK_LAUNCH();
+            };
+            launch(64);  // warm-up
+            for (int rep = 0; rep < 3; ++rep) {
+                SDPG_CUDA(cudaEventRecord(a));
+                launch(iters);
+                SDPG_CUDA(cudaEventRecord(b));
+                SDPG_CUDA(cudaEventSynchronize(b));
+                float ms = 0;
+                SDPG_CUDA(cudaEventElapsedTime(&ms, a, b));
+                best = std::min(best, ms);
+            }
+            const double per_mma = kind == 1 ? 2.0 * 16 * 8 * 32 : 2.0 * 16 * 8 * 16;
+            ops = (double)blocks * (threads / 32) * iters * 8 * per_mma;
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        *ops_per_second = ops / (best * 1e-3);
+        return (int)SDPG_OK;
+    });
+}
 
 int sdpg_set_gemm_method(int method) {
     return sdpg_guard([&] {

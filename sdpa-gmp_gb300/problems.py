@@ -330,6 +330,15 @@ def control_dense(m: int, blocks, rng: np.random.Generator):
     return c, F0, F
 
 
+def batch_instance_size(seed: int) -> tuple[int, list[int]]:
+    """(m, block sizes) of batch_instance(seed), from the same first draws, without
+    building the instance."""
+    rng = np.random.default_rng(seed)
+    m = int(rng.integers(20, 351))
+    blocks = [int(x) for x in rng.integers(15, 91, size=2)]
+    return m, blocks
+
+
 def batch_instance(seed: int):
     """One instance of the batched workload: m ~ U[20, 350], two blocks of sizes
     ~ U[15, 90], control/LMI construction, all drawn from `seed`."""

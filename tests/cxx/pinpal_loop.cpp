@@ -7,6 +7,8 @@
 // Prints the iteration table and summary to stdout (and to OUT when given).
 #include <stdio.h>
 
+#include <algorithm>
+
 #include "sdpa_gb300.hpp"
 
 using namespace sdpa;
@@ -109,16 +111,31 @@ int main(int argc, char **argv) {
         IO::printLastInfo(pIteration, mu, theta, solveInfo, alpha, beta, currentRes, phase, currentPt, 0.0, inputData,
                           work, com, param, fpOut, Display);
         if (fpOut) fclose(fpOut);
-        // a host-side check of the Lal helpers on the final iterate: the smallest
-        // eigenvalue of each (small) block of X is positive
+        // a host-side check of the Lal helpers on the final iterate: X is singular at the
+        // optimum, so S = X X^T + diag(1, 2, .., n) (via Lal::multiply_tran) has every
+        // eigenvalue >= 1, a simple smallest one, and a Cholesky factor
+        // (Lal::choleskyFactorWithAdjust)
         currentPt.fetch();
         for (auto &blk : currentPt.xMat.SDP_block) {
             if (blk.nRow > 64) continue;
+            DenseMatrix S;
+            Lal::multiply_tran(S, blk, blk);
+            for (int i = 0; i < S.nRow; ++i) {
+                const double one = 1.0 + i;
+                std::vector<uint32_t> a(2 + S.limbs), b(2 + S.limbs);
+                uint32_t *sii = &S.de_ele[((size_t)i + (size_t)S.nRow * i) * (2 + S.limbs)];
+                gb300::check(sdpg_ml_from_double(S.limbs, &one, 1, b.data()));
+                gb300::check(sdpg_ml_host_op(S.limbs, SDPG_OP_ADD, 1, sii, b.data(), a.data()));
+                std::copy(a.begin(), a.end(), sii);
+            }
             Vector ev, wv;
-            const Real lmin = Lal::getMinEigenValue(blk, ev, wv);
-            printf("lal: block %d min eigenvalue of X %s\n", blk.nRow, lmin.str(6).c_str());
-            if (!(lmin > 0.0)) {
-                fprintf(stderr, "X is not positive definite at the end\n");
+            const Real lmin = Lal::getMinEigenValue(S, ev, wv);
+            DenseMatrix F = S;
+            const bool chol = Lal::choleskyFactorWithAdjust(F);
+            printf("lal: block %d min eigenvalue of X X^T + D %s, Cholesky %s\n", blk.nRow, lmin.str(6).c_str(),
+                   chol ? "ok" : "failed");
+            if (!(lmin >= 0.999) || !chol) {
+                fprintf(stderr, "the Lal check on the final iterate failed\n");
                 return 1;
             }
         }

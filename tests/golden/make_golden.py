@@ -60,12 +60,15 @@ CASES = {
 # gives fixed-iteration comparisons of the same run.
 P80 = "%+.80Fe"
 P160 = "%+.160Fe"
+P200 = "%+.200Fe"
 PRECISE = {
     "gpp500_hp": ("gpp", dict(n=500, p=0.02, seed=0), 256, dict(print_format=P80)),
     "gpp500_it5": ("gpp", dict(n=500, p=0.02, seed=0), 256, dict(print_format=P80, max_iteration=5)),
     "gpp500_it10": ("gpp", dict(n=500, p=0.02, seed=0), 256, dict(print_format=P80, max_iteration=10)),
     "gpp500_it20": ("gpp", dict(n=500, p=0.02, seed=0), 256, dict(print_format=P80, max_iteration=20)),
     "gpp500_p512_it10": ("gpp", dict(n=500, p=0.02, seed=0), 512, dict(print_format=P160, max_iteration=10)),
+    # the same ten iterations at 1024 bits: a yardstick for both the 256- and 512-bit runs
+    "gpp500_p1024_it10": ("gpp", dict(n=500, p=0.02, seed=0), 1024, dict(print_format=P200, max_iteration=10)),
     "control231_hp": ("control", dict(m=231, blocks=(40, 20), seed=0), 256, dict(print_format=P80)),
     "maxcut124pm_hp": ("maxcut", dict(n=124, p=0.1, seed=0, signed=True), 256, dict(print_format=P80)),
     "maxcut100_hp": ("maxcut", dict(n=100, p=0.1, seed=0), 256, dict(print_format=P80)),
@@ -129,13 +132,13 @@ def result_layout(text: str) -> list[str]:
     return out
 
 
-def precise_fields(r: dict, prob) -> None:
+def precise_fields(r: dict, prob, digits: int = 90) -> None:
     """Replace r's xMat / yMat by a digest when large and add the objectives computed
     exactly (decimal, 200 digits) from the printed solution: objValPrimal = c.xVec and
     objValDual = F0.yMat (SDPA's printed primal / dual, sdpa_io.cpp:1095-1109, 1166-1173),
     and the relative gap |P - D| / max(1, (|P| + |D|) / 2) (sdpa_io.cpp:1001-1003)."""
     from decimal import Decimal, getcontext
-    getcontext().prec = 200
+    getcontext().prec = 2 * digits + 40
     x = [Decimal(v) for v in r["xVec"]]
     objp = sum(Decimal(c) * xi for c, xi in zip(prob.c, x))
     sizes = [abs(b) for b in prob.block_struct]
@@ -157,9 +160,9 @@ def precise_fields(r: dict, prob) -> None:
         if k == 0:
             objd += Decimal(v) * y(blk, i, j) * (1 if i == j else 2)
     gap = abs(objp - objd) / max(Decimal(1), (abs(objp) + abs(objd)) / 2)
-    r["objValPrimal_hp"] = format(objp, ".90e")
-    r["objValDual_hp"] = format(objd, ".90e")
-    r["relgap_hp"] = format(gap, ".40e")
+    r["objValPrimal_hp"] = format(objp, f".{digits}e")
+    r["objValDual_hp"] = format(objd, f".{digits}e")
+    r["relgap_hp"] = format(gap, f".{digits}e")
     if len(ymat) > FULL_MATRIX_LIMIT:
         dig = {}
         for key in ("xMat", "yMat"):
@@ -262,7 +265,8 @@ def main() -> None:
             param_text = problems.param_text(precision=prec, **pkw)
             t0 = time.time()
             r = run_case(binary, dat_text, param_text, work, name)
-            precise_fields(r, prob)
+            # digits of the stored objectives: ten beyond the print format's
+            precise_fields(r, prob, digits=int(pkw["print_format"].split(".")[1].rstrip("Fe")) + 10)
             r.update(name=name, generator=gen, kwargs={k: (list(v) if isinstance(v, tuple) else v)
                                                          for k, v in kw.items()},
                      precision=prec, sha256=hashlib.sha256(dat_text.encode()).hexdigest(), param=pkw,

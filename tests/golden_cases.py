@@ -3,6 +3,7 @@ solver's own output, see tests/golden/make_golden.py) and write its input."""
 import hashlib
 import importlib
 import json
+import math
 import os
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -41,3 +42,15 @@ def init_file(g):
     if not ini:
         return None
     return os.path.join(GOLDEN, ini["file"]), bool(ini["sparse"])
+
+
+def close_printed(a: float, b_str: str, digits: int) -> bool:
+    """`a` agrees with the reference's printed value `b_str` (printed with `digits`
+    digits after the point) to within two units of the last printed digit."""
+    b = float(b_str)
+    if b == 0.0:
+        return abs(a) < 1e-300 or a == 0.0
+    if abs(b) < 1e-60:  # residual ratios at rounding-noise level differ by construction
+        return abs(a) < 1e-55
+    ulp = 10.0 ** (math.floor(math.log10(abs(b))) - digits)
+    return abs(a - b) <= 2.0 * ulp + 1e-12 * abs(b)

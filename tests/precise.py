@@ -19,7 +19,7 @@ from __future__ import annotations
 import math
 from decimal import Decimal, getcontext
 
-getcontext().prec = 200
+getcontext().prec = 400
 
 
 def _d(s) -> Decimal:
@@ -32,15 +32,21 @@ def _log2(x: Decimal) -> float:
     return math.log2(float(x)) if float(x) > 0 else float(x.ln() / Decimal(2).ln())
 
 
-def errors(sdpg, solver, golden: dict, digits: int = 90) -> dict:
+def errors(sdpg, solver, golden: dict, digits: int | None = None) -> dict:
     """Relative errors of `solver` (after run()) against `golden`; values are floats and
-    their log2 under "<key>_log2"."""
+    their log2 under "<key>_log2".  The solver's values are read as decimal text with
+    `digits` significant digits (default: 20 more than the golden's precision holds, so
+    the text itself adds nothing to the error)."""
+    if digits is None:
+        digits = int(int(golden.get("precision", 256)) * 0.30103) + 20
     P = _d(solver.text(0, digits))
     D = _d(solver.text(1, digits))
     Pr, Dr = _d(golden["objValPrimal_hp"]), _d(golden["objValDual_hp"])
     scale = max(Decimal(1), (abs(Pr) + abs(Dr)) / 2)
     gap = abs(P - D) / max(Decimal(1), (abs(P) + abs(D)) / 2)
-    gapr = _d(golden["relgap_hp"])
+    # the reference's gap from its objectives (stored to more digits than relgap_hp in
+    # older fixtures)
+    gapr = abs(Pr - Dr) / max(Decimal(1), (abs(Pr) + abs(Dr)) / 2)
     out = {
         "objValPrimal": abs(P - Pr) / max(Decimal(1), abs(Pr)),
         "objValDual": abs(D - Dr) / max(Decimal(1), abs(Dr)),
@@ -72,6 +78,39 @@ def errors(sdpg, solver, golden: dict, digits: int = 90) -> dict:
             for a, r in zip(got, ref):
                 big = max(big, abs(r))
                 worst = max(worst, abs(_d(a) - r))
+        out[key] = worst / big
+    res = {}
+    for k, v in out.items():
+        res[k] = float(v)
+        res[k + "_log2"] = _log2(v) if v > 0 else -math.inf
+    return res
+
+
+def golden_errors(golden: dict, yardstick: dict) -> dict:
+    """The same errors between two reference fixtures of one problem and iteration count
+    (e.g. the reference at 256 bits against itself at 512 bits): objectives, gap and xVec,
+    and xMat / yMat over the digest entries both fixtures hold."""
+    P, D = _d(golden["objValPrimal_hp"]), _d(golden["objValDual_hp"])
+    Pr, Dr = _d(yardstick["objValPrimal_hp"]), _d(yardstick["objValDual_hp"])
+    scale = max(Decimal(1), (abs(Pr) + abs(Dr)) / 2)
+    gap = abs(P - D) / max(Decimal(1), (abs(P) + abs(D)) / 2)
+    gapr = abs(Pr - Dr) / max(Decimal(1), (abs(Pr) + abs(Dr)) / 2)
+    out = {
+        "objValPrimal": abs(P - Pr) / max(Decimal(1), abs(Pr)),
+        "objValDual": abs(D - Dr) / max(Decimal(1), abs(Dr)),
+        "relgap": abs(gap - gapr) * max(Decimal(1), (abs(P) + abs(D)) / 2) / scale,
+    }
+    x = [_d(v) for v in golden["xVec"]]
+    xr = [_d(v) for v in yardstick["xVec"]]
+    out["xVec"] = max(abs(a - b) for a, b in zip(x, xr)) / max(Decimal(1), max(abs(v) for v in xr))
+    for key in ("xMat", "yMat"):
+        worst, big = Decimal(0), Decimal(1)
+        for part in ("diag", "col0"):
+            for blk, blkr in zip(golden["digest"][key][part], yardstick["digest"][key][part]):
+                for a, b in zip(blk, blkr):
+                    r = _d(b)
+                    big = max(big, abs(r))
+                    worst = max(worst, abs(_d(a) - r))
         out[key] = worst / big
     res = {}
     for k, v in out.items():

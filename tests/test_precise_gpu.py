@@ -24,36 +24,66 @@ import os
 
 import pytest
 
-from golden_cases import GOLDEN, load, write_inputs
-from precise import errors
+from golden_cases import GOLDEN, close_printed, load, write_inputs
+from precise import errors, golden_errors
 
-# case -> (max log2 relative error of objectives / gap, of xVec, of xMat / yMat)
+# case -> (max log2 relative error of objectives / gap, of xVec, of xMat / yMat).  Each
+# bound sits a few bits above the error measured on a GB300 (in brackets: objValPrimal,
+# objValDual, relgap; xVec; xMat, yMat).
 BOUNDS = {
-    "gpp500_it5": (-240, -240, -240),
-    "gpp500_it10": (-240, -240, -240),
-    "gpp500_it20": (-200, -200, -200),
-    "gpp500_p512_it10": (-496, -496, -496),
-    "gpp500_hp": (-150, -100, -100),
-    "control231_hp": (-150, -100, -100),
-    "maxcut124pm_hp": (-150, -100, -100),
-    "maxcut100_hp": (-120, -85, -70),
+    # after 5 iterations: [-225.9, -234.2, exact; -225.9; -226.1, -234.2]
+    "gpp500_it5": (-220, -220, -220),
+    # after 10: [-135.3, -135.6, -134.5; -133.4; -133.4, -133.9]
+    "gpp500_it10": (-128, -128, -128),
+    # after 20: [-153.5, -147.0, -147.0; -131.1; -131.1, -145.3]
+    "gpp500_it20": (-140, -125, -125),
+    "gpp500_p512_it10": (-256, -256, -256),
+    "gpp500_hp": (-100, -64, -64),
+    # full solve, 43 iterations to pdOPT: [-119.9, -118.5, -118.0; -89.9; -84.8, -93.9]
+    "control231_hp": (-110, -80, -75),
+    # full solve, 42 iterations to pdOPT: [-118.9, -118.0, -119.2; -106.3; -105.6, -84.8]
+    "maxcut124pm_hp": (-110, -95, -75),
+    # full solve, 41 iterations to pdOPT: [-131.3, -111.3, -111.3; -90.1; -88.4, -76.5]
+    "maxcut100_hp": (-105, -85, -70),
 }
 # the full graph-partition solve stops in pFEAS when the step collapses (no strictly
 # feasible primal point); where exactly depends on rounding, so its iteration count
 # may differ by a few
 DEGENERATE = {"gpp500_hp"}
+# The same ten graph-partition iterations run by the reference at 256, 512 and 1024 bits:
+# (run, yardstick) pairs in which the yardstick holds the more precise iterate.  The
+# reference's own distance from the yardstick shows how far rounding at the run's
+# precision moves the iterate; this solver's distance is held to that, within a factor
+# of 2^MARGIN_BITS.
+YARDSTICKS = [("gpp500_it10", "gpp500_p512_it10"), ("gpp500_it10", "gpp500_p1024_it10"),
+              ("gpp500_p512_it10", "gpp500_p1024_it10")]
+MARGIN_BITS = 6
+KEYS = ("objValPrimal", "objValDual", "relgap", "xVec", "xMat", "yMat")
 
 
 def cases():
     return [c for c in BOUNDS if os.path.exists(os.path.join(GOLDEN, c + ".json"))]
 
 
-@pytest.mark.gpu
-@pytest.mark.parametrize("name", cases())
-def test_precise_parity(sdpg, name, tmp_path):
+def have(name):
+    return os.path.exists(os.path.join(GOLDEN, name + ".json"))
+
+
+def solve(sdpg, name, tmp_path):
     dat, par, g = write_inputs(name, str(tmp_path))
     solver = sdpg.Solver(sdpg.Problem.read(dat), sdpg.Param.read(par))
     solver.run()
+    return solver, g
+
+
+def fmt(e):
+    return "  ".join(f"{k}={e[k + '_log2']:.1f}" for k in KEYS)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", cases())
+def test_precise_parity(sdpg, name, tmp_path):
+    solver, g = solve(sdpg, name, tmp_path)
     info = solver.info()
     assert info["phase"] == g["phase"], (info["phase"], g["phase"])
     if name in DEGENERATE:
@@ -61,12 +91,22 @@ def test_precise_parity(sdpg, name, tmp_path):
     else:
         assert info["iteration"] == g["iteration"], (info["iteration"], g["iteration"])
     if info["iteration"] != g["iteration"]:
-        pytest.skip(f"{name}: stopped at iteration {info['iteration']}, the reference at {g['iteration']}; "
-                    "the final iterates are not comparable")
+        # a degenerate solve that stopped elsewhere: the iterates are compared through the
+        # printed table while mu > 1e-12, and the final objectives to the stop's own scale
+        hist = solver.history()
+        for row, ref in zip(hist, g["iterations_table"]):
+            if float(ref[1]) < 1e-12:
+                break
+            for col, digits in ((1, 1), (4, 2), (5, 2)):  # mu, objP, objD as printed
+                assert close_printed(row[col], ref[col], digits), (int(row[0]), col, row[col], ref[col])
+        for key in ("objValPrimal", "objValDual"):
+            ref = float(g[key])
+            assert abs(info[key] - ref) <= 1e-9 * max(1.0, abs(ref)), (key, info[key], ref)
+        print(f"\n{name}: stopped at iteration {info['iteration']} ({info['phase']}), the reference at "
+              f"{g['iteration']}; table and objectives agree (final iterates not comparable digit by digit)")
+        return
     e = errors(sdpg, solver, g)
-    line = "  ".join(f"{k}={e[k + '_log2']:.1f}" for k in ("objValPrimal", "objValDual", "relgap", "xVec",
-                                                          "xMat", "yMat"))
-    print(f"\n{name} ({g['precision']}-bit, {info['iteration']} iterations, {info['phase']}): log2 error {line}")
+    print(f"\n{name} ({g['precision']}-bit, {info['iteration']} iterations, {info['phase']}): log2 error {fmt(e)}")
     b_obj, b_x, b_mat = BOUNDS[name]
     for key in ("objValPrimal", "objValDual", "relgap"):
         assert e[key + "_log2"] <= b_obj, (key, e[key + "_log2"], b_obj)
@@ -75,11 +115,39 @@ def test_precise_parity(sdpg, name, tmp_path):
         assert e[key + "_log2"] <= b_mat, (key, e[key + "_log2"], b_mat)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("run,yardstick", [p for p in YARDSTICKS if have(p[0]) and have(p[1])])
+def test_precise_against_higher_precision(sdpg, run, yardstick, tmp_path):
+    """This solver at the run's precision is no further from the higher-precision iterate
+    than the reference at the same precision is (within 2^MARGIN_BITS)."""
+    solver, g = solve(sdpg, run, tmp_path)
+    y = load(yardstick)
+    assert solver.info()["iteration"] == y["iteration"]
+    ours = errors(sdpg, solver, y)
+    ref = golden_errors(g, y)
+    print(f"\n{run} vs {yardstick}: this solver {fmt(ours)}\n{'':>{len(run) + len(yardstick) + 4}}"
+          f"  reference   {fmt(ref)}")
+    for key in KEYS:
+        assert ours[key + "_log2"] <= ref[key + "_log2"] + MARGIN_BITS, (key, ours[key + "_log2"],
+                                                                         ref[key + "_log2"])
+
+
 def test_precise_fixtures_present():
     """The benchmark configuration's fixtures are committed (CPU-side check of the set)."""
-    have = cases()
+    have_ = cases()
     for need in ("gpp500_hp", "gpp500_it5", "gpp500_it10", "gpp500_it20", "gpp500_p512_it10"):
-        assert need in have, need
+        assert need in have_, need
     g = load("gpp500_it5")
     assert g["param"]["print_format"] == "%+.80Fe" and g["iteration"] == 5
     assert not math.isnan(float(g["objValPrimal_hp"]))
+
+
+def test_reference_precision_ladder():
+    """The reference's own 256-bit iterate after ten graph-partition iterations lies within
+    2^-120 of its 512-bit one (CPU-side: fixtures only).  This is the scale on which the
+    256-bit parity bounds above are set."""
+    if not (have("gpp500_it10") and have("gpp500_p512_it10")):
+        pytest.skip("fixtures absent")
+    e = golden_errors(load("gpp500_it10"), load("gpp500_p512_it10"))
+    for key in KEYS:
+        assert e[key + "_log2"] <= -120, (key, e[key + "_log2"])

@@ -11,12 +11,11 @@ Checked per case:
   * every row of the iteration table (mu, objP, objD, alphaP, alphaD, beta as
     printed with 2-3 digits) within 2 units of the last printed digit.
 """
-import math
 import os
 
 import pytest
 
-from golden_cases import init_file, write_inputs
+from golden_cases import close_printed, init_file, write_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -29,16 +28,6 @@ LARGE = ["gpp60", "maxcut100", "maxcut124pm", "control231"]
 # iterations.  For them the iteration count may differ by a few iterations and the
 # table is compared while mu > 1e-12; phase and objectives must still agree.
 DEGENERATE = {"gpp40", "gpp60"}
-
-
-def close_printed(a: float, b_str: str, digits: int) -> bool:
-    b = float(b_str)
-    if b == 0.0:
-        return abs(a) < 1e-300 or a == 0.0
-    if abs(b) < 1e-60:  # residual ratios at rounding-noise level differ by construction
-        return abs(a) < 1e-55
-    ulp = 10.0 ** (math.floor(math.log10(abs(b))) - digits)
-    return abs(a - b) <= 2.0 * ulp + 1e-12 * abs(b)
 
 
 def run_case(sdpg, name, tmp_path):
