@@ -257,12 +257,7 @@ int sdpg_rpotrf(int limbs, int n, void *A, int lda, int *info) {
             int rc = with_device_copy(limbs, (size_t)lda * n, A, true, A, [&](void *dA) {
                 Workspace &ws = thread_workspace(nullptr);
                 ws.reset();
-                GemmProblem<N> p{};
-                p.M = n;
-                p.Nn = 32;
-                p.K = n;
-                p.batch = 1;
-                ws.reserve(gemm_workspace_bytes<N>(p) + (1 << 20));
+                ws.reserve(ml_potrf_workspace_bytes<N>(n) + (1 << 20));
                 ml_potrf<N>(n, (mlf<N> *)dA, lda, (int *)dinfo.p, ws, nullptr);
                 return (int)SDPG_OK;
             });

@@ -440,11 +440,18 @@ void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t 
     mlf<N> *rinv = (mlf<N> *)ws.carve(NB * sizeof(mlf<N>));
     mlf<N> *Lsc = (mlf<N> *)ws.carve(NB * NB * sizeof(mlf<N>));
     const mlf<N> mone = ml_from_int<N>(-1), one = ml_one<N>();
+    // 256-bit factors of at least 128 rows: the panel products read the residues of the
+    // finished columns, converted once each (crt_cache_*)
+    const bool cached = crt_cache_applies<N>(n);
+    CrtCache cache;
+    if (cached) cache = crt_cache_init<N>(n, A, lda, ws.carve(crt_cache_bytes(n)), s);
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int kb = min(NB, n - k0);
         const int rows = n - k0 - kb;
         mlf<N> *Akk = A + k0 + (long long)k0 * lda;
-        if (k0 > 0) {
+        if (k0 > 0 && cached) {
+            crt_cache_panel<N>(cache, k0, kb, A, lda, ws.error, s);
+        } else if (k0 > 0) {
             GemmProblem<N> p = gemm_nn<N>(n - k0, kb, k0, mone, A + k0, lda, 'N', A + k0, lda, 'T', one, Akk, lda);
             p.lower_only = 1;
             const size_t m2 = ws.used;
@@ -459,8 +466,21 @@ void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t 
         panel_trsm_kernel<N><<<ceil_div((long long)rows * 32, 256), 256, 0, s>>>(Lsc, Akk + kb, lda, kb, rows, info,
                                                                                rinv);
         SDPG_CHECK_LAUNCH_KT("panel_trsm_kernel", s);
+        if (cached) crt_cache_put<N>(cache, A, lda, k0, kb, ws.error, s);
     }
     ws.used = mark;
+}
+
+template <int N>
+size_t ml_potrf_workspace_bytes(int n) {
+    GemmProblem<N> p{};
+    p.M = n;
+    p.Nn = NB;
+    p.K = n;
+    p.batch = 1;
+    size_t b = gemm_workspace_bytes<N>(p);
+    if (crt_cache_applies<N>(n)) b = std::max(b, crt_cache_bytes(n));
+    return b + (size_t)(NB + NB * NB) * sizeof(mlf<N>) + 4096;
 }
 
 namespace {
@@ -623,6 +643,7 @@ void ml_potrs(int n, const mlf<N> *L, int ldl, mlf<N> *x, Workspace &ws, cudaStr
 
 #define SDPG_INST_CHOL(N)                                                                       \
     template void ml_potrf<N>(int, mlf<N> *, int, int *, Workspace &, cudaStream_t);            \
+    template size_t ml_potrf_workspace_bytes<N>(int);                                                       \
     template void ml_trtri_lower<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t); \
     template size_t ml_trtri_workspace_bytes<N>(int);                                                       \
     template void ml_potrs<N>(int, const mlf<N> *, int, mlf<N> *, Workspace &, cudaStream_t);             \

@@ -4,7 +4,10 @@
 //   1. Exponents: EA_i = max_k exponent(op(A)[i,k]), EB_j likewise over op(B)[:,j].
 //   2. Residues: each entry becomes the integer X = trunc(x 2^(R - E)), |X| < 2^R with
 //      R = 276, and is stored as its balanced residues modulo L = 70 primes below 512
-//      (fp16, exact), K contiguous.
+//      (fp16, exact), K contiguous.  The residues come from the tensor cores too: with
+//      X = sum_c x_c 2^(8c) (36 bytes), X mod m_l = (sum_c x_c t_lc) mod m_l where
+//      t_lc = 2^(8c) mod m_l, one fp16 product of [128 entries x 64 bytes] and
+//      [64 x 80 moduli] per tile, exact in fp32.
 //   3. Tensor cores (tc_gemm.cu): for each prime, S = A_l B_l^T exactly in fp32, then
 //      y_l = S mod m_l.
 //   4. Reconstruction: the exact sum V = sum_k X_ik X_kj satisfies
@@ -16,11 +19,14 @@
 // The only rounding is the truncation of the inputs to R bits (relative 2^-276 of
 // the row / column maximum) and the final conversion to 256 bits, so the error obeys
 // the same normwise bound as the digit GEMM in gemm.cu.
+#include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "crt_tables.h"
 #include "gemm.cuh"
 #include "tc_gemm.cuh"
+#include "tcgen05.cuh"
 
 namespace sdpg {
 
@@ -31,12 +37,50 @@ __constant__ float c_minv[kCrtL];  // 1.0f / m_l, correctly rounded (as the divi
 __constant__ int c_pow16[kCrtL][kCrtPowChunks];
 __constant__ uint32_t c_inv[kCrtL][kCrtInvWords];
 __constant__ uint32_t c_mtot[8];
+__constant__ uint32_t c_mdiv[kCrtL];  // ceil(2^32 / m_l): x / m_l = umulhi(x, c_mdiv[l]) for x < 2^23
 __device__ int d_moduli[kCrtL];
 __device__ int d_error;
 
+// Residues on the tensor cores: an entry's integer X (below 2^276) is written as 36
+// bytes x_c (X = sum_c x_c 2^(8c)); then X mod m_l = (sum_c x_c t_lc) mod m_l with
+// t_lc = 2^(8c) mod m_l.  The sums are one fp16 GEMM [entries x 64 chunks] x [64 x 80
+// moduli] with fp32 accumulation, exact: every partial sum is an integer below
+// 36 * 255 * 508 < 2^23.
+constexpr int kResChunks = 36;  // bytes of a 288-bit integer
+constexpr int kResK = 64;       // GEMM K: the chunks, zero-padded (one 128-byte swizzle row)
+constexpr int kResN = 80;       // GEMM N: the moduli, zero-padded to a multiple of 16
+constexpr int kResM = 128;      // entries per tile (tcgen05 M)
+constexpr int kResTileA = kResM * kResK * 2;  // 16 KB
+constexpr int kResTileB = kResN * kResK * 2;  // 10 KB
+constexpr int kResSmem = kResTileA + kResTileB + 1024 + 64;
+// dynamic shared memory requested per CTA: at most four CTAs per SM, whose tensor-memory
+// allocations (128 columns each) then fit the SM's 512 columns together
+constexpr int kResSmemLaunch = 46 * 1024;
+static_assert(kResSmem <= kResSmemLaunch, "residue kernel shared memory");
+static_assert(kCrtL <= kResN && kResChunks * 8 >= kCrtR && kResChunks <= kResK, "residue GEMM shape");
+static_assert((long long)kResChunks * 255 * 508 < (1 << 23), "residue sums must stay exact in fp32");
+
 struct CrtDevice {
     int *moduli = nullptr, *error = nullptr;
+    const uint4 *res_table = nullptr;  // t_lc as fp16, [kResN][kResK] in the 128-byte-swizzled K-major layout
+    int sms = 0;
 };
+
+// The table t_lc = 2^(8c) mod m_l laid out as the tcgen05 B operand: row l (modulus),
+// 64 K-elements of 2 bytes, the 16-byte chunk j of row l stored at chunk j ^ (l mod 8).
+std::vector<uint16_t> residue_table_host() {
+    std::vector<uint16_t> t((size_t)kResN * kResK, 0);
+    for (int l = 0; l < kCrtL; ++l) {
+        const int m = kCrtModuli[l];
+        int p = 1 % m;
+        for (int c = 0; c < kResChunks; ++c) {
+            const int j = c / 8, w = c % 8;
+            t[(size_t)l * kResK + ((j ^ (l & 7)) * 8) + w] = __half_as_ushort(__float2half((float)p));  // p < 512: exact
+            p = (p * 256) % m;
+        }
+    }
+    return t;
+}
 
 // Per device: upload the tables once and look up the global-memory copies' addresses.
 CrtDevice crt_device() {
@@ -56,9 +100,20 @@ CrtDevice crt_device() {
         SDPG_CUDA(cudaMemcpyToSymbol(c_inv, kCrtInv, sizeof(kCrtInv)));
         SDPG_CUDA(cudaMemcpyToSymbol(c_mtot, kCrtMtotMant, sizeof(kCrtMtotMant)));
         SDPG_CUDA(cudaMemcpyToSymbol(d_moduli, kCrtModuli, sizeof(kCrtModuli)));
+        uint32_t mdiv[kCrtL];
+        for (int l = 0; l < kCrtL; ++l)
+            mdiv[l] = (uint32_t)(((1ull << 32) + (unsigned long long)kCrtModuli[l] - 1) / kCrtModuli[l]);
+        SDPG_CUDA(cudaMemcpyToSymbol(c_mdiv, mdiv, sizeof(mdiv)));
         CrtDevice c;
+        SDPG_CUDA(cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, dev));
         SDPG_CUDA(cudaGetSymbolAddress((void **)&c.moduli, d_moduli));
         SDPG_CUDA(cudaGetSymbolAddress((void **)&c.error, d_error));
+        // the residue table lives for the life of the process (one per device)
+        const std::vector<uint16_t> tab = residue_table_host();
+        void *dt = nullptr;
+        SDPG_CUDA(cudaMalloc(&dt, tab.size() * sizeof(uint16_t)));
+        SDPG_CUDA(cudaMemcpy(dt, tab.data(), tab.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+        c.res_table = (const uint4 *)dt;
         cache[dev] = c;
         ready[dev] = true;
     }
@@ -76,7 +131,23 @@ struct CrtOperands {
     int cnt[2];  // batch entries to process (0: operand not needed in this pass)
     int *E[2];
     __half *Q[2];
-    int lg[2];   // modulus groups per entry (residue kernel)
+};
+
+// One operand of the residue conversion: entries (o, k) of X for o < rows, k < W (W
+// entries per row; either 128 is a multiple of W or W a multiple of 128, so a tile of 128
+// entries covers whole rows or part of one).  Entries with o >= O or k >= K are zero.  The
+// residue of (o, k) for modulus l goes to Q[b qbatch + l qplane + o qrow + k], for rows
+// o < store_rows only; the row scale is E[b ebatch + o].  With tri set, entries above the
+// diagonal (o < k) count as zero.
+template <int N>
+struct ResSrc {
+    Operand<N> X;
+    int O, K, W, rows, store_rows, cnt;
+    int tri;  // 1: entries with o < k are zero (the strict upper part of a lower factor)
+    const int *E;
+    long long ebatch;
+    __half *Q;
+    long long qrow, qplane, qbatch;
 };
 
 template <int N>
@@ -86,10 +157,14 @@ __global__ void crt_exp_kernel(CrtOperands<N> ops, int K) {
     const int op = z < ops.cnt[0] ? 0 : 1;
     const int b = op ? z - ops.cnt[0] : z;
     const int o = blockIdx.x * kExpWarps + warp;
-    if (o >= ops.Opad[op]) return;
-    const Operand<N> X = ops.X[op];
+    // the operand's fields are selected, not indexed by a run-time value (which would
+    // put the parameter arrays in local memory)
+    const int Opad = op ? ops.Opad[1] : ops.Opad[0], O = op ? ops.O[1] : ops.O[0];
+    if (o >= Opad) return;
+    const Operand<N> X = op ? ops.X[1] : ops.X[0];
+    int *E = op ? ops.E[1] : ops.E[0];
     int emax = INT_MIN;
-    if (o < ops.O[op]) {
+    if (o < O) {
         const mlf<N> *base = X.X + b * X.sb + o * X.so;
         for (int k = lane; k < K; k += 32) {
             const mlf<N> *v = base + k * X.sk;
@@ -98,75 +173,181 @@ __global__ void crt_exp_kernel(CrtOperands<N> ops, int K) {
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, off));
-    if (lane == 0) ops.E[op][(long long)b * ops.Opad[op] + o] = (emax == INT_MIN) ? 0 : emax;
+    if (lane == 0) E[(long long)b * Opad + o] = (emax == INT_MIN) ? 0 : emax;
 }
 
-// Residues of op(X)[o,k] scaled to an integer below 2^R: Q[(b L + l)][o][k], padded
-// entries zero.  Threads run along k so that each modulus plane is written in
-// contiguous 64-byte rows.
-//
-// Small operands are spread over lgroups thread groups per entry, each taking every
-// lgroups-th modulus, so that enough threads are in flight.
+// Entry (o, k) of op(X) as the integer trunc(|x| 2^(R - E)) (below 2^R, R = 276) in ten
+// 32-bit words, and its sign; zero for padding and for entries far below the row scale.
 template <int N>
-__global__ void __launch_bounds__(256) crt_residue_kernel(CrtOperands<N> ops, int K, int Kpad) {
+__device__ __forceinline__ bool crt_integer(const Operand<N> &X, int b, int o, int k, int O, int K, int Erow,
+                                            uint32_t (&T)[10]) {
     constexpr int R = kCrtR;
-    constexpr int LB = 10;
-    const int k = blockIdx.x * 32 + threadIdx.x;
-    const int o = blockIdx.y * 8 + threadIdx.y;
-    const int z0 = ops.cnt[0] * ops.lg[0];
-    const int op = (int)blockIdx.z < z0 ? 0 : 1;
-    const int zz = op ? (int)blockIdx.z - z0 : (int)blockIdx.z;
-    const int lgroups = ops.lg[op];
-    const int b = zz / lgroups, lg = zz - b * lgroups;
-    const int O = ops.O[op], Opad = ops.Opad[op];
-    const Operand<N> X = ops.X[op];
-    const int *E = ops.E[op];
-    __half *Q = ops.Q[op];
-    if (o >= Opad || k >= Kpad) return;
-    uint32_t chunk[kCrtPowChunks];
 #pragma unroll
-    for (int c = 0; c < kCrtPowChunks; ++c) chunk[c] = 0;
-    bool neg = false;
-    if (o < O && k < K) {
-        const mlf<N> v = X.X[b * X.sb + o * X.so + k * X.sk];
-        if (v.m[N - 1] != 0) {
-            const int s = v.e - E[(long long)b * Opad + o] + R - 32 * N;  // integer = M * 2^s
-            if (s > -32 * N) {
-                uint32_t T[LB];
+    for (int w = 0; w < 10; ++w) T[w] = 0;
+    if (o >= O || k >= K) return false;
+    const mlf<N> v = X.X[b * X.sb + o * X.so + k * X.sk];
+    if (v.m[N - 1] == 0) return false;
+    const int s = v.e - Erow + R - 32 * N;  // integer = M * 2^s
+    if (s <= -32 * N) return false;
 #pragma unroll
-                for (int w = 0; w < LB; ++w) T[w] = (w < N) ? v.m[w] : 0u;
-                if (s >= 0) {
-                    ml_limb_shl<LB>(T, s >> 5);
-                    ml_bit_shl<LB>(T, s & 31);
-                } else {
-                    ml_limb_shr<LB>(T, (-s) >> 5);
-                    ml_bit_shr<LB>(T, (-s) & 31);
-                }
-#pragma unroll
-                for (int c = 0; c < kCrtPowChunks; ++c) chunk[c] = (T[c >> 1] >> (16 * (c & 1))) & 0xFFFFu;
-                neg = v.s != 0;
-            }
+    for (int w = 0; w < 10; ++w) T[w] = (w < N) ? v.m[w] : 0u;
+    if (s >= 0) {
+        ml_limb_shl<10>(T, s >> 5);
+        ml_bit_shl<10>(T, s & 31);
+    } else {
+        ml_limb_shr<10>(T, (-s) >> 5);
+        ml_bit_shr<10>(T, (-s) & 31);
+    }
+    return v.s != 0;
+}
+
+// y = s mod m_l (s < 2^23, an exact fp32 sum), balanced to |y| <= (m_l - 1) / 2, signed, as
+// fp16 into residue plane L
+template <int L>
+__device__ __forceinline__ void store_residue(__half *q, long long plane, uint32_t bits, bool neg) {
+    const uint32_t x = __float2uint_rn(__uint_as_float(bits));
+    const int m = c_moduli[L];
+    int r = (int)(x - __umulhi(x, c_mdiv[L]) * (uint32_t)m);
+    if (2 * r > m) r -= m;
+    if (neg) r = -r;
+    q[(long long)L * plane] = __int2half_rn(r);
+}
+
+// columns C0 .. C0 + W - 1 of a thread's tensor-memory row: the moduli with those indices
+template <int C0, int W>
+struct ResidueColumns {
+    template <int NR>
+    static __device__ __forceinline__ void run(__half *q, long long plane, const uint32_t (&v)[NR], bool neg) {
+        if constexpr (W > 0) {
+            if constexpr (C0 < kCrtL) store_residue<C0>(q, plane, v[NR - W], neg);
+            ResidueColumns<C0 + 1, W - 1>::run(q, plane, v, neg);
         }
     }
-    __half *q = Q + ((long long)b * kCrtL * Opad + o) * Kpad + k;
-    const long long plane = (long long)Opad * Kpad;
-#pragma unroll 2
-    for (int l = lg; l < kCrtL; l += lgroups) {
-        const int m = c_moduli[l];
-        int acc = 0;  // < 18 * 65535 * 511 < 2^31
+};
+
+// Residues of op(X)[o, k] scaled to an integer below 2^R (ResSrc: where they go, padded
+// entries zero).  A CTA takes tiles of 128 consecutive entries of the region (entry e =
+// o W + k; thread t one entry): it writes the entries' 36 bytes as the rows of a
+// 128 x 64 fp16 tile (128-byte swizzle), one thread issues the four K = 16 products with
+// the table t_lc (80 x 64, loaded once per CTA), and each thread reduces its row of the
+// 128 x 80 fp32 accumulator modulo the 70 primes.  The tile's plane stores are
+// contiguous along e for every modulus.  The product wait is bounded: on time-out the
+// CTA records error 4 and stops.
+template <int N>
+__global__ void __launch_bounds__(kResM) tc_residue_kernel(ResSrc<N> s0, ResSrc<N> s1,
+                                                           const uint4 *__restrict__ table, int *error, int *sticky) {
+    using namespace tc;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *tA = smem;
+    uint8_t *tB = smem + kResTileA;
+    uint64_t *bar = (uint64_t *)(tB + kResTileB);
+    uint32_t *tmem_slot = (uint32_t *)(bar + 1);
+    __shared__ int abort_flag;
+
+    const int t = threadIdx.x, warp = t >> 5;
+    const int z = blockIdx.y;
+    const bool second = z >= s0.cnt;
+    const ResSrc<N> &S = second ? s1 : s0;
+    const int b = second ? z - s0.cnt : z;
+    const int W = S.W, O = S.O;
+    const Operand<N> X = S.X;
+    const int *E = S.E + (long long)b * S.ebatch;
+    const long long region = (long long)S.rows * W;
+    const int ntiles = (int)(region / kResM);
+    if ((int)blockIdx.x >= ntiles) return;  // the whole CTA: this operand is the smaller one
+
+    for (int i = t; i < kResTileB / 16; i += kResM) reinterpret_cast<uint4 *>(tB)[i] = table[i];
+    if (t == 0) {
+        abort_flag = 0;
+        mbar_init(smem_u32(bar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        tmem_alloc(smem_u32(tmem_slot), 128);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    __half *qbase = S.Q + (long long)b * S.qbatch;
+    const long long qplane = S.qplane;
+    const __half2 k1024 = __half2half2(__ushort_as_half(0x6400));
+    uint32_t phase = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, phase ^= 1u) {
+        const long long e = (long long)tile * kResM + t;
+        const int o = (int)(e / W), k = (int)(e - (long long)o * W);
+        const int Erow = o < O ? E[o] : 0;
+        uint32_t T[10];
+        const bool neg = crt_integer<N>(X, b, o, k, (S.tri && o < k) ? 0 : O, S.K, Erow, T);
+        // the entry's 36 bytes, each as fp16 (0x6400 | byte is 1024 + byte, minus 1024)
+        uint8_t *row = tA + t * 128;
 #pragma unroll
-        for (int c = 0; c < kCrtPowChunks; ++c) acc += (int)chunk[c] * c_pow16[l][c];
-        int r = acc - (int)((float)acc * c_minv[l]) * m;
-        if (r < 0) r += m;
-        if (r >= m) r -= m;
-        if (2 * r > m) r -= m;  // balanced: |r| <= (m - 1) / 2
-        if (neg) r = -r;
-        q[l * plane] = __int2half_rn(r);
+        for (int j = 0; j < kResK / 8; ++j) {  // 16-byte chunk j holds K elements 8j .. 8j + 7
+            uint32_t h[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int c0 = 8 * j + 2 * q, c1 = c0 + 1;
+                const uint32_t b0 = c0 < kResChunks ? (T[c0 >> 2] >> (8 * (c0 & 3))) & 0xFFu : 0u;
+                const uint32_t b1 = c1 < kResChunks ? (T[c1 >> 2] >> (8 * (c1 & 3))) & 0xFFu : 0u;
+                const __half2 x = __halves2half2(__ushort_as_half((unsigned short)(0x6400u | b0)),
+                                                 __ushort_as_half((unsigned short)(0x6400u | b1)));
+                const __half2 y = __hsub2(x, k1024);
+                h[q] = *reinterpret_cast<const uint32_t *>(&y);
+            }
+            *reinterpret_cast<uint4 *>(row + ((j ^ (t & 7)) * 16)) = make_uint4(h[0], h[1], h[2], h[3]);
+        }
+        // the tile was written through the generic proxy and is read by the tensor cores
+        // through the async proxy; the barrier also orders the previous tile's
+        // tensor-memory reads before this tile's products
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (t == 0) {
+            const uint64_t ad = sw128_kmajor_desc(smem_u32(tA)), bd = sw128_kmajor_desc(smem_u32(tB));
+            constexpr uint32_t idesc = idesc_f16_f32(kResM, kResN);
+#pragma unroll
+            for (int kk = 0; kk < kResK / 16; ++kk)
+                tc_mma(tmem, ad + (uint64_t)(2 * kk), bd + (uint64_t)(2 * kk), idesc, kk > 0 ? 1u : 0u);
+            tc_commit(smem_u32(bar));
+        }
+        __syncwarp();
+        // the products above are issued: a drain-type wait with the full budget
+        if (!mbar_wait(smem_u32(bar), phase)) {
+            atomicExch(error, 4);
+            if (sticky && sticky != error) atomicExch(sticky, 4);
+            abort_flag = 1;
+        }
+        __syncthreads();
+        if (abort_flag) break;
+        tc_fence_after();
+        __half *q = qbase + (long long)o * S.qrow + k;
+        const bool store = o < S.store_rows;
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        uint32_t v[32];
+        tmem_ld32(lane_addr, v);
+        tmem_ld_wait();
+        if (store) ResidueColumns<0, 32>::run(q, qplane, v, neg);
+        tmem_ld32(lane_addr + 32, v);
+        tmem_ld_wait();
+        if (store) ResidueColumns<32, 32>::run(q, qplane, v, neg);
+        uint32_t w[8];
+        tmem_ld8(lane_addr + 64, w);
+        tmem_ld_wait();
+        if (store) ResidueColumns<64, 8>::run(q, qplane, w, neg);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 128);
     }
 }
 
 // V / M as the centred fractional part of sum_l y_l c_l / m_l (320-bit fixed point), then
-// C = alpha V 2^(EA + EB - 2R) + beta C.  Each thread takes two neighbouring outputs
+// C = alpha V 2^(EA + EB - 2R) + beta C.  A group of lanes takes two neighbouring outputs
 // along j and reads both residues of a plane with one 32-bit load.
 template <int N>
 __device__ __forceinline__ void crt_finish(const unsigned long long (&acc)[kCrtInvWords], int escale, int alpha_one,
@@ -202,6 +383,12 @@ __device__ __forceinline__ void crt_finish(const unsigned long long (&acc)[kCrtI
     *cp = v;
 }
 
+// Eight lanes share one output pair: lane g sums the moduli l = g, g + 8, ...; the
+// 64-bit word sums are combined across the eight lanes with shuffles and lanes 0 and 1
+// of the group finish the pair's two outputs.  Small products (the narrow panels of the
+// factorisations) thus still spread over many SMs.
+constexpr int kRecLanes = 8;
+
 template <int N>
 __global__ void __launch_bounds__(128)
     crt_reconstruct_kernel(const uint16_t *Y, int Mpad, int Npad, const int *EA, const int *EB, long long sEA,
@@ -210,34 +397,49 @@ __global__ void __launch_bounds__(128)
     // still fill whole warps
     const int npairs = (p.Nn + 1) >> 1;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)p.M * npairs) return;
-    const int i = (int)(t / npairs);
-    const int j = 2 * (int)(t - (long long)i * npairs);
+    const long long pair = t / kRecLanes;
+    const int g = (int)(t % kRecLanes);
+    const bool live = pair < (long long)p.M * npairs;
+    const int i = live ? (int)(pair / npairs) : 0;
+    const int j = live ? 2 * (int)(pair - (long long)i * npairs) : 0;
     const int bl = blockIdx.y;
-    const bool ok0 = j < p.Nn && !(p.lower_only && i < j);
-    const bool ok1 = j + 1 < p.Nn && !(p.lower_only && i < j + 1);
-    if (!ok0 && !ok1) return;
-    const uint32_t *y = reinterpret_cast<const uint32_t *>(Y + ((long long)bl * kCrtL * Mpad + i) * Npad + j);
-    const long long plane = (long long)Mpad * Npad / 2;  // in pairs
+    const bool ok0 = live && j < p.Nn && !(p.lower_only && i < j);
+    const bool ok1 = live && j + 1 < p.Nn && !(p.lower_only && i < j + 1);
     unsigned long long a0[kCrtInvWords], a1[kCrtInvWords];
 #pragma unroll
     for (int w = 0; w < kCrtInvWords; ++w) a0[w] = a1[w] = 0;
-#pragma unroll 10
-    for (int l = 0; l < kCrtL; ++l) {
-        const uint32_t yy = __ldg(y + l * plane);
-        const uint32_t y0 = yy & 0xFFFFu, y1 = yy >> 16;
+    if (ok0 || ok1) {
+        const uint32_t *y = reinterpret_cast<const uint32_t *>(Y + ((long long)bl * kCrtL * Mpad + i) * Npad + j);
+        const long long plane = (long long)Mpad * Npad / 2;  // in pairs
+#pragma unroll 3
+        for (int l = g; l < kCrtL; l += kRecLanes) {
+            const uint32_t yy = __ldg(y + l * plane);
+            const uint32_t y0 = yy & 0xFFFFu, y1 = yy >> 16;
 #pragma unroll
-        for (int w = 0; w < kCrtInvWords; ++w) {
-            const uint32_t c = c_inv[l][w];
-            a0[w] += (unsigned long long)y0 * c;
-            a1[w] += (unsigned long long)y1 * c;
+            for (int w = 0; w < kCrtInvWords; ++w) {
+                const uint32_t c = c_inv[l][w];
+                a0[w] += (unsigned long long)y0 * c;
+                a1[w] += (unsigned long long)y1 * c;
+            }
         }
     }
+    // every lane takes part in the shuffles (the group's lanes are consecutive)
+#pragma unroll
+    for (int off = kRecLanes / 2; off > 0; off >>= 1)
+#pragma unroll
+        for (int w = 0; w < kCrtInvWords; ++w) {
+            a0[w] += __shfl_xor_sync(0xffffffffu, a0[w], off);
+            a1[w] += __shfl_xor_sync(0xffffffffu, a1[w], off);
+        }
     const int bg = b0 + bl;
-    const int ea = EA[bl * sEA + i] - 2 * kCrtR;
-    if (ok0) crt_finish<N>(a0, ea + EB[bl * sEB + j], alpha_one, p, p.C + bg * p.sc + i + (long long)j * p.ldc);
-    if (ok1)
+    if (g == 0 && ok0) {
+        const int ea = EA[bl * sEA + i] - 2 * kCrtR;
+        crt_finish<N>(a0, ea + EB[bl * sEB + j], alpha_one, p, p.C + bg * p.sc + i + (long long)j * p.ldc);
+    }
+    if (g == 1 && ok1) {
+        const int ea = EA[bl * sEA + i] - 2 * kCrtR;
         crt_finish<N>(a1, ea + EB[bl * sEB + j + 1], alpha_one, p, p.C + bg * p.sc + i + (long long)(j + 1) * p.ldc);
+    }
 }
 
 struct CrtLayout {
@@ -274,10 +476,18 @@ CrtLayout crt_layout(const GemmProblem<N> &p) {
 
 inline char *align256(char *p) { return (char *)(((uintptr_t)p + 255) & ~(uintptr_t)255); }
 
-// modulus groups per entry for the residue kernel: aim at about 1200 blocks of 256
-inline int residue_groups(long long blocks) {
-    long long g = 1200 / (blocks > 0 ? blocks : 1);
-    return (int)(g < 1 ? 1 : g > 7 ? 7 : g);
+// The residue conversion of up to two operands in one launch: enough CTAs to fill the SMs
+// four deep, each looping over the tiles of its operand.
+template <int N>
+void residue_launch(const ResSrc<N> &s0, const ResSrc<N> &s1, const CrtDevice &dev, int *error, cudaStream_t s) {
+    for (const ResSrc<N> *r : {&s0, &s1})
+        if (r->cnt > 0 && (((long long)r->rows * r->W) % kResM != 0 || (kResM % r->W != 0 && r->W % kResM != 0)))
+            throw sdpg_error(SDPG_ERR_ARG, "residue conversion: unsupported region shape");
+    const int ops = s0.cnt + s1.cnt;
+    if (ops <= 0) return;
+    const long long tiles = std::max((long long)s0.rows * s0.W * (s0.cnt > 0), (long long)s1.rows * s1.W * (s1.cnt > 0)) / kResM;
+    const int grid_x = (int)std::min<long long>(tiles, std::max<long long>(1, 4LL * dev.sms / ops + 1));
+    tc_residue_kernel<N><<<dim3(grid_x, ops), kResM, kResSmemLaunch, s>>>(s0, s1, dev.res_table, error, dev.error);
 }
 
 }  // namespace
@@ -353,12 +563,26 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
                 crt_exp_kernel<N><<<dim3(ceil_div(opad, kExpWarps), ops.cnt[0] + ops.cnt[1]), 32 * kExpWarps, 0, s>>>(
                     ops, p.K);
                 SDPG_CHECK_LAUNCH_KTW("crt_exp_kernel", s, entries * sizeof(mlf<N>) + rows * 4);
-                const int lg = residue_groups((long long)(L.Kpad / 32) * (opad / 8) * (ops.cnt[0] + ops.cnt[1]));
-                ops.lg[0] = ops.lg[1] = lg;
+                ResSrc<N> rs[2];
+                for (int q = 0; q < 2; ++q) {
+                    rs[q].X = ops.X[q];
+                    rs[q].O = ops.O[q];
+                    rs[q].K = p.K;
+                    rs[q].W = L.Kpad;
+                    rs[q].rows = ops.Opad[q];
+                    rs[q].store_rows = ops.Opad[q];
+                    rs[q].cnt = ops.cnt[q];
+                    rs[q].E = ops.E[q];
+                    rs[q].ebatch = ops.Opad[q];
+                    rs[q].Q = ops.Q[q];
+                    rs[q].qrow = L.Kpad;
+                    rs[q].qplane = (long long)ops.Opad[q] * L.Kpad;
+                    rs[q].qbatch = (long long)kCrtL * ops.Opad[q] * L.Kpad;
+                    rs[q].tri = 0;
+                }
                 SDPG_KT_BEGIN(s);
-                crt_residue_kernel<N><<<dim3(L.Kpad / 32, opad / 8, (ops.cnt[0] + ops.cnt[1]) * lg), dim3(32, 8), 0,
-                                        s>>>(ops, p.K, L.Kpad);
-                SDPG_CHECK_LAUNCH_KTW("crt_residue_kernel", s,
+                residue_launch<N>(rs[0], rs[1], dev, p.error ? p.error : dev.error, s);
+                SDPG_CHECK_LAUNCH_KTW("tc_residue_kernel", s,
                                       entries * (sizeof(mlf<N>) + 2.0 * kCrtL) + rows * 4);
             }
             TcModGemm t{};
@@ -389,7 +613,8 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
             }
             if (p.ev_after) SDPG_CUDA(cudaEventRecord(p.ev_after, s));
             SDPG_KT_BEGIN(s);
-            crt_reconstruct_kernel<N><<<dim3(ceil_div((long long)p.M * ((p.Nn + 1) / 2), 128), G), 128, 0, s>>>(
+            crt_reconstruct_kernel<N><<<dim3(ceil_div((long long)p.M * ((p.Nn + 1) / 2) * kRecLanes, 128), G), 128, 0,
+                                        s>>>(
                 Y, L.Mpad, L.Npad, EA, EB, ab ? L.Mpad : 0, bb ? L.Npad : 0, b0, alpha_one, p);
             // every output: its kCrtL residues read, the result written, C read when beta != 0
             SDPG_CHECK_LAUNCH_KTW("crt_reconstruct_kernel", s,
@@ -398,6 +623,155 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
         }
     }
 }
+
+
+// ---- residues of a Cholesky factor's finished columns --------------------------------
+//
+// The left-looking factorisation's panel product C[k0:n, k0:k0+kb] -= L[k0:n, :k0]
+// L[k0:k0+kb, :k0]^T reads every finished column again at every later panel.  With a
+// row scale that does not depend on k0, the residues of a finished column stay valid,
+// so each column is converted once, right after its panel is factored, into planes that
+// every later panel product reads directly.  The scale of row i is 2^E_i with
+// E_i = ceil(e_i / 2) + 1, A_ii in [2^(e_i - 1), 2^e_i): |L_ik| <= sqrt(A_ii) < 2^(E_i - 1)
+// for a positive definite A, so every integer stays below 2^R.  The truncation error of a
+// product entry is then at most K 2^(E_i + E_j - R), the form of Cholesky's own backward
+// error bound (|L| |L|^T <= sqrt(A_ii A_jj) entrywise).
+
+namespace {
+
+template <int N>
+__global__ void cache_scale_kernel(int n, const mlf<N> *A, long long lda, int *E) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const mlf<N> d = A[i + (long long)i * lda];
+    // ceil(e / 2) for either sign of e, plus the margin bit
+    E[i] = (ml_is_zero(d) ? 0 : (d.e >= 0 ? (d.e + 1) / 2 : -((-d.e) / 2))) + 1;
+}
+
+}  // namespace
+
+size_t crt_cache_bytes(int n) {
+    const size_t rows = round_up(n, kTcBM), kp = round_up(n, kTcBK);
+    const size_t planes = (size_t)kCrtL * rows * kp * 2;
+    const size_t y = (size_t)kCrtL * rows * kTcBN * 2;  // one panel product's result planes
+    return planes + y + rows * 4 + 4 * 256;
+}
+
+template <int N>
+bool crt_cache_applies(int n) {
+    if constexpr (N != 8) {
+        return false;
+    } else {
+        return g_gemm_method != 1 && n >= kTcBM && n <= kCrtMaxK;
+    }
+}
+
+template <int N>
+CrtCache crt_cache_init(int n, const mlf<N> *A, long long lda, void *mem, cudaStream_t s) {
+    CrtCache c;
+    c.n = n;
+    c.rows = (int)round_up(n, kTcBM);
+    c.kpitch = (int)round_up(n, kTcBK);
+    char *cur = align256((char *)mem);
+    c.Q = (__half *)cur;
+    cur = align256(cur + (size_t)kCrtL * c.rows * c.kpitch * 2);
+    c.Y = (uint16_t *)cur;
+    cur = align256(cur + (size_t)kCrtL * c.rows * kTcBN * 2);
+    c.E = (int *)cur;
+    // planes start at zero: columns not yet finished and the upper triangle read as zero
+    SDPG_CUDA(cudaMemsetAsync(c.Q, 0, (size_t)kCrtL * c.rows * c.kpitch * 2, s));
+    SDPG_KT_BEGIN(s);
+    cache_scale_kernel<N><<<ceil_div(n, 128), 128, 0, s>>>(n, A, lda, c.E);
+    SDPG_CHECK_LAUNCH_KT("cache_scale_kernel", s);
+    return c;
+}
+
+template <int N>
+void crt_cache_put(const CrtCache &c, const mlf<N> *A, long long lda, int k0, int kb, int *error, cudaStream_t s) {
+    if constexpr (N != 8) {
+        throw sdpg_error(SDPG_ERR_ARG, "residue path is for 256-bit operands");
+    } else {
+        const CrtDevice dev = crt_device();
+        const int rows = c.n - k0;
+        ResSrc<N> r{};
+        r.X = Operand<N>{A + k0 + (long long)k0 * lda, 1, lda, 0};
+        r.O = rows;
+        r.K = kb;
+        r.W = 32;
+        r.rows = (int)round_up(rows, kResM / 32);
+        r.store_rows = rows;
+        r.cnt = 1;
+        r.tri = 1;
+        r.E = c.E + k0;
+        r.ebatch = 0;
+        r.Q = c.Q + (long long)k0 * c.kpitch + k0;
+        r.qrow = c.kpitch;
+        r.qplane = (long long)c.rows * c.kpitch;
+        r.qbatch = 0;
+        ResSrc<N> none{};
+        SDPG_KT_BEGIN(s);
+        residue_launch<N>(r, none, dev, error ? error : dev.error, s);
+        SDPG_CHECK_LAUNCH_KTW("tc_residue_kernel", s, (double)rows * kb * (sizeof(mlf<N>) + 2.0 * kCrtL));
+    }
+}
+
+template <int N>
+void crt_cache_panel(const CrtCache &c, int k0, int kb, mlf<N> *A, long long lda, int *error, cudaStream_t s) {
+    if constexpr (N != 8) {
+        throw sdpg_error(SDPG_ERR_ARG, "residue path is for 256-bit operands");
+    } else {
+        const CrtDevice dev = crt_device();
+        const int M = c.n - k0;
+        TcModGemm t{};
+        t.A = c.Q + (long long)k0 * c.kpitch;
+        t.B = t.A;
+        t.Y = c.Y;
+        t.L = kCrtL;
+        t.batch = 1;
+        t.Mpad = (int)round_up(M, kTcBM);
+        t.Npad = kTcBN;
+        t.a_rows = t.b_rows = c.rows;
+        t.a_skip = t.b_skip = k0;
+        t.kpitch = c.kpitch;
+        t.lower_only = 1;
+        t.moduli = dev.moduli;
+        t.error = error ? error : dev.error;
+        t.sticky = dev.error;
+        const int Kpad = (int)round_up(k0, kTcBK);
+        for (int q0 = 0; q0 < Kpad; q0 += kTcMaxK) {
+            t.k0 = q0;
+            t.Kpad = std::min(kTcMaxK, Kpad - q0);
+            t.accumulate = q0 > 0;
+            t.alg_flops = 2.0 * kCrtL * (double)M * kb * std::min(kTcMaxK, k0 - q0);
+            tc_modgemm(t, s);
+        }
+        GemmProblem<N> p{};
+        p.M = M;
+        p.Nn = kb;
+        p.K = k0;
+        p.batch = 1;
+        p.C = A + k0 + (long long)k0 * lda;
+        p.ldc = lda;
+        p.sc = 0;
+        p.alpha = ml_from_int<N>(-1);
+        p.beta = ml_one<N>();
+        p.lower_only = 1;
+        SDPG_KT_BEGIN(s);
+        crt_reconstruct_kernel<N><<<dim3(ceil_div((long long)M * ((kb + 1) / 2) * kRecLanes, 128), 1), 128, 0, s>>>(
+            c.Y, t.Mpad, t.Npad, c.E + k0, c.E + k0, 0, 0, 0, 0, p);
+        SDPG_CHECK_LAUNCH_KTW("crt_reconstruct_kernel", s,
+                              (double)M * kb * (2.0 * kCrtL + 2.0 * sizeof(mlf<N>)));
+    }
+}
+
+template bool crt_cache_applies<8>(int);
+template bool crt_cache_applies<16>(int);
+template CrtCache crt_cache_init<8>(int, const mlf<8> *, long long, void *, cudaStream_t);
+template CrtCache crt_cache_init<16>(int, const mlf<16> *, long long, void *, cudaStream_t);
+template void crt_cache_put<8>(const CrtCache &, const mlf<8> *, long long, int, int, int *, cudaStream_t);
+template void crt_cache_put<16>(const CrtCache &, const mlf<16> *, long long, int, int, int *, cudaStream_t);
+template void crt_cache_panel<8>(const CrtCache &, int, int, mlf<8> *, long long, int *, cudaStream_t);
+template void crt_cache_panel<16>(const CrtCache &, int, int, mlf<16> *, long long, int *, cudaStream_t);
 
 // device-wide sticky word: set by every tensor-core kernel that gave up a bounded wait
 int *crt_error_word() { return crt_device().error; }

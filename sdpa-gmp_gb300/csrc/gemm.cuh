@@ -18,6 +18,8 @@
 // (row-max x column-max) bound with R = 28D - 2 >= 32N + 22 guard bits; GMP's
 // sequential truncated summation in Rgemm has the same form with 2^-p.
 #pragma once
+#include <cuda_fp16.h>
+
 #include "common.cuh"
 
 namespace sdpg {
@@ -94,6 +96,30 @@ template <int N>
 size_t crt_gemm_workspace_bytes(const GemmProblem<N> &p);
 template <int N>
 void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t stream);
+// Residues of a Cholesky factor's finished columns, kept across its panels (crt_gemm.cu):
+// Q planes [kCrtL][rows][kpitch] (row i, column k of the factor), the row scales E and the
+// result planes of one panel product.
+struct CrtCache {
+    __half *Q = nullptr;
+    uint16_t *Y = nullptr;
+    int *E = nullptr;
+    int n = 0, rows = 0, kpitch = 0;
+};
+size_t crt_cache_bytes(int n);
+template <int N>
+bool crt_cache_applies(int n);
+// zeroes the planes and sets the row scales from A's diagonal (before the factorisation)
+template <int N>
+CrtCache crt_cache_init(int n, const mlf<N> *A, long long lda, void *mem, cudaStream_t s);
+// residues of the finished columns k0 .. k0 + kb - 1 (rows k0 .. n - 1; the diagonal
+// block's upper part read as zero)
+template <int N>
+void crt_cache_put(const CrtCache &c, const mlf<N> *A, long long lda, int k0, int kb, int *error, cudaStream_t s);
+// A[k0:n, k0:k0+kb] -= L[k0:n, :k0] L[k0:k0+kb, :k0]^T (lower part of the top block) from
+// the cached residues
+template <int N>
+void crt_cache_panel(const CrtCache &c, int k0, int kb, mlf<N> *A, long long lda, int *error, cudaStream_t s);
+
 // Device-wide sticky flag: set (and never cleared) when any tensor-core kernel on the
 // current device gave up a bounded wait, in addition to the product's own error word.
 int *crt_error_word();

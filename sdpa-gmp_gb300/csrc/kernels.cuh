@@ -95,6 +95,9 @@ void k_schur_f1_dense_scatter(const BlockDev<N> &B, const int *owners, int cnt, 
 // triangle is left untouched.
 template <int N>
 void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t s);
+// workspace ml_potrf carves beyond ws.used
+template <int N>
+size_t ml_potrf_workspace_bytes(int n);
 // Linv = inverse of the lower-triangular L (Rtrsm on the identity, sdpa_linear.cpp:439-455);
 // Linv's strict upper triangle is set to zero.
 template <int N>

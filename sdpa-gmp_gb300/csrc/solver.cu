@@ -393,10 +393,12 @@ class Solver final : public SolverBase {
             }
             max_ws = std::max(max_ws, gemm_bytes(32, n, n, 1) + 32 * (size_t)n * sizeof(V));
             max_ws = std::max(max_ws, ml_trtri_workspace_bytes<N>(n));
+            max_ws = std::max(max_ws, ml_potrf_workspace_bytes<N>(n));
         }
         max_ws = std::max(max_ws, gemm_bytes(m_, m_, 32, 1));
         max_ws = std::max(max_ws, gemm_bytes(m_, 32, m_, 1));  // left-looking Cholesky panel update
         max_ws = std::max(max_ws, ml_trtri_workspace_bytes<N>(m_));
+        max_ws = std::max(max_ws, ml_potrf_workspace_bytes<N>(m_));
         ws_.reserve(max_ws + (64u << 20));
         ws2_.reserve(max_ws + (64u << 20));
         // this solver's own tensor-core time-out word (zeroed by dalloc_raw): a wait that

@@ -49,8 +49,8 @@ __global__ void __launch_bounds__(128, 1)
     if (p.lower_only && n0 > m0 + kTcBM - 1) return;  // whole tile above the diagonal
     const int z = blockIdx.z;
     const int b = z / p.L, l = z - b * p.L;
-    const int arow = ((p.a_batched ? b : 0) * p.L + l) * p.Mpad + m0;
-    const int brow = ((p.b_batched ? b : 0) * p.L + l) * p.Npad + n0;
+    const int arow = ((p.a_batched ? b : 0) * p.L + l) * p.a_rows + m0;
+    const int brow = ((p.b_batched ? b : 0) * p.L + l) * p.b_rows + n0;
     const int nk = p.Kpad / kTcBK;
     const int nacc = (p.Kpad + kTcKChunk - 1) / kTcKChunk;
     const uint32_t ncols = nacc <= 1 ? 128u : nacc <= 2 ? 256u : 512u;
@@ -248,12 +248,17 @@ void tc_modgemm(const TcModGemm &p, cudaStream_t s) {
     std::call_once(attr_once, [] {
         SDPG_CUDA(cudaFuncSetAttribute(tc_modgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     });
-    const long long arows = (long long)(p.a_batched ? p.batch : 1) * p.L * p.Mpad;
-    const long long brows = (long long)(p.b_batched ? p.batch : 1) * p.L * p.Npad;
+    TcModGemm q = p;
+    if (q.a_rows <= 0) q.a_rows = p.Mpad;
+    if (q.b_rows <= 0) q.b_rows = p.Npad;
+    if (q.a_rows < p.Mpad && q.a_batched) throw sdpg_error(SDPG_ERR_ARG, "tc_modgemm: plane stride below the tile extent");
+    // the maps cover exactly the planes' rows (a caller whose tiles run past the last
+    // plane's end reads the fill value there)
+    const long long arows = (long long)(p.a_batched ? p.batch : 1) * p.L * q.a_rows - p.a_skip;
+    const long long brows = (long long)(p.b_batched ? p.batch : 1) * p.L * q.b_rows - p.b_skip;
     const CUtensorMap ma = make_map(p.A, arows, p.kpitch);
     const CUtensorMap mb = make_map(p.B, brows, p.kpitch);
     dim3 grid(p.Npad / kTcBN, p.Mpad / kTcBM, p.batch * p.L);
-    TcModGemm q = p;
     q.wait_cycles = g_tc_wait_cycles > 0 ? g_tc_wait_cycles : kWaitCycles;
     SDPG_KT_BEGIN(s);
     tc_modgemm_kernel<<<grid, 128, kSmemBytes, s>>>(ma, mb, q);

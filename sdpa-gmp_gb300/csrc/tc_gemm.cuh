@@ -29,6 +29,10 @@ struct TcModGemm {
     int batch;        // z = b * L + l; A plane (bA * L + l) with bA = b if a_batched else 0
     int a_batched, b_batched;
     int Mpad, Npad, Kpad;  // multiples of 128, 128, 64; Kpad <= kTcMaxK: the K range of this call
+    int a_rows, b_rows;    // rows between consecutive planes of A / B (0: Mpad / Npad); the
+                           // Y planes are always Mpad x Npad
+    int a_skip, b_skip;    // rows of the first plane before A / B (the pointers sit that far
+                           // into a plane store whose planes are a_rows / b_rows apart)
     int k0;                // first K index of this call within the planes (a multiple of 64)
     int kpitch;            // K extent of the planes (their row length)
     int accumulate;        // 1: Y = (Y + new) mod m (a later K chunk of the same product)
