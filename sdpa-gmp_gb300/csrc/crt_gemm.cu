@@ -134,8 +134,8 @@ struct CrtOperands {
 };
 
 // One operand of the residue conversion: entries (o, k) of X for o < rows, k < W (W
-// entries per row; either 128 is a multiple of W or W a multiple of 128, so a tile of 128
-// entries covers whole rows or part of one).  Entries with o >= O or k >= K are zero.  The
+// entries per row, rows * W a multiple of 128; a tile of 128 consecutive entries may span
+// rows).  Entries with o >= O or k >= K are zero.  The
 // residue of (o, k) for modulus l goes to Q[b qbatch + l qplane + o qrow + k], for rows
 // o < store_rows only; the row scale is E[b ebatch + o].  With tri set, entries above the
 // diagonal (o < k) count as zero.
@@ -383,13 +383,11 @@ __device__ __forceinline__ void crt_finish(const unsigned long long (&acc)[kCrtI
     *cp = v;
 }
 
-// Eight lanes share one output pair: lane g sums the moduli l = g, g + 8, ...; the
-// 64-bit word sums are combined across the eight lanes with shuffles and lanes 0 and 1
-// of the group finish the pair's two outputs.  Small products (the narrow panels of the
-// factorisations) thus still spread over many SMs.
-constexpr int kRecLanes = 8;
-
-template <int N>
+// G lanes share one output pair: lane g sums the moduli l = g, g + G, ...; the 64-bit
+// word sums are combined across the G lanes with shuffles and lanes 0 and 1 of the group
+// finish the pair's two outputs.  Small products (the narrow panels of the
+// factorisations) thus still spread over many SMs; large ones take G = 1.
+template <int N, int kRecLanes>
 __global__ void __launch_bounds__(128)
     crt_reconstruct_kernel(const uint16_t *Y, int Mpad, int Npad, const int *EA, const int *EB, long long sEA,
                            long long sEB, int b0, int alpha_one, GemmProblem<N> p) {
@@ -436,9 +434,26 @@ __global__ void __launch_bounds__(128)
         const int ea = EA[bl * sEA + i] - 2 * kCrtR;
         crt_finish<N>(a0, ea + EB[bl * sEB + j], alpha_one, p, p.C + bg * p.sc + i + (long long)j * p.ldc);
     }
-    if (g == 1 && ok1) {
+    if (g == (kRecLanes > 1 ? 1 : 0) && ok1) {
         const int ea = EA[bl * sEA + i] - 2 * kCrtR;
         crt_finish<N>(a1, ea + EB[bl * sEB + j + 1], alpha_one, p, p.C + bg * p.sc + i + (long long)(j + 1) * p.ldc);
+    }
+}
+
+// the reconstruction with the fewest lanes per output pair that still puts about
+// 80k threads in flight
+template <int N>
+void reconstruct_launch(const uint16_t *Y, int Mpad, int Npad, const int *EA, const int *EB, long long sEA,
+                        long long sEB, int b0, int alpha_one, const GemmProblem<N> &p, int batch, cudaStream_t s) {
+    const long long pairs = (long long)p.M * ((p.Nn + 1) / 2);
+    const long long want = 80 * 1024;
+    const int G = pairs * batch >= want ? 1 : pairs * batch * 2 >= want ? 2 : pairs * batch * 4 >= want ? 4 : 8;
+    const dim3 grid((unsigned)ceil_div(pairs * G, 128), batch);
+    switch (G) {
+    case 1: crt_reconstruct_kernel<N, 1><<<grid, 128, 0, s>>>(Y, Mpad, Npad, EA, EB, sEA, sEB, b0, alpha_one, p); break;
+    case 2: crt_reconstruct_kernel<N, 2><<<grid, 128, 0, s>>>(Y, Mpad, Npad, EA, EB, sEA, sEB, b0, alpha_one, p); break;
+    case 4: crt_reconstruct_kernel<N, 4><<<grid, 128, 0, s>>>(Y, Mpad, Npad, EA, EB, sEA, sEB, b0, alpha_one, p); break;
+    default: crt_reconstruct_kernel<N, 8><<<grid, 128, 0, s>>>(Y, Mpad, Npad, EA, EB, sEA, sEB, b0, alpha_one, p); break;
     }
 }
 
@@ -481,7 +496,7 @@ inline char *align256(char *p) { return (char *)(((uintptr_t)p + 255) & ~(uintpt
 template <int N>
 void residue_launch(const ResSrc<N> &s0, const ResSrc<N> &s1, const CrtDevice &dev, int *error, cudaStream_t s) {
     for (const ResSrc<N> *r : {&s0, &s1})
-        if (r->cnt > 0 && (((long long)r->rows * r->W) % kResM != 0 || (kResM % r->W != 0 && r->W % kResM != 0)))
+        if (r->cnt > 0 && ((long long)r->rows * r->W) % kResM != 0)
             throw sdpg_error(SDPG_ERR_ARG, "residue conversion: unsupported region shape");
     const int ops = s0.cnt + s1.cnt;
     if (ops <= 0) return;
@@ -613,9 +628,7 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
             }
             if (p.ev_after) SDPG_CUDA(cudaEventRecord(p.ev_after, s));
             SDPG_KT_BEGIN(s);
-            crt_reconstruct_kernel<N><<<dim3(ceil_div((long long)p.M * ((p.Nn + 1) / 2) * kRecLanes, 128), G), 128, 0,
-                                        s>>>(
-                Y, L.Mpad, L.Npad, EA, EB, ab ? L.Mpad : 0, bb ? L.Npad : 0, b0, alpha_one, p);
+            reconstruct_launch<N>(Y, L.Mpad, L.Npad, EA, EB, ab ? L.Mpad : 0, bb ? L.Npad : 0, b0, alpha_one, p, G, s);
             // every output: its kCrtL residues read, the result written, C read when beta != 0
             SDPG_CHECK_LAUNCH_KTW("crt_reconstruct_kernel", s,
                                   (double)G * p.M * p.Nn * (p.lower_only ? 0.5 : 1.0) *
@@ -757,8 +770,7 @@ void crt_cache_panel(const CrtCache &c, int k0, int kb, mlf<N> *A, long long lda
         p.beta = ml_one<N>();
         p.lower_only = 1;
         SDPG_KT_BEGIN(s);
-        crt_reconstruct_kernel<N><<<dim3(ceil_div((long long)M * ((kb + 1) / 2) * kRecLanes, 128), 1), 128, 0, s>>>(
-            c.Y, t.Mpad, t.Npad, c.E + k0, c.E + k0, 0, 0, 0, 0, p);
+        reconstruct_launch<N>(c.Y, t.Mpad, t.Npad, c.E + k0, c.E + k0, 0, 0, 0, 0, p, 1, s);
         SDPG_CHECK_LAUNCH_KTW("crt_reconstruct_kernel", s,
                               (double)M * kb * (2.0 * kCrtL + 2.0 * sizeof(mlf<N>)));
     }

@@ -121,41 +121,71 @@ __device__ float ml_to_float_scaled(const mlf<N> &a, int E) {
     return a.s ? -f : f;
 }
 
+// an mlf value from another lane of the two lanes (0 and 1) that evaluate the recurrences
+template <int M>
+__device__ __forceinline__ mlf<M> ml_shfl2(const mlf<M> &v, int src) {
+    mlf<M> r;
+    r.e = __shfl_sync(0x3u, v.e, src);
+    r.s = __shfl_sync(0x3u, v.s, src);
+#pragma unroll
+    for (int w = 0; w < M; ++w) r.m[w] = __shfl_sync(0x3u, v.m[w], src);
+    return r;
+}
+
 // p_k(lam), p_k'(lam) and p_{k-1}(lam) of det(lam I - T) at M limbs, from the diagonal d
-// and the squared off-diagonal b2 held at N limbs in shared memory
+// and the squared off-diagonal b2 held at N limbs in shared memory.  Lanes 0 and 1 of the
+// warp run it together: lane 0 the recurrence p_i = a_i p_{i-1} - b2 p_{i-2}, lane 1 its
+// derivative p_i' = p_{i-1} + a_i p_{i-1}' - b2 p_{i-2}' (a_i = lam - d_i), which takes
+// p_{i-1} from lane 0 each step; both lanes return all three values.
 template <int M, int N>
 __device__ void charpoly_at(int k, const mlf<N> *d, const mlf<N> *b2s, const mlf<M> &lam, mlf<M> *pk, mlf<M> *dpk,
                             mlf<M> *pkm1) {
-    mlf<M> p_prev = ml_one<M>(), p_cur = ml_sub(lam, ml_narrow<M, N>(d[0]));
-    mlf<M> dp_prev = ml_zero<M>(), dp_cur = ml_one<M>();
+    const bool deriv = (threadIdx.x & 1) != 0;
+    const mlf<M> p1 = mlc_sub(lam, ml_narrow<M, N>(d[0]));
+    mlf<M> x_prev = deriv ? ml_zero<M>() : ml_one<M>();
+    mlf<M> x_cur = deriv ? ml_one<M>() : p1;
+    mlf<M> p_cur = p1;  // p_{i-1}, the derivative lane's extra term
     for (int i = 1; i < k; ++i) {
-        const mlf<M> a = ml_sub(lam, ml_narrow<M, N>(d[i]));
+        const mlf<M> a = mlc_sub(lam, ml_narrow<M, N>(d[i]));
         const mlf<M> b2 = ml_narrow<M, N>(b2s[i - 1]);
-        const mlf<M> p_new = ml_sub(ml_mul(a, p_cur), ml_mul(b2, p_prev));
-        const mlf<M> dp_new = ml_sub(ml_add(p_cur, ml_mul(a, dp_cur)), ml_mul(b2, dp_prev));
-        p_prev = p_cur;
-        p_cur = p_new;
-        dp_prev = dp_cur;
-        dp_cur = dp_new;
+        mlf<M> x_new = mlc_sub(mlc_mul(a, x_cur), mlc_mul(b2, x_prev));
+        if (deriv) x_new = mlc_add(x_new, p_cur);
+        p_cur = ml_shfl2(x_new, 0);
+        x_prev = x_cur;
+        x_cur = x_new;
     }
-    *pk = p_cur;
-    *dpk = dp_cur;
-    *pkm1 = p_prev;
+    *pk = ml_shfl2(x_cur, 0);
+    *pkm1 = ml_shfl2(x_prev, 0);
+    *dpk = ml_shfl2(x_cur, 1);
+}
+
+// a / b to about H limbs of relative precision, returned at M limbs
+template <int H, int M>
+__device__ __forceinline__ mlf<M> ml_div_half(const mlf<M> &a, const mlf<M> &b) {
+    if constexpr (H >= M) {
+        return mlc_div(a, b);
+    } else {
+        return ml_widen<M, H>(mlc_div(ml_narrow<H, M>(a), ml_narrow<H, M>(b)));
+    }
 }
 
 // Newton on det(lam I - T) at M limbs until the step is below 2^-tol of the scale
-// 2^scale_e (at most maxit evaluations).  Returns 1 when that tolerance was met.
+// 2^scale_e (at most maxit evaluations).  Returns 1 when that tolerance was met.  The
+// step p_k / p_k' is formed at half precision: entering a step with relative error e,
+// the step is about e, so a quotient good to half of M's bits leaves an error of order
+// e 2^-(16 M), below the quadratic term's.  Run by lanes 0 and 1 together.
 template <int M, int N>
 __device__ int newton_level(int k, const mlf<N> *d, const mlf<N> *b2s, mlf<M> &lam, int scale_e, int tol, int maxit,
                             mlf<M> *pkm1, mlf<M> *dpk) {
+    constexpr int H = M / 2 > 2 ? M / 2 : 2;
     int prev_e = INT_MAX;
     for (int it = 0; it < maxit; ++it) {
         mlf<M> pk;
         charpoly_at<M, N>(k, d, b2s, lam, &pk, dpk, pkm1);
         if (ml_is_zero(pk)) return 1;
         if (ml_is_zero(*dpk)) return 0;
-        const mlf<M> delta = ml_div(pk, *dpk);
-        lam = ml_sub(lam, delta);
+        const mlf<M> delta = ml_div_half<H, M>(pk, *dpk);
+        lam = mlc_sub(lam, delta);
         if (ml_is_zero(delta) || delta.e < scale_e - tol) return 1;
         // steps that no longer shrink fourfold: the rounding floor of the recurrence
         if (delta.e > prev_e - 2) return 1;
@@ -171,8 +201,8 @@ __device__ int newton_level(int k, const mlf<N> *d, const mlf<N> *b2s, mlf<M> &l
 // the Gershgorin interval on the Sturm count (one point per lane) down to about 20
 // bits, then Newton's method on the characteristic polynomial from the left end of
 // the bracket at 2, 4, ... limbs up to full precision (from the left of the smallest
-// root of a real-rooted polynomial, Newton increases monotonically towards it).
-// out[1] = |z_k| = sqrt(p_{k-1}(lam) / p_k'(lam)).
+// root of a real-rooted polynomial, Newton increases monotonically towards it), on
+// lanes 0 and 1.  out[1] = |z_k| = sqrt(p_{k-1}(lam) / p_k'(lam)).
 template <int N>
 __global__ void tridiag_min_kernel(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *status,
                                    const int *gate) {
@@ -253,7 +283,7 @@ __global__ void tridiag_min_kernel(int k, const mlf<N> *d, const mlf<N> *e, mlf<
         if (i + 1 < k) b2s[i] = ml_mul(e[i], e[i]);
     }
     __syncwarp();
-    if (lane != 0) return;
+    if (lane >= 2) return;  // lanes 0 and 1 evaluate the recurrences (charpoly_at)
     const int scale_e = E + ilogbf(scale) + 1;
     mlf<2> l2 = ml_ldexp(ml_from_float<2>(bounds[0]), E);
     mlf<N> lam, pkm1, dpk;
@@ -281,10 +311,15 @@ __global__ void tridiag_min_kernel(int k, const mlf<N> *d, const mlf<N> *e, mlf<
         }
         ok = newton_level<N, N>(k, ds, b2s, lam, scale_e, 32 * N - 4, 8, &pkm1, &dpk);
     }
-    out[0] = lam;
-    const mlf<N> z2 = ml_is_zero(dpk) ? ml_zero<N>() : ml_abs(ml_div(pkm1, dpk));
-    out[1] = ml_sqrt(z2);
-    *status = ok ? 0 : 2;
+    // |z_k| = sqrt(p_{k-1} / p_k') = |p_{k-1}| / sqrt(|p_{k-1} p_k'|): one inverse square
+    // root instead of a quotient and a square root
+    const mlf<N> prod = ml_abs(mlc_mul(pkm1, dpk));
+    const mlf<N> z = ml_is_zero(prod) ? ml_zero<N>() : mlc_mul(ml_abs(pkm1), mlc_rsqrt(prod));
+    if (lane == 0) {
+        out[0] = lam;
+        out[1] = z;
+        *status = ok ? 0 : 2;
+    }
 }
 
 // Householder reduction of the symmetric n x n A (lower triangle used) to tridiagonal form.
@@ -400,6 +435,17 @@ void k_tridiag_min(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *st
 // run goes on, ctl[1] = steps done.  Every kernel of a step returns at once when ctl[0]
 // is 0, so the host can enqueue several steps ahead and read the state once.
 
+// The next step's vectors, by the CTA that decided to take it: qold = q, q = r / beta.
+template <int N>
+__device__ void lz_advance(int n, const mlf<N> *r, const mlf<N> *sl, mlf<N> *q, mlf<N> *qold, const int *ctl) {
+    if (!ctl[0]) return;
+    const mlf<N> inv = sl[0];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        qold[i] = q[i];
+        q[i] = mlc_mul(r[i], inv);
+    }
+}
+
 template <int N>
 __global__ void lz_next_kernel(int n, const mlf<N> *r, const mlf<N> *sl, mlf<N> *q, mlf<N> *qold, const int *ctl) {
     if (!ctl[0]) return;
@@ -418,20 +464,26 @@ __device__ void lz_control(mlf<N> *sl, mlf<N> *te, int *ctl, int k, int eig, int
         sl[8] = sl[4];
         sl[10] = sl[5];
     }
-    const mlf<N> beta = ml_sqrt(sl[6]);
+    // beta = sqrt(r.r) and 1/beta from one inverse square root: y = (r.r)^(-1/2) is 1/beta,
+    // beta = (r.r) y refined by half a Newton step
+    const mlf<N> rr = sl[6];
+    const mlf<N> y = mlc_rsqrt(rr);
+    mlf<N> beta = mlc_mul(rr, y);
+    beta = mlc_add(beta, ml_ldexp(mlc_mul(y, mlc_sub(rr, mlc_mul(beta, beta))), -1));
+    if (ml_is_zero(rr) || rr.s) beta = ml_zero<N>();
     te[k] = beta;
     sl[1] = beta;
-    sl[0] = ml_is_zero(beta) ? ml_zero<N>() : ml_div(ml_one<N>(), beta);
+    sl[0] = ml_is_zero(beta) ? ml_zero<N>() : y;
     ctl[1] = k + 1;
     const int kn = k + 1;
     const mlf<N> mn = sl[8], mo = sl[9], er = sl[10];
     bool go = kn < n && kn < kgo && ml_cmp(beta, ml_from_double<N>(1.0e-16)) > 0;
     if (go) {
         const mlf<N> amin = ml_abs(mn);
-        const bool c1 = ml_cmp(ml_abs(ml_sub(mn, mo)),
-                               ml_add(ml_mul(ml_from_double<N>(1.0e-5), amin), ml_from_double<N>(1.0e-8))) > 0;
-        const bool c2 = ml_cmp(ml_abs(ml_mul(er, beta)),
-                               ml_add(ml_mul(ml_from_double<N>(1.0e-2), amin), ml_from_double<N>(1.0e-4))) > 0;
+        const bool c1 = ml_cmp(ml_abs(mlc_sub(mn, mo)),
+                               mlc_add(mlc_mul(ml_from_double<N>(1.0e-5), amin), ml_from_double<N>(1.0e-8))) > 0;
+        const bool c2 = ml_cmp(ml_abs(mlc_mul(er, beta)),
+                               mlc_add(mlc_mul(ml_from_double<N>(1.0e-2), amin), ml_from_double<N>(1.0e-4))) > 0;
         go = c1 || c2;
     }
     if (kn + 1 >= kmax) go = false;
@@ -442,7 +494,7 @@ __device__ void lz_control(mlf<N> *sl, mlf<N> *te, int *ctl, int k, int eig, int
 // r.r in one CTA of 256 threads (the strided pairs and block sum of the dot kernel);
 // without an eigenvalue solve at this step also the loop control.
 template <int N>
-__global__ void __launch_bounds__(256) lz_update_kernel(int n, const mlf<N> *w, const mlf<N> *q, const mlf<N> *qold,
+__global__ void __launch_bounds__(256) lz_update_kernel(int n, const mlf<N> *w, mlf<N> *q, mlf<N> *qold,
                                                         mlf<N> *td, mlf<N> *te, mlf<N> *sl, mlf<N> *r, int *ctl,
                                                         int k, int eig, int kgo, int kmax) {
     __shared__ mlf<N> alpha_s;
@@ -451,46 +503,58 @@ __global__ void __launch_bounds__(256) lz_update_kernel(int n, const mlf<N> *w, 
     mlf<N> a0 = ml_zero<N>(), a1 = ml_zero<N>();
     int i = threadIdx.x;
     for (; i + stride < n; i += 2 * stride) {
-        a0 = ml_add(a0, ml_mul(q[i], w[i]));
-        a1 = ml_add(a1, ml_mul(q[i + stride], w[i + stride]));
+        a0 = mlc_add(a0, mlc_mul(q[i], w[i]));
+        a1 = mlc_add(a1, mlc_mul(q[i + stride], w[i + stride]));
     }
-    if (i < n) a0 = ml_add(a0, ml_mul(q[i], w[i]));
-    const mlf<N> alpha = ml_block_sum(ml_add(a0, a1));
+    if (i < n) a0 = mlc_add(a0, mlc_mul(q[i], w[i]));
+    const mlf<N> alpha = mlc_block_sum(mlc_add(a0, a1));
     if (threadIdx.x == 0) {
         alpha_s = alpha;
         td[k] = alpha;
     }
     __syncthreads();
     const mlf<N> al = alpha_s, be = sl[1];
-    for (int j = threadIdx.x; j < n; j += stride) r[j] = ml_sub(ml_sub(w[j], ml_mul(q[j], al)), ml_mul(qold[j], be));
+    for (int j = threadIdx.x; j < n; j += stride) r[j] = mlc_sub(mlc_sub(w[j], mlc_mul(q[j], al)), mlc_mul(qold[j], be));
     __syncthreads();
     a0 = ml_zero<N>();
     a1 = ml_zero<N>();
     i = threadIdx.x;
     for (; i + stride < n; i += 2 * stride) {
-        a0 = ml_add(a0, ml_mul(r[i], r[i]));
-        a1 = ml_add(a1, ml_mul(r[i + stride], r[i + stride]));
+        a0 = mlc_add(a0, mlc_mul(r[i], r[i]));
+        a1 = mlc_add(a1, mlc_mul(r[i + stride], r[i + stride]));
     }
-    if (i < n) a0 = ml_add(a0, ml_mul(r[i], r[i]));
-    const mlf<N> rr = ml_block_sum(ml_add(a0, a1));
+    if (i < n) a0 = mlc_add(a0, mlc_mul(r[i], r[i]));
+    const mlf<N> rr = mlc_block_sum(mlc_add(a0, a1));
     if (threadIdx.x == 0) {
         sl[6] = rr;
         if (!eig) lz_control(sl, te, ctl, k, 0, n, kgo, kmax);
     }
+    if (!eig) {
+        __syncthreads();
+        lz_advance(n, r, sl, q, qold, ctl);
+    }
 }
 
 template <int N>
-__global__ void lz_control_kernel(mlf<N> *sl, mlf<N> *te, int *ctl, int k, int n, int kgo, int kmax) {
-    if (!ctl[0]) return;
-    lz_control(sl, te, ctl, k, 1, n, kgo, kmax);
+__global__ void __launch_bounds__(256) lz_control_kernel(int n, const mlf<N> *r, mlf<N> *q, mlf<N> *qold, mlf<N> *sl,
+                                                         mlf<N> *te, int *ctl, int k, int kgo, int kmax) {
+    // every thread reads the flag before thread 0 may rewrite it
+    const int go = ctl[0];
+    __syncthreads();
+    if (!go) return;
+    if (threadIdx.x == 0) lz_control(sl, te, ctl, k, 1, n, kgo, kmax);
+    __syncthreads();
+    lz_advance(n, r, sl, q, qold, ctl);
 }
 
 template <int N>
 void k_lanczos_step(int n, const mlf<N> *M, mlf<N> *r, mlf<N> *q, mlf<N> *qold, mlf<N> *w, mlf<N> *td, mlf<N> *te,
                     mlf<N> *sl, int *ctl, int *status, int k, int eig, int kgo, int kmax, cudaStream_t s) {
-    SDPG_KT_BEGIN(s);
-    lz_next_kernel<N><<<ceil_div(n, 128), 128, 0, s>>>(n, r, sl, q, qold, ctl);
-    SDPG_CHECK_LAUNCH_KT("lz_next_kernel", s);
+    if (k == 0) {  // later steps get q from the previous step's update or control kernel
+        SDPG_KT_BEGIN(s);
+        lz_next_kernel<N><<<ceil_div(n, 128), 128, 0, s>>>(n, r, sl, q, qold, ctl);
+        SDPG_CHECK_LAUNCH_KT("lz_next_kernel", s);
+    }
     if (n >= 128) {
         SDPG_KT_BEGIN(s);
         matvec_t_split_kernel<N><<<ceil_div(n, kWarpsPerBlock / kMvSplit), 32 * kWarpsPerBlock, 0, s>>>(n, M, 0, q, w,
@@ -506,7 +570,7 @@ void k_lanczos_step(int n, const mlf<N> *M, mlf<N> *r, mlf<N> *q, mlf<N> *qold, 
     if (eig) {
         k_tridiag_min<N>(k + 1, td, te, sl + 4, status, s, ctl);
         SDPG_KT_BEGIN(s);
-        lz_control_kernel<N><<<1, 1, 0, s>>>(sl, te, ctl, k, n, kgo, kmax);
+        lz_control_kernel<N><<<1, 256, 0, s>>>(n, r, q, qold, sl, te, ctl, k, kgo, kmax);
         SDPG_CHECK_LAUNCH_KT("lz_control_kernel", s);
     }
 }

@@ -9,7 +9,8 @@ Each routine replaces one MPLAPACK call of the reference's Lal class:
 
 Residuals are formed exactly (dyadic integers) from the GPU's outputs.  Tolerances
 (p = 32 * limbs bits, normwise like GMP's truncated arithmetic in MPLAPACK):
-  Cholesky   max|L L^T - A|    <= 2^-(p-20) n max|A|
+  Cholesky   max|L L^T - A|    <= 2^-(p-20) n max|A|  (n <= 97, exact residual);
+             |L L^T - A|_ij    <= 2^-(p-24) n sqrt(A_ii A_jj)  (n = 200 .. 501)
   inverse    max|L X - I|      <= 2^-(p-24) n max|L| max|X|, strict upper of X exactly 0
   solve      max|L L^T x - b|  <= 2^-(p-24) n^2 max|L|^2 max|x|
   eigen      no eigenvalue below lambda - delta, one below lambda + delta (exact inertia),
@@ -74,6 +75,41 @@ def test_rpotrf_residual(sdpg, exact, limbs, n):
     assert worst <= Fraction(n) * exact.max_abs(Ad) / (1 << (32 * limbs - 20)), float(worst)
     # diagonal of the factor is positive
     assert all(L[i + i * n][0] > 0 for i in range(n))
+
+
+@gpu
+@pytest.mark.parametrize("n,spread", [(200, 0), (333, 40), (501, 20)])
+def test_rpotrf_residual_large(sdpg, n, spread):
+    """Factors of the Schur and X / Z sizes (256 bits, the residue path with the panel
+    residues cached): A = D^(1/2) (c I + S) D^(1/2) with S symmetric in [-1, 1] and the
+    row scales D_i = 2^k_i, k_i uniform in [-spread, spread].  The residual L L^T - A,
+    formed by the digit GEMM (normwise error 2^-240), must satisfy Cholesky's
+    componentwise backward-error form |R_ij| <= 2^-(p-24) n sqrt(A_ii A_jj)."""
+    rng = np.random.default_rng(n + spread)
+    S = rng.uniform(-1, 1, (n, n))
+    S = np.round((S + S.T) * 2.0 ** 20) / 2.0 ** 21
+    k = rng.integers(-spread, spread + 1, n) if spread else np.zeros(n, dtype=int)
+    half = np.exp2(k / 2.0).round(6)  # exact doubles, about 2^(k/2)
+    A = (S + np.eye(n) * (n / 4.0)) * np.outer(half, half)
+    Aml = sdpg.ml_from_double(A.T.reshape(-1), 8)  # column-major
+    Lml, info = sdpg.rpotrf(Aml, n, n)
+    assert info == 0
+    lower = np.tril(np.ones((n, n), dtype=bool)).T.reshape(-1)  # column-major i >= j
+    Lml[~lower] = 0
+    one = sdpg.ml_from_double(np.array([1.0]), 8)
+    mone = sdpg.ml_from_double(np.array([-1.0]), 8)
+    old = sdpg.set_gemm_method(1)
+    try:
+        R = sdpg.rgemm("N", "T", n, n, n, one, Lml, n, Lml, n, mone, Aml, n)
+    finally:
+        sdpg.set_gemm_method(old)
+    Rd = np.abs(sdpg.ml_to_double(R).reshape(n, n).T)
+    d = np.sqrt(np.diag(A))
+    bound = 2.0 ** -(256 - 24) * n * np.outer(d, d)
+    worst = float(np.max(Rd / bound))
+    print(f"\nn={n} spread={spread}: max |L L^T - A| / bound = {worst:.3e}")
+    assert worst <= 1.0
+    assert sdpg.tensor_error(0) == 0
 
 
 @gpu
