@@ -141,15 +141,15 @@ template <int M, int N>
 __device__ void charpoly_at(int k, const mlf<N> *d, const mlf<N> *b2s, const mlf<M> &lam, mlf<M> *pk, mlf<M> *dpk,
                             mlf<M> *pkm1) {
     const bool deriv = (threadIdx.x & 1) != 0;
-    const mlf<M> p1 = mlc_sub(lam, ml_narrow<M, N>(d[0]));
+    const mlf<M> p1 = ml_sub(lam, ml_narrow<M, N>(d[0]));
     mlf<M> x_prev = deriv ? ml_zero<M>() : ml_one<M>();
     mlf<M> x_cur = deriv ? ml_one<M>() : p1;
     mlf<M> p_cur = p1;  // p_{i-1}, the derivative lane's extra term
     for (int i = 1; i < k; ++i) {
-        const mlf<M> a = mlc_sub(lam, ml_narrow<M, N>(d[i]));
+        const mlf<M> a = ml_sub(lam, ml_narrow<M, N>(d[i]));
         const mlf<M> b2 = ml_narrow<M, N>(b2s[i - 1]);
-        mlf<M> x_new = mlc_sub(mlc_mul(a, x_cur), mlc_mul(b2, x_prev));
-        if (deriv) x_new = mlc_add(x_new, p_cur);
+        mlf<M> x_new = ml_sub(ml_mul(a, x_cur), ml_mul(b2, x_prev));
+        if (deriv) x_new = ml_add(x_new, p_cur);
         p_cur = ml_shfl2(x_new, 0);
         x_prev = x_cur;
         x_cur = x_new;
