@@ -200,7 +200,7 @@ __device__ int newton_level(int k, const mlf<N> *d, const mlf<N> *b2s, mlf<M> &l
 // Smallest eigenvalue of tridiag(e, d, e): a 32-way single-precision multisection of
 // the Gershgorin interval on the Sturm count (one point per lane) down to about 20
 // bits, then Newton's method on the characteristic polynomial from the left end of
-// the bracket at 2, 4, ... limbs up to full precision (from the left of the smallest
+// the bracket at 4, 8, ... limbs up to full precision (from the left of the smallest
 // root of a real-rooted polynomial, Newton increases monotonically towards it), on
 // lanes 0 and 1.  out[1] = |z_k| = sqrt(p_{k-1}(lam) / p_k'(lam)).
 template <int N>
@@ -285,21 +285,19 @@ __global__ void tridiag_min_kernel(int k, const mlf<N> *d, const mlf<N> *e, mlf<
     __syncwarp();
     if (lane >= 2) return;  // lanes 0 and 1 evaluate the recurrences (charpoly_at)
     const int scale_e = E + ilogbf(scale) + 1;
-    mlf<2> l2 = ml_ldexp(ml_from_float<2>(bounds[0]), E);
     mlf<N> lam, pkm1, dpk;
     int ok;
-    {
-        mlf<2> a, b;
-        newton_level<2, N>(k, ds, b2s, l2, scale_e, 50, 8, &a, &b);
-    }
     if constexpr (N <= 4) {
-        lam = ml_widen<N, 2>(l2);
-        ok = newton_level<N, N>(k, ds, b2s, lam, scale_e, 32 * N - 4, 8, &pkm1, &dpk);
+        lam = ml_ldexp(ml_from_float<N>(bounds[0]), E);
+        ok = newton_level<N, N>(k, ds, b2s, lam, scale_e, 32 * N - 4, 10, &pkm1, &dpk);
     } else {
-        mlf<4> l4 = ml_widen<4, 2>(l2);
+        // from the ~20-bit float bracket straight to 4 limbs: a 2-limb step costs about
+        // as much as a 4-limb one here, so three 4-limb steps (20 -> 40 -> 80 -> 124 bits)
+        // replace two of each
+        mlf<4> l4 = ml_ldexp(ml_from_float<4>(bounds[0]), E);
         {
             mlf<4> a, b;
-            newton_level<4, N>(k, ds, b2s, l4, scale_e, 110, 6, &a, &b);
+            newton_level<4, N>(k, ds, b2s, l4, scale_e, 110, 8, &a, &b);
         }
         if constexpr (N <= 8) {
             lam = ml_widen<N, 4>(l4);
