@@ -50,7 +50,7 @@ TC_TRAFFIC_BYTES = 81.8e6
 TRAFFIC_PER_ALG_BYTE = {"crt_residue_kernel": 71.1 / 90.0, "crt_reconstruct_kernel": 35.9 / 45.0}
 # Kernel families with an algorithmic-work figure (sdpg_kernel_times' work column):
 # roofline bound and the unit of that work.
-FAMILY_BOUND = {"crt_residue_kernel": "hbm", "crt_exp_kernel": "hbm", "crt_reconstruct_kernel": "hbm",
+FAMILY_BOUND = {"tc_residue_kernel": "hbm", "crt_exp_kernel": "hbm", "crt_reconstruct_kernel": "hbm",
                 "lz_matvec_kernel": "hbm", "tc_modgemm_kernel": "tensor"}
 
 

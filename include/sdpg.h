@@ -277,7 +277,7 @@ int sdpg_tensor_error(int device, int *flag);
  * "name launches milliseconds work", sorted by name, into buf, forgets the records and
  * returns the number of lines (SDPG_ERR_TOO_LARGE if cap is too small).  `work` is the
  * launches' summed algorithmic work where the library states one: for
- * crt_residue_kernel, crt_exp_kernel, crt_reconstruct_kernel and lz_matvec_kernel the
+ * tc_residue_kernel, crt_exp_kernel, crt_reconstruct_kernel and lz_matvec_kernel the
  * bytes the kernel must move (multi-limb entries read, residue planes written, ...), for
  * tc_modgemm_kernel the fp16 tensor flops 2 M N K per residue GEMM; 0 elsewhere. */
 int sdpg_kernel_timing(int enable);
@@ -288,7 +288,9 @@ int sdpg_kernel_times(char *buf, int cap);
  * copy takes, those waits give up: the kernel records the time-out in the caller's
  * error word and the sticky device flag (sdpg_tensor_error), waits with the full
  * budget for the copies and products it already issued, frees its tensor memory and
- * returns; a solver then fails with SDPG_ERR_TIMEOUT.  Returns the previous setting. */
+ * returns; a solver then fails with SDPG_ERR_TIMEOUT.  The same budget bounds each
+ * barrier wait of the one-launch Lanczos loop (a give-up there also fails the solver
+ * with SDPG_ERR_TIMEOUT, after the loop has run out).  Returns the previous setting. */
 long long sdpg_set_tensor_wait_budget(long long cycles);
 /* Measured throughput of signed 32x32->64 multiply-adds (IMAD.WIDE) on one GPU, the
  * instruction the multi-limb GEMM is built from; the plain path's roofline denominator. */

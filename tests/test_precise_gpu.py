@@ -31,8 +31,10 @@ from precise import errors, golden_errors
 # bound sits a few bits above the error measured on a GB300 (in brackets: objValPrimal,
 # objValDual, relgap; xVec; xMat, yMat).
 BOUNDS = {
-    # after 5 iterations: [-225.9, -234.2, exact; -225.9; -226.1, -234.2]
-    "gpp500_it5": (-220, -220, -220),
+    # after 5 iterations: [-218.8, -218.8, exact; -218.8; -218.3, -218.8] (-225.9 .. -234.2
+    # with the earlier tridiagonal Newton ladder: the agreement moves by a few bits with
+    # the rounding of the step lengths, amplified by the iterations)
+    "gpp500_it5": (-214, -214, -214),
     # after 10: [-135.3, -135.6, -134.5; -133.4; -133.4, -133.9]
     "gpp500_it10": (-128, -128, -128),
     # after 20: [-153.5, -147.0, -147.0; -131.1; -131.1, -145.3]
