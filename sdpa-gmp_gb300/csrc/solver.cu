@@ -19,6 +19,18 @@
 
 namespace sdpg {
 
+namespace {
+std::atomic<int> g_device_shared[64];
+}
+
+void device_shared_enter(int device) {
+    if (device >= 0 && device < 64) g_device_shared[device].fetch_add(1);
+}
+void device_shared_leave(int device) {
+    if (device >= 0 && device < 64) g_device_shared[device].fetch_sub(1);
+}
+int device_shared(int device) { return (device >= 0 && device < 64) ? g_device_shared[device].load() : 0; }
+
 const char *phase_name(int phase) {
     switch (phase) {
         case noINFO: return "noINFO    ";
@@ -38,30 +50,6 @@ const char *phase_name(int phase) {
 namespace {
 
 enum Formula { F1 = 0, F2 = 1, F3 = 2 };
-
-// Solvers alive per device (a solver counts from construction to destruction).
-std::atomic<int> g_live_solvers[64];
-
-int live_solvers(int device) { return (device >= 0 && device < 64) ? g_live_solvers[device].load() : 0; }
-
-class LiveSolver {
-  public:
-    LiveSolver() = default;
-    explicit LiveSolver(int device) : dev_(device >= 0 && device < 64 ? device : -1) {
-        if (dev_ >= 0) g_live_solvers[dev_].fetch_add(1);
-    }
-    LiveSolver(const LiveSolver &) = delete;
-    LiveSolver &operator=(LiveSolver &&o) noexcept {
-        std::swap(dev_, o.dev_);
-        return *this;
-    }
-    ~LiveSolver() {
-        if (dev_ >= 0) g_live_solvers[dev_].fetch_sub(1);
-    }
-
-  private:
-    int dev_ = -1;
-};
 
 template <int N>
 class Solver final : public SolverBase {
@@ -94,7 +82,6 @@ class Solver final : public SolverBase {
     Solver(const RawProblem &P, const Param &par, int device, cudaStream_t stream)
         : par_(par), lambda_default_(par.lambdaStar), dev_(device), st_(stream) {
         SDPG_CUDA(cudaSetDevice(device));
-        live_ = LiveSolver(device);
         if (!st_) throw sdpg_error(SDPG_ERR_ARG, "the solver needs a stream");
         keep_pool_memory(device);
         ws_.stream = st_;
@@ -925,9 +912,9 @@ class Solver final : public SolverBase {
             const char *e = getenv("SDPG_LANCZOS_STEPWISE");
             return e && *e && *e != '0';
         }();
-        // with other solvers running on the device their kernels could hold SMs the
-        // cooperative launch waits for: the step-by-step launches then
-        if (stepwise || T.empty() || T.size() > (size_t)kLzMaxRuns || live_solvers(dev_) > 1) return false;
+        // while a batch runs several solvers at once on this device, their kernels hold SMs
+        // the cooperative launch would wait for: the step-by-step launches then
+        if (stepwise || T.empty() || T.size() > (size_t)kLzMaxRuns || device_shared(dev_)) return false;
         int ctas = 0, kmax_all = 0;
         for (const Lz &t : T) {
             if (!t.active || t.B->lanczos_kmax > 128) return false;
@@ -1917,7 +1904,6 @@ class Solver final : public SolverBase {
     V *BLinv_ = nullptr, *BLinvT_ = nullptr, *Dytmp_ = nullptr;  // inverse of the Schur factor and its transpose
     V *b_ = nullptr, *y_ = nullptr, *Dy_ = nullptr, *g_ = nullptr, *p_ = nullptr, *B_ = nullptr, *slot_ = nullptr;
     int *info_ = nullptr, *status_ = nullptr;
-    LiveSolver live_;
     int *lz_err_ = nullptr;    // device: a barrier wait of the one-launch Lanczos loop gave up
     int *lz_err_h_ = nullptr;  // its host copy (a pinned slot)
     R muInit_, muCur_, thP_, thD_, aP_, aD_, betaV_, rho_, etaP_, etaD_, objP_, objD_, normP_, normD_;
