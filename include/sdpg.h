@@ -288,9 +288,7 @@ int sdpg_kernel_times(char *buf, int cap);
  * copy takes, those waits give up: the kernel records the time-out in the caller's
  * error word and the sticky device flag (sdpg_tensor_error), waits with the full
  * budget for the copies and products it already issued, frees its tensor memory and
- * returns; a solver then fails with SDPG_ERR_TIMEOUT.  The same budget bounds each
- * barrier wait of the one-launch Lanczos loop (a give-up there also fails the solver
- * with SDPG_ERR_TIMEOUT, after the loop has run out).  Returns the previous setting. */
+ * returns; a solver then fails with SDPG_ERR_TIMEOUT.  Returns the previous setting. */
 long long sdpg_set_tensor_wait_budget(long long cycles);
 /* Measured throughput of signed 32x32->64 multiply-adds (IMAD.WIDE) on one GPU, the
  * instruction the multi-limb GEMM is built from; the plain path's roofline denominator. */

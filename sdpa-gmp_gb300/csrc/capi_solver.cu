@@ -629,12 +629,6 @@ int sdpg_solve_batch(int count, sdpg_problem *const *problems, const sdpg_param 
             }
         };
         const int nt = std::min(concurrency, std::max(count, 1));
-        struct Shared {  // the device is shared while more than one solver runs at once
-            int dev;
-            bool on;
-            Shared(int d, bool o) : dev(d), on(o) { if (on) device_shared_enter(dev); }
-            ~Shared() { if (on) device_shared_leave(dev); }
-        } shared(device, nt > 1);
         std::vector<std::thread> threads;
         threads.reserve(nt);
         for (int t = 0; t < nt; ++t) threads.emplace_back(worker);

@@ -581,210 +581,6 @@ void k_lanczos_step(int n, const mlf<N> *M, mlf<N> *r, mlf<N> *q, mlf<N> *qold, 
     }
 }
 
-// ---- the whole Lanczos loop in one cooperative launch ---------------------------------
-//
-// Every run (a block and side) gets its own group of CTAs; all CTAs of the launch are
-// resident at once (cooperative launch), and the CTAs of one run meet at a barrier of
-// their own (an arrival counter and a generation word) four times per step:
-//   A  w = M q, one warp per output (rows of the symmetric operator read as columns),
-//      and each CTA's part of alpha = q.w;
-//   B  alpha from the parts, r = (w - alpha q) - beta qold for a slice of the entries,
-//      and each CTA's part of r.r;
-//   C  the run's first CTA: r.r, the tridiagonal entry, the tridiagonal eigenvalue solve
-//      on an eigenvalue step (one warp), and the loop control of Lal::getMinEigen;
-//   D  if the loop goes on, q = r / beta and qold = q for a slice of the entries.
-// Data written by one CTA and read by another go through L2 (ld.global.cg), never a
-// stale L1 line.  Every barrier wait is bounded: on time-out the launch's error word is
-// set, later barriers no longer wait, and the kernel runs out its (bounded) loop.
-
-template <int N>
-__device__ __forceinline__ mlf<N> ml_ldcg(const mlf<N> *p) {
-    static_assert(sizeof(mlf<N>) % 8 == 0, "mlf is a whole number of 8-byte words");
-    mlf<N> v;
-    const int2 *src = reinterpret_cast<const int2 *>(p);
-    int2 *dst = reinterpret_cast<int2 *>(&v);
-#pragma unroll
-    for (int w = 0; w < (int)(sizeof(mlf<N>) / 8); ++w) dst[w] = __ldcg(src + w);
-    return v;
-}
-
-__device__ __forceinline__ int lz_grid_sync(unsigned *bar, int ncta, int *error, long long budget) {
-    __shared__ int ok_s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = *(volatile int *)error == 0;
-        if (ok) {
-            const unsigned gen = *(volatile unsigned *)&bar[1];
-            __threadfence();
-            if (atomicAdd(&bar[0], 1u) == (unsigned)ncta - 1u) {
-                atomicExch(&bar[0], 0u);
-                __threadfence();
-                atomicAdd(&bar[1], 1u);
-            } else {
-                const long long t0 = clock64();
-                while (*(volatile unsigned *)&bar[1] == gen) {
-                    if (clock64() - t0 > budget) {
-                        atomicExch(error, 1);
-                        ok = 0;
-                        break;
-                    }
-                    __nanosleep(64);
-                }
-            }
-            __threadfence();
-        }
-        ok_s = ok;
-    }
-    __syncthreads();
-    return ok_s;
-}
-
-// sum of one value per CTA thread-0 slot over a block of 256 threads: v on every
-// thread, result on thread 0 (out-of-line additions)
-template <int N>
-__device__ __forceinline__ mlf<N> lz_sum_parts(const mlf<N> *part, int cnt) {
-    mlf<N> v = ml_zero<N>();
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) v = mlc_add(v, ml_ldcg(part + i));
-    return mlc_block_sum(v);
-}
-
-template <int N>
-__global__ void __launch_bounds__(256) lz_persistent_kernel(LzLaunch<N> P) {
-    extern __shared__ uint8_t lz_smem[];  // the tridiagonal solve's 2 kmax values (first CTA of a run)
-    __shared__ mlf<N> bcast;
-    __shared__ int go_s;
-    // this CTA's run (selected, not indexed by a run-time value)
-    LzRunDev<N> R = P.run[0];
-#pragma unroll
-    for (int i = 1; i < kLzMaxRuns; ++i)
-        if (i < P.nruns && (int)blockIdx.x >= P.run[i].cta0) R = P.run[i];
-    const int c = (int)blockIdx.x - R.cta0;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int n = R.n;
-    const int T = R.ncta * (int)blockDim.x;  // elementwise stride of the run
-    const long long budget = P.wait_cycles;
-    int *err = P.error;
-    // step 0 starts from r = 1, beta = |r| (the slots) and q = 0: qold = q, q = r / beta
-    if (R.k0 == 0) {
-        const mlf<N> inv = ml_ldcg(R.sl + 0);
-        for (int o = c * (int)blockDim.x + threadIdx.x; o < n; o += T) {
-            R.qold[o] = ml_ldcg(R.q + o);
-            R.q[o] = mlc_mul(ml_ldcg(R.r + o), inv);
-        }
-        lz_grid_sync(R.bar, R.ncta, err, budget);
-    }
-    for (int k = R.k0; k < n && k + 1 < R.kmax; ++k) {
-        if (threadIdx.x == 0) go_s = *(volatile int *)&R.ctl[0] != 0 && *(volatile int *)err == 0;
-        __syncthreads();
-        if (!go_s) break;
-        // A: w = M q and this CTA's part of alpha = q.w
-        mlf<N> pa = ml_zero<N>();
-        for (int o = c * nw + warp; o < n; o += R.ncta * nw) {
-            const mlf<N> *col = R.M + (long long)o * n;
-            mlf<N> a0 = ml_zero<N>(), a1 = ml_zero<N>();
-            int i = lane;
-            for (; i + 32 < n; i += 64) {
-                a0 = ml_add(a0, ml_mul(col[i], ml_ldcg(R.q + i)));
-                a1 = ml_add(a1, ml_mul(col[i + 32], ml_ldcg(R.q + i + 32)));
-            }
-            if (i < n) a0 = ml_add(a0, ml_mul(col[i], ml_ldcg(R.q + i)));
-            const mlf<N> wo = mlc_warp_sum(mlc_add(a0, a1));
-            if (lane == 0) {
-                R.w[o] = wo;
-                pa = mlc_add(pa, mlc_mul(ml_ldcg(R.q + o), wo));
-            }
-        }
-        {
-            const mlf<N> s = mlc_block_sum(lane == 0 ? pa : ml_zero<N>());
-            if (threadIdx.x == 0) R.partA[c] = s;
-        }
-        lz_grid_sync(R.bar, R.ncta, err, budget);
-        // B: alpha, r and this CTA's part of r.r
-        {
-            const mlf<N> al = lz_sum_parts(R.partA, R.ncta);
-            if (threadIdx.x == 0) bcast = al;
-            __syncthreads();
-        }
-        const mlf<N> alpha = bcast;
-        const mlf<N> beta = ml_ldcg(R.sl + 1);
-        mlf<N> prr = ml_zero<N>();
-        for (int o = c * (int)blockDim.x + threadIdx.x; o < n; o += T) {
-            const mlf<N> ro = mlc_sub(mlc_sub(ml_ldcg(R.w + o), mlc_mul(ml_ldcg(R.q + o), alpha)),
-                                      mlc_mul(ml_ldcg(R.qold + o), beta));
-            R.r[o] = ro;
-            prr = mlc_add(prr, mlc_mul(ro, ro));
-        }
-        {
-            const mlf<N> s = mlc_block_sum(prr);
-            if (threadIdx.x == 0) R.partR[c] = s;
-        }
-        lz_grid_sync(R.bar, R.ncta, err, budget);
-        // C: the run's first CTA closes the step
-        const int eig = k < 128 && ((((k >> 6) ? R.eig[1] : R.eig[0]) >> (k & 63)) & 1ull);
-        if (c == 0) {
-            const mlf<N> rr = lz_sum_parts(R.partR, R.ncta);
-            if (threadIdx.x == 0) {
-                R.sl[6] = rr;
-                R.td[k] = alpha;
-            }
-            __syncthreads();
-            if (eig) {
-                if (warp == 0) tridiag_min_warp<N>(k + 1, R.td, R.te, R.sl + 4, R.status,
-                                                   reinterpret_cast<mlf<N> *>(lz_smem));
-                __syncthreads();
-            }
-            if (threadIdx.x == 0) lz_control(R.sl, R.te, R.ctl, k, eig, n, R.kgo, R.kmax);
-        }
-        lz_grid_sync(R.bar, R.ncta, err, budget);
-        // D: the next step's vectors
-        if (threadIdx.x == 0) go_s = *(volatile int *)&R.ctl[0];
-        __syncthreads();
-        if (go_s) {
-            const mlf<N> inv = ml_ldcg(R.sl + 0);
-            for (int o = c * (int)blockDim.x + threadIdx.x; o < n; o += T) {
-                R.qold[o] = ml_ldcg(R.q + o);
-                R.q[o] = mlc_mul(ml_ldcg(R.r + o), inv);
-            }
-        }
-        lz_grid_sync(R.bar, R.ncta, err, budget);
-    }
-}
-
-// CTAs of the cooperative Lanczos launch that can be resident at once on `device` (0 when
-// the device has no cooperative launch)
-template <int N>
-int k_lanczos_persistent_capacity(int device, int kmax_all) {
-    static int cap[64][2] = {};  // per device: kmax the figure was taken for, CTAs
-    if (device < 0 || device >= 64) return 0;
-    if (cap[device][0] != kmax_all + 1) {
-        int coop = 0, sms = 0, per_sm = 0;
-        SDPG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
-        SDPG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        const size_t smem = (size_t)2 * (kmax_all + 2) * sizeof(mlf<N>);
-        SDPG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lz_persistent_kernel<N>, 256, smem));
-        cap[device][0] = kmax_all + 1;
-        cap[device][1] = coop ? per_sm * sms : 0;
-    }
-    return cap[device][1];
-}
-
-template <int N>
-int k_lanczos_persistent_ctas(int n) {
-    return std::max(1, std::min(64, ceil_div(n, 8)));
-}
-
-template <int N>
-void k_lanczos_persistent(LzLaunch<N> P, int kmax_all, cudaStream_t s) {
-    int total = 0;
-    for (int i = 0; i < P.nruns; ++i) total = std::max(total, P.run[i].cta0 + P.run[i].ncta);
-    const size_t smem = (size_t)2 * (kmax_all + 2) * sizeof(mlf<N>);
-    if (2 * (kmax_all + 2) > 2 * kMaxTri) throw sdpg_error(SDPG_ERR_TOO_LARGE, "Lanczos run too long");
-    void *args[] = {&P};
-    SDPG_KT_BEGIN(s);
-    SDPG_CUDA(cudaLaunchCooperativeKernel((void *)lz_persistent_kernel<N>, dim3(total), dim3(256), args, smem, s));
-    SDPG_CHECK_LAUNCH_KT("lz_persistent_kernel", s);
-}
-
 // The LP rule of Jal::getMinEigen (sdpa_jordan.cpp:79-85): min over k of
 // X[k][k] * L[k][k] * L[k][k] for a diagonal block (L its inverse Cholesky factor),
 // one CTA; out[0] = the minimum, out[1] = 0 (no Lanczos error term).
@@ -842,9 +638,6 @@ void k_tridiagonalize_small(int n, mlf<N> *A, mlf<N> *d, mlf<N> *e, cudaStream_t
     template void k_matvec<N>(int, const mlf<N> *, char, int, const mlf<N> *, mlf<N> *, cudaStream_t);   \
     template void k_tridiag_min<N>(int, const mlf<N> *, const mlf<N> *, mlf<N> *, int *, cudaStream_t,     \
                                    const int *);                                                          \
-    template void k_lanczos_persistent<N>(LzLaunch<N>, int, cudaStream_t);                                \
-    template int k_lanczos_persistent_capacity<N>(int, int);                                               \
-    template int k_lanczos_persistent_ctas<N>(int);                                                       \
     template void k_lanczos_step<N>(int, const mlf<N> *, mlf<N> *, mlf<N> *, mlf<N> *, mlf<N> *, mlf<N> *, \
                                     mlf<N> *, mlf<N> *, int *, int *, int, int, int, int, cudaStream_t);   \
     template void k_tridiagonalize_small<N>(int, mlf<N> *, mlf<N> *, mlf<N> *, cudaStream_t);              \

@@ -141,34 +141,6 @@ void k_tridiag_min(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *st
 template <int N>
 void k_lanczos_step(int n, const mlf<N> *M, mlf<N> *r, mlf<N> *q, mlf<N> *qold, mlf<N> *w, mlf<N> *td, mlf<N> *te,
                     mlf<N> *sl, int *ctl, int *status, int k, int eig, int kgo, int kmax, cudaStream_t s);
-
-// The whole Lanczos loop of several runs in one cooperative launch (eig.cu): each run
-// has its own CTAs (cta0 .. cta0 + ncta - 1), vectors, state slots and barrier words
-// (bar[0] arrivals, bar[1] generation: zero before the launch).
-constexpr int kLzMaxRuns = 4;
-template <int N>
-struct LzRunDev {
-    const mlf<N> *M;
-    mlf<N> *r, *q, *qold, *w, *td, *te, *sl, *partA, *partR;
-    int *ctl, *status;
-    unsigned *bar;
-    unsigned long long eig[2];  // steps 0 .. 127 with a tridiagonal eigenvalue solve
-    int n, kgo, kmax, k0, cta0, ncta;
-};
-template <int N>
-struct LzLaunch {
-    LzRunDev<N> run[kLzMaxRuns];
-    int nruns;
-    int *error;             // set when a barrier wait gave up
-    long long wait_cycles;  // budget of one barrier wait
-};
-template <int N>
-void k_lanczos_persistent(LzLaunch<N> P, int kmax_all, cudaStream_t s);
-template <int N>
-int k_lanczos_persistent_capacity(int device, int kmax_all);
-// CTAs for a run of size n (one output per warp, at most 64)
-template <int N>
-int k_lanczos_persistent_ctas(int n);
 // Householder tridiagonalisation of a dense symmetric n x n (n <= 64) in place; writes
 // d[0..n-1], e[0..n-2].  (Rsytrd 'L', the first stage of Rsyev.)
 template <int N>

@@ -13,23 +13,8 @@
 #include <utility>
 
 #include "solver.cuh"
-#include "tc_gemm.cuh"
-
-#include <atomic>
 
 namespace sdpg {
-
-namespace {
-std::atomic<int> g_device_shared[64];
-}
-
-void device_shared_enter(int device) {
-    if (device >= 0 && device < 64) g_device_shared[device].fetch_add(1);
-}
-void device_shared_leave(int device) {
-    if (device >= 0 && device < 64) g_device_shared[device].fetch_sub(1);
-}
-int device_shared(int device) { return (device >= 0 && device < 64) ? g_device_shared[device].load() : 0; }
 
 const char *phase_name(int phase) {
     switch (phase) {
@@ -63,8 +48,6 @@ class Solver final : public SolverBase {
         V *q[2], *qold[2], *r[2], *w[2], *tmp[2], *td[2], *te[2], *sl[2];
         V *Mop[2] = {nullptr, nullptr}, *Mtmp[2] = {nullptr, nullptr};  // L X L^T of a Lanczos run (n > 20)
         int *lzctl[2] = {nullptr, nullptr};  // device loop flags of a Lanczos run: [0] going on, [1] steps done
-        V *lzpart[2] = {nullptr, nullptr};       // per-CTA parts of alpha and r.r (one launch)
-        unsigned *lzbar[2] = {nullptr, nullptr}; // barrier words of the one-launch Lanczos run
         V *SW1 = nullptr, *SW2 = nullptr;  // Z-side work matrices of the small-block eigenvalue path
         BlockDev<N> cons;
         std::vector<int> f1_owners_h;
@@ -385,8 +368,6 @@ class Solver final : public SolverBase {
                 B.te[side] = dalloc(std::max(B.lanczos_kmax, n) + 2);
                 B.sl[side] = dalloc(16);
                 B.lzctl[side] = (int *)dalloc_raw(16);
-                B.lzpart[side] = dalloc(128);
-                B.lzbar[side] = (unsigned *)dalloc_raw(16);
             }
             if (B.lp) {
                 // no eigenvalue work space: the LP rule reads the diagonals
@@ -428,8 +409,6 @@ class Solver final : public SolverBase {
         SDPG_CUDA(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
         SDPG_CUDA(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
         pinned_ = (V *)pinned_acquire(kPinned * sizeof(V));
-        lz_err_h_ = reinterpret_cast<int *>(pinned_ + kPinned - 5);  // the slot below the policy's
-        lz_err_ = (int *)dalloc_raw(sizeof(int));
         info2_ = (int *)dalloc_raw(sizeof(int) * (4 * blk_.size() + 16));
         info_all_ = (int *)dalloc_raw(sizeof(int) * (4 * blk_.size() + 16));
         ev_.resize(2);
@@ -879,97 +858,18 @@ class Solver final : public SolverBase {
             t.active = t.n > 0 && kmax > 1;
         }
         // (the pinned slots are next written by stream-ordered copies, after the uploads)
-        if (lanczos_one_launch(T)) {
-            lanczos_persistent(T);
-        } else {
-            lanczos_stepwise(T);
-        }
+        lanczos_stepwise(T);
         for (Lz &t : T) {
             d2h_ += 11 * (long long)sizeof(V);
             SDPG_CUDA(cudaMemcpyAsync(t.hp, t.B->sl[t.side], 11 * sizeof(V), cudaMemcpyDeviceToHost, t.st));
         }
-        int lz_err = 0;
-        if (!T.empty()) {
-            d2h_ += (long long)sizeof(int);
-            SDPG_CUDA(cudaMemcpyAsync(lz_err_h_, lz_err_, sizeof(int), cudaMemcpyDeviceToHost, st_));
-        }
         SDPG_CUDA(cudaStreamSynchronize(st_));
         SDPG_CUDA(cudaStreamSynchronize(st2_));
-        if (!T.empty()) lz_err = *lz_err_h_;
-        if (lz_err) throw sdpg_error(SDPG_ERR_TIMEOUT, "Lanczos: a barrier wait of the one-launch loop gave up");
         for (Lz &t : T) {
             t.beta = R(t.hp[1]);
             t.min = R(t.hp[8]);
             t.error = R(t.hp[10]);
         }
-    }
-
-    // The one-launch Lanczos loop applies when every run fits its limits and all their
-    // CTAs can be resident together (SDPG_LANCZOS_STEPWISE=1 keeps the step-by-step
-    // launches, for comparison).
-    bool lanczos_one_launch(const std::vector<Lz> &T) {
-        static const bool stepwise = [] {
-            const char *e = getenv("SDPG_LANCZOS_STEPWISE");
-            return e && *e && *e != '0';
-        }();
-        // while a batch runs several solvers at once on this device, their kernels hold SMs
-        // the cooperative launch would wait for: the step-by-step launches then
-        if (stepwise || T.empty() || T.size() > (size_t)kLzMaxRuns || device_shared(dev_)) return false;
-        int ctas = 0, kmax_all = 0;
-        for (const Lz &t : T) {
-            if (!t.active || t.B->lanczos_kmax > 128) return false;
-            ctas += k_lanczos_persistent_ctas<N>(t.n);
-            kmax_all = std::max(kmax_all, t.B->lanczos_kmax);
-        }
-        return ctas <= k_lanczos_persistent_capacity<N>(dev_, kmax_all);
-    }
-
-    void lanczos_persistent(std::vector<Lz> &T) {
-        // the runs' set-up (operators, initial state) was enqueued on their own streams
-        SDPG_CUDA(cudaEventRecord(ev_join_, st2_));
-        SDPG_CUDA(cudaStreamWaitEvent(st_, ev_join_, 0));
-        LzLaunch<N> P{};
-        int cta = 0, kmax_all = 0;
-        for (size_t i = 0; i < T.size(); ++i) {
-            Lz &t = T[i];
-            Blk &B = *t.B;
-            const int s = t.side;
-            LzRunDev<N> &Rn = P.run[i];
-            Rn.M = B.Mop[s];
-            Rn.r = B.r[s];
-            Rn.q = B.q[s];
-            Rn.qold = B.qold[s];
-            Rn.w = B.w[s];
-            Rn.td = B.td[s];
-            Rn.te = B.te[s];
-            Rn.sl = B.sl[s];
-            Rn.partA = B.lzpart[s];
-            Rn.partR = B.lzpart[s] + 64;
-            Rn.ctl = B.lzctl[s];
-            Rn.status = status_;
-            Rn.bar = B.lzbar[s];
-            Rn.eig[0] = Rn.eig[1] = 0;
-            for (int k = 0; k < (int)t.eig.size() && k < 128; ++k)
-                if (t.eig[k]) Rn.eig[k >> 6] |= 1ull << (k & 63);
-            Rn.n = t.n;
-            Rn.kgo = t.kgo;
-            Rn.kmax = B.lanczos_kmax;
-            Rn.k0 = 0;
-            Rn.cta0 = cta;
-            Rn.ncta = k_lanczos_persistent_ctas<N>(t.n);
-            cta += Rn.ncta;
-            kmax_all = std::max(kmax_all, B.lanczos_kmax);
-            SDPG_CUDA(cudaMemsetAsync(B.lzbar[s], 0, 2 * sizeof(unsigned), st_));
-        }
-        P.nruns = (int)T.size();
-        P.error = lz_err_;
-        // about one second per barrier wait; the tensor-core test hook shortens it too
-        P.wait_cycles = g_tc_wait_cycles > 0 ? g_tc_wait_cycles : (1ll << 31);
-        SDPG_CUDA(cudaMemsetAsync(lz_err_, 0, sizeof(int), st_));
-        k_lanczos_persistent<N>(P, kmax_all, st_);
-        // the Z-side results are read on the second stream
-        SDPG_CUDA(cudaEventRecord(ev_fork_, st_));
-        SDPG_CUDA(cudaStreamWaitEvent(st2_, ev_fork_, 0));
     }
 
     // step-by-step launches: the host enqueues a few steps ahead and reads the loop flags
@@ -1904,8 +1804,6 @@ class Solver final : public SolverBase {
     V *BLinv_ = nullptr, *BLinvT_ = nullptr, *Dytmp_ = nullptr;  // inverse of the Schur factor and its transpose
     V *b_ = nullptr, *y_ = nullptr, *Dy_ = nullptr, *g_ = nullptr, *p_ = nullptr, *B_ = nullptr, *slot_ = nullptr;
     int *info_ = nullptr, *status_ = nullptr;
-    int *lz_err_ = nullptr;    // device: a barrier wait of the one-launch Lanczos loop gave up
-    int *lz_err_h_ = nullptr;  // its host copy (a pinned slot)
     R muInit_, muCur_, thP_, thD_, aP_, aD_, betaV_, rho_, etaP_, etaD_, objP_, objD_, normP_, normD_;
     R initNormP_, initNormD_;
     int phase_ = noINFO, final_phase_ = noINFO, reductionOn_ = 1, iter_ = 0;

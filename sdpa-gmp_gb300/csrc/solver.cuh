@@ -109,11 +109,4 @@ class SolverBase {
 // Build a solver for the SDP blocks of P at the precision in `param`.
 SolverBase *make_solver(const RawProblem &P, const Param &param, int device, cudaStream_t stream);
 
-// Marks a device as shared by several solvers running at once (the batched solve): the
-// solvers on it then run their Lanczos loops as step-by-step launches instead of one
-// cooperative launch, which would wait for SMs the others hold.
-void device_shared_enter(int device);
-void device_shared_leave(int device);
-int device_shared(int device);
-
 }  // namespace sdpg
