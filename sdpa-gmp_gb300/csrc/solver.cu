@@ -491,6 +491,7 @@ class Solver final : public SolverBase {
     GraphSlot g_schur_chol_, g_schur_inv_;
     bool capturing_ = false;  // GEMMs issued into a graph are not bracketed by profiling events
     std::vector<GraphSlot> g_invchol_;  // per block: X (main stream), then Z (second stream)
+    std::vector<GraphSlot> g_lanczos_;  // per block and side: every Lanczos step of a run
 
     // ---------------------------------------------------------------- memory helpers
 
@@ -858,7 +859,7 @@ class Solver final : public SolverBase {
             t.active = t.n > 0 && kmax > 1;
         }
         // (the pinned slots are next written by stream-ordered copies, after the uploads)
-        lanczos_stepwise(T);
+        lanczos_graphed(T);
         for (Lz &t : T) {
             d2h_ += 11 * (long long)sizeof(V);
             SDPG_CUDA(cudaMemcpyAsync(t.hp, t.B->sl[t.side], 11 * sizeof(V), cudaMemcpyDeviceToHost, t.st));
@@ -869,6 +870,24 @@ class Solver final : public SolverBase {
             t.beta = R(t.hp[1]);
             t.min = R(t.hp[8]);
             t.error = R(t.hp[10]);
+        }
+    }
+
+    // Every step a run can take, enqueued at once as one CUDA graph per (block, side)
+    // (captured on the second call, replayed after): the steps past the loop's end return
+    // at once on the device flag, and the host waits only for the final result.
+    void lanczos_graphed(std::vector<Lz> &T) {
+        if (g_lanczos_.size() != 2 * blk_.size()) g_lanczos_.resize(2 * blk_.size());
+        for (Lz &t : T) {
+            if (!t.active) continue;
+            Blk &B = *t.B;
+            const int s = t.side;
+            const size_t slot = 2 * (size_t)(t.B - blk_.data()) + (size_t)s;
+            graphed(g_lanczos_[slot], t.st, [&] {
+                for (int k = 0; k < t.n && k + 1 < B.lanczos_kmax; ++k)
+                    k_lanczos_step<N>(t.n, B.Mop[s], B.r[s], B.q[s], B.qold[s], B.w[s], B.td[s], B.te[s], B.sl[s],
+                                      B.lzctl[s], status_, k, t.eig[k], t.kgo, B.lanczos_kmax, t.st);
+            });
         }
     }
 
