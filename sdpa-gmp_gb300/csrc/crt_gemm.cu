@@ -150,30 +150,41 @@ struct ResSrc {
     long long qrow, qplane, qbatch;
 };
 
+// The largest exponent of each row's nonzero entries; kExpSplit warps share a row (each
+// a strided quarter of it) so that enough loads are in flight for short operands.
+constexpr int kExpSplit = 4;
+
 template <int N>
-__global__ void crt_exp_kernel(CrtOperands<N> ops, int K) {
+__global__ void __launch_bounds__(32 * kExpWarps) crt_exp_kernel(CrtOperands<N> ops, int K) {
+    __shared__ int part[kExpWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int z = blockIdx.y;
     const int op = z < ops.cnt[0] ? 0 : 1;
     const int b = op ? z - ops.cnt[0] : z;
-    const int o = blockIdx.x * kExpWarps + warp;
+    const int o = blockIdx.x * (kExpWarps / kExpSplit) + warp / kExpSplit;
+    const int sub = warp % kExpSplit;
     // the operand's fields are selected, not indexed by a run-time value (which would
     // put the parameter arrays in local memory)
     const int Opad = op ? ops.Opad[1] : ops.Opad[0], O = op ? ops.O[1] : ops.O[0];
-    if (o >= Opad) return;
     const Operand<N> X = op ? ops.X[1] : ops.X[0];
     int *E = op ? ops.E[1] : ops.E[0];
     int emax = INT_MIN;
     if (o < O) {
         const mlf<N> *base = X.X + b * X.sb + o * X.so;
-        for (int k = lane; k < K; k += 32) {
+        for (int k = sub * 32 + lane; k < K; k += 32 * kExpSplit) {
             const mlf<N> *v = base + k * X.sk;
             if (v->m[N - 1] != 0) emax = max(emax, v->e);
         }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, off));
-    if (lane == 0) E[(long long)b * Opad + o] = (emax == INT_MIN) ? 0 : emax;
+    if (lane == 0) part[warp] = emax;
+    __syncthreads();
+    if (sub == 0 && lane == 0 && o < Opad) {
+#pragma unroll
+        for (int q = 1; q < kExpSplit; ++q) emax = max(emax, part[warp + q]);
+        E[(long long)b * Opad + o] = (emax == INT_MIN) ? 0 : emax;
+    }
 }
 
 // Entry (o, k) of op(X) as the integer trunc(|x| 2^(R - E)) (below 2^R, R = 276) in ten
@@ -403,21 +414,36 @@ __global__ void __launch_bounds__(128)
     const int bl = blockIdx.y;
     const bool ok0 = live && j < p.Nn && !(p.lower_only && i < j);
     const bool ok1 = live && j + 1 < p.Nn && !(p.lower_only && i < j + 1);
+    // the table floor(2^320 c_l / m_l) in shared memory: lanes of a group read different rows
+    __shared__ uint32_t inv_s[kCrtL * kCrtInvWords];
+    for (int q = threadIdx.x; q < kCrtL * kCrtInvWords; q += blockDim.x) inv_s[q] = c_inv[q / kCrtInvWords][q % kCrtInvWords];
+    __syncthreads();
     unsigned long long a0[kCrtInvWords], a1[kCrtInvWords];
 #pragma unroll
     for (int w = 0; w < kCrtInvWords; ++w) a0[w] = a1[w] = 0;
     if (ok0 || ok1) {
         const uint32_t *y = reinterpret_cast<const uint32_t *>(Y + ((long long)bl * kCrtL * Mpad + i) * Npad + j);
         const long long plane = (long long)Mpad * Npad / 2;  // in pairs
-#pragma unroll 3
-        for (int l = g; l < kCrtL; l += kRecLanes) {
-            const uint32_t yy = __ldg(y + l * plane);
-            const uint32_t y0 = yy & 0xFFFFu, y1 = yy >> 16;
+        // ten residue loads in flight per thread before they are used
+        constexpr int kLoads = 10;
+        for (int l0 = g; l0 < kCrtL; l0 += kLoads * kRecLanes) {
+            uint32_t yy[kLoads];
 #pragma unroll
-            for (int w = 0; w < kCrtInvWords; ++w) {
-                const uint32_t c = c_inv[l][w];
-                a0[w] += (unsigned long long)y0 * c;
-                a1[w] += (unsigned long long)y1 * c;
+            for (int q = 0; q < kLoads; ++q) {
+                const int l = l0 + q * kRecLanes;
+                yy[q] = l < kCrtL ? __ldg(y + l * plane) : 0u;
+            }
+#pragma unroll
+            for (int q = 0; q < kLoads; ++q) {
+                const int l = l0 + q * kRecLanes;
+                if (l >= kCrtL) break;
+                const uint32_t y0 = yy[q] & 0xFFFFu, y1 = yy[q] >> 16;
+#pragma unroll
+                for (int w = 0; w < kCrtInvWords; ++w) {
+                    const uint32_t c = inv_s[l * kCrtInvWords + w];
+                    a0[w] += (unsigned long long)y0 * c;
+                    a1[w] += (unsigned long long)y1 * c;
+                }
             }
         }
     }
@@ -575,8 +601,8 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
             const double rows = (double)ops.cnt[0] * p.M + (double)ops.cnt[1] * p.Nn;
             if (ops.cnt[0] + ops.cnt[1] > 0) {
                 SDPG_KT_BEGIN(s);
-                crt_exp_kernel<N><<<dim3(ceil_div(opad, kExpWarps), ops.cnt[0] + ops.cnt[1]), 32 * kExpWarps, 0, s>>>(
-                    ops, p.K);
+                crt_exp_kernel<N><<<dim3(ceil_div(opad, kExpWarps / kExpSplit), ops.cnt[0] + ops.cnt[1]),
+                                     32 * kExpWarps, 0, s>>>(ops, p.K);
                 SDPG_CHECK_LAUNCH_KTW("crt_exp_kernel", s, entries * sizeof(mlf<N>) + rows * 4);
                 ResSrc<N> rs[2];
                 for (int q = 0; q < 2; ++q) {
