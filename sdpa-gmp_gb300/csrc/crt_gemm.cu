@@ -12,7 +12,8 @@
 //      y_l = S mod m_l.
 //   4. Reconstruction: the exact sum V = sum_k X_ik X_kj satisfies
 //      V / M = sum_l y_l c_l / m_l (mod 1), c_l = (M / m_l)^-1 mod m_l, with
-//      |V / M| < 2^-6, so V / M is the centred fractional part of that sum, formed in
+//      |V / M| < K 2^(2R) / M < 1/4 (K <= 2^14, M >= 2^568), so V / M is the centred
+//      fractional part of that sum, formed in
 //      320-bit fixed point from the table floor(2^320 c_l / m_l); then
 //      C = alpha V 2^(EA_i + EB_j - 2R) + beta C.
 //
@@ -533,8 +534,10 @@ void residue_launch(const ResSrc<N> &s0, const ResSrc<N> &s1, const CrtDevice &d
 
 }  // namespace
 
-// Longest sum the moduli cover: K 2^(2R) = 2^566 keeps |V / M| below 1/4.
+// Longest sum the moduli cover: K 2^(2R) = 2^566 keeps |V / M| below 1/4 (M, the product
+// of the moduli, lies in [2^(kCrtMtotExp - 1), 2^kCrtMtotExp)).
 constexpr int kCrtMaxK = 1 << 14;
+static_assert(14 + 2 * kCrtR <= (kCrtMtotExp - 1) - 2, "K 2^(2R) / M must stay below 1/4 for K <= kCrtMaxK");
 
 // 0: tensor-core residue path where it applies and the product is not tiny;
 // 1: digit GEMM only; 2: residue path for every 256-bit product with K <= 1024

@@ -329,16 +329,20 @@ template <int N>
 void k_dot_batched(long long n, const mlf<N> *x, const long long *xoff, const mlf<N> *y, const long long *yoff,
                    int batch, mlf<N> *out, Workspace &ws, cudaStream_t s) {
     if (batch <= 0) return;
-    int G = (int)((n + kThreads * 8 - 1) / (kThreads * 8));
+    // a single dot: about two products per thread (short multiply-add chains: these dots
+    // are latency-bound), at most 1024 partial sums; batched dots keep eight products per
+    // thread and at most 64 partials each (the workspace their callers reserve)
+    const int per = batch == 1 ? 2 : 8, gmax = batch == 1 ? 1024 : 64;
+    int G = (int)((n + kThreads * per - 1) / (kThreads * per));
     if (G < 1) G = 1;
-    if (G > 64) G = 64;
+    if (G > gmax) G = gmax;
     mlf<N> *partial = (mlf<N> *)ws.carve((size_t)G * batch * sizeof(mlf<N>));
     dim3 g(G, batch);
     SDPG_KT_BEGIN(s);
     dot_partial_kernel<N><<<g, kThreads, 0, s>>>(n, x, xoff, y, yoff, partial);
     SDPG_CHECK_LAUNCH_KT("dot_partial_kernel", s);
     SDPG_KT_BEGIN(s);
-    sum_partials_kernel<N><<<batch, 64, 0, s>>>(G, partial, out);
+    sum_partials_kernel<N><<<batch, kThreads, 0, s>>>(G, partial, out);
     SDPG_CHECK_LAUNCH_KT("sum_partials_kernel", s);
 }
 

@@ -5,8 +5,8 @@ allocation's device synchronisation is not acceptable in their loop).
 The entry point works out of one fixed device array instead of allocating; this
 test calls it through the C ABI twice in a row (different precisions and shapes,
 so the second call reuses the array the first call left dirty) and compares each
-result with the allocating entry point sdpg_rgemm_device on the same inputs, to
-the tolerance the GEMM tests use: 2^-(p-16) of |alpha| K max|a_i.| max|b_.j|
+result with the exact product and with the allocating entry point
+sdpg_rgemm_device on the same inputs, to the tolerance the GEMM tests use: 2^-(p-16) of |alpha| K max|a_i.| max|b_.j|
 + |beta c_ij| per entry (p = 32 * limbs).  It also checks that a product larger
 than the fixed scratch is refused with SDPG_ERR_TOO_LARGE.  The file is named so
 that pytest collects it last."""
@@ -57,9 +57,12 @@ def test_noalloc_gemm_matches_allocating_gemm(sdpg, exact):
         torch.cuda.synchronize()
         got_ref = dC_ref.cpu().numpy().view(np.uint32)
         got_new = dC_new.cpu().numpy().view(np.uint32)
-        _, scale = exact.gemm(ta, tb, m, n, k, exact.ml_decode(alpha)[0], exact.ml_decode(A), lda,
-                              exact.ml_decode(B), ldb, exact.ml_decode(beta)[0], exact.ml_decode(C), ldc)
+        ref, scale = exact.gemm(ta, tb, m, n, k, exact.ml_decode(alpha)[0], exact.ml_decode(A), lda,
+                                exact.ml_decode(B), ldb, exact.ml_decode(beta)[0], exact.ml_decode(C), ldc)
         rows = [i + j * ldc for j in range(n) for i in range(m)]
+        # against the exact product, then against the allocating entry point
+        err_exact = exact.max_rel_err(got_new[rows], [ref[r] for r in rows], [scale[r] for r in rows])
+        assert err_exact <= 2.0 ** -(32 * limbs - 16), (call, err_exact)
         err = exact.max_rel_err(got_new[rows], exact.ml_decode(got_ref[rows]), [scale[r] for r in rows])
         assert err <= 2.0 ** -(32 * limbs - 16), (call, err)
         pad = [m + j * ldc for j in range(n)]
