@@ -61,11 +61,44 @@ static_assert(kResSmem <= kResSmemLaunch, "residue kernel shared memory");
 static_assert(kCrtL <= kResN && kResChunks * 8 >= kCrtR && kResChunks <= kResK, "residue GEMM shape");
 static_assert((long long)kResChunks * 255 * 508 < (1 << 23), "residue sums must stay exact in fp32");
 
+// Reconstruction on the tensor cores: with F_l = floor(2^320 c_l / m_l) written as 40 bytes
+// f_lp, sum_l y_l F_l = sum_p 2^(8p) S_p where S_p = sum_l y_l f_lp: one fp16 product
+// [128 outputs x 128 moduli (70 used)] x [128 x 48 bytes (40 used)] per tile with fp32
+// accumulation, exact (every partial sum is an integer below 70 * 508 * 255 < 2^24).  The
+// same integer as summing y_l F_l word by word, so the result is bit-identical.
+constexpr int kRecBytes = 4 * kCrtInvWords;  // 40
+constexpr int kRecN = 48;                    // GEMM N: the bytes, zero-padded to a multiple of 16
+constexpr int kRecM = 128;                   // outputs per tile (tcgen05 M)
+constexpr int kRecAtomA = kRecM * 128;       // one 64-modulus K atom of A: 16 KB
+constexpr int kRecAtomB = kRecN * 128;       // one 64-modulus K atom of B: 6 KB
+constexpr int kRecSmem = 2 * kRecAtomA + 2 * kRecAtomB + 1024 + 64;
+// at most four CTAs per SM (tensor memory: 64 columns each would allow eight)
+constexpr int kRecSmemLaunch = 52 * 1024;
+static_assert(kRecSmem <= kRecSmemLaunch, "reconstruction kernel shared memory");
+static_assert((long long)kCrtL * 508 * 255 < (1 << 24), "reconstruction sums must stay exact in fp32");
+static_assert(kCrtL <= 128 && kRecBytes <= kRecN, "reconstruction GEMM shape");
+
 struct CrtDevice {
     int *moduli = nullptr, *error = nullptr;
+    const uint4 *rec_table = nullptr;  // f_lp as fp16: two [kRecN][64] K-major swizzled atoms (moduli 0-63, 64-127)
     const uint4 *res_table = nullptr;  // t_lc as fp16, [kResN][kResK] in the 128-byte-swizzled K-major layout
     int sms = 0;
 };
+
+// The bytes f_lp of F_l laid out as the tcgen05 B operand: atom l / 64, row p (byte), 64
+// K-elements (moduli) of 2 bytes, the 16-byte chunk j of row p stored at chunk j ^ (p mod 8).
+std::vector<uint16_t> reconstruct_table_host() {
+    std::vector<uint16_t> t((size_t)2 * kRecN * 64, 0);
+    for (int l = 0; l < kCrtL; ++l) {
+        const int atom = l / 64, lk = l % 64;
+        for (int pb = 0; pb < kRecBytes; ++pb) {
+            const uint32_t byte = (kCrtInv[l][pb / 4] >> (8 * (pb % 4))) & 0xFFu;
+            t[(size_t)atom * kRecN * 64 + (size_t)pb * 64 + (((lk / 8) ^ (pb & 7)) * 8) + lk % 8] =
+                __half_as_ushort(__float2half((float)byte));  // byte < 256: exact
+        }
+    }
+    return t;
+}
 
 // The table t_lc = 2^(8c) mod m_l laid out as the tcgen05 B operand: row l (modulus),
 // 64 K-elements of 2 bytes, the 16-byte chunk j of row l stored at chunk j ^ (l mod 8).
@@ -115,6 +148,11 @@ CrtDevice crt_device() {
         SDPG_CUDA(cudaMalloc(&dt, tab.size() * sizeof(uint16_t)));
         SDPG_CUDA(cudaMemcpy(dt, tab.data(), tab.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
         c.res_table = (const uint4 *)dt;
+        const std::vector<uint16_t> rtab = reconstruct_table_host();
+        void *drt = nullptr;
+        SDPG_CUDA(cudaMalloc(&drt, rtab.size() * sizeof(uint16_t)));
+        SDPG_CUDA(cudaMemcpy(drt, rtab.data(), rtab.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+        c.rec_table = (const uint4 *)drt;
         cache[dev] = c;
         ready[dev] = true;
     }
@@ -467,8 +505,146 @@ __global__ void __launch_bounds__(128)
     }
 }
 
+// The reconstruction on the tensor cores.  A CTA takes tiles of 128 consecutive outputs
+// (e = i Nn + j, row-major, thread t one output): each thread gathers its 70 residues
+// (coalesced along j for every modulus) as one row of a 128 x 128 fp16 tile (two
+// 64-modulus swizzle atoms), one thread issues the five K = 16 products with the byte
+// table (48 x 128, loaded once per CTA), and each thread forms its output's 320-bit
+// fixed-point sum from the 40 exact byte sums and finishes it (crt_finish).  The product
+// wait is bounded: on time-out the CTA records error 5 and stops.
+template <int N>
+__global__ void __launch_bounds__(kRecM) tc_reconstruct_kernel(const uint16_t *Y, int Mpad, int Npad, const int *EA,
+                                                               const int *EB, long long sEA, long long sEB, int b0,
+                                                               int alpha_one, GemmProblem<N> p,
+                                                               const uint4 *__restrict__ table, int *error,
+                                                               int *sticky) {
+    using namespace tc;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *tA = smem;                   // two atoms of 128 rows x 128 bytes
+    uint8_t *tB = smem + 2 * kRecAtomA;   // two atoms of 48 rows x 128 bytes
+    uint64_t *bar = (uint64_t *)(tB + 2 * kRecAtomB);
+    uint32_t *tmem_slot = (uint32_t *)(bar + 1);
+    __shared__ int abort_flag;
+    const int t = threadIdx.x, warp = t >> 5;
+    const int bl = blockIdx.y;
+    const long long outputs = (long long)p.M * p.Nn;
+    const int ntiles = (int)((outputs + kRecM - 1) / kRecM);
+    if ((int)blockIdx.x >= ntiles) return;  // the whole CTA
+    for (int q = t; q < 2 * kRecAtomB / 16; q += kRecM) reinterpret_cast<uint4 *>(tB)[q] = table[q];
+    // moduli 70 .. 127 of every row stay zero: clear the second atom once
+    for (int q = t; q < kRecAtomA / 16; q += kRecM) reinterpret_cast<uint4 *>(tA + kRecAtomA)[q] = make_uint4(0, 0, 0, 0);
+    if (t == 0) {
+        abort_flag = 0;
+        mbar_init(smem_u32(bar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        tmem_alloc(smem_u32(tmem_slot), 64);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const long long plane = (long long)Mpad * Npad;
+    const uint16_t *ybase = Y + (long long)bl * kCrtL * plane;
+    const int bg = b0 + bl;
+    uint32_t phase = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, phase ^= 1u) {
+        const long long e = (long long)tile * kRecM + t;
+        const bool live = e < outputs;
+        const int i = live ? (int)(e / p.Nn) : 0;
+        const int j = live ? (int)(e - (long long)i * p.Nn) : 0;
+        // the output's residues as the row t of the A tile (K element l at atom l / 64)
+        const uint16_t *y = ybase + (long long)i * Npad + j;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {  // 16-byte chunks: moduli 8c .. 8c + 7 (chunk 8 is atom 1's first)
+            uint32_t h[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int l0 = 8 * c + 2 * q, l1 = l0 + 1;
+                const uint32_t v0 = (live && l0 < kCrtL) ? (uint32_t)__ldg(y + l0 * plane) : 0u;
+                const uint32_t v1 = (live && l1 < kCrtL) ? (uint32_t)__ldg(y + l1 * plane) : 0u;
+                const __half2 x = __halves2half2(__ushort2half_rn((unsigned short)v0), __ushort2half_rn((unsigned short)v1));
+                h[q] = *reinterpret_cast<const uint32_t *>(&x);
+            }
+            uint8_t *row = tA + (c >> 3) * kRecAtomA + t * 128;
+            const int cj = c & 7;
+            *reinterpret_cast<uint4 *>(row + ((cj ^ (t & 7)) * 16)) = make_uint4(h[0], h[1], h[2], h[3]);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (t == 0) {
+            constexpr uint32_t idesc = idesc_f16_f32(kRecM, kRecN);
+            const uint64_t a0 = sw128_kmajor_desc(smem_u32(tA)), b0d = sw128_kmajor_desc(smem_u32(tB));
+            const uint64_t a1 = sw128_kmajor_desc(smem_u32(tA + kRecAtomA)),
+                           b1d = sw128_kmajor_desc(smem_u32(tB + kRecAtomB));
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+                tc_mma(tmem, a0 + (uint64_t)(2 * kk), b0d + (uint64_t)(2 * kk), idesc, kk > 0 ? 1u : 0u);
+            tc_mma(tmem, a1, b1d, idesc, 1u);  // moduli 64 .. 79 (70 .. 79 zero)
+            tc_commit(smem_u32(bar));
+        }
+        __syncwarp();
+        // the products above are issued: a drain-type wait with the full budget
+        if (!mbar_wait(smem_u32(bar), phase)) {
+            atomicExch(error, 5);
+            if (sticky && sticky != error) atomicExch(sticky, 5);
+            abort_flag = 1;
+        }
+        __syncthreads();
+        if (abort_flag) break;
+        tc_fence_after();
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        uint32_t v[32], w8[8];
+        tmem_ld32(lane_addr, v);
+        tmem_ld8(lane_addr + 32, w8);
+        tmem_ld_wait();
+        unsigned long long acc[kCrtInvWords];
+#pragma unroll
+        for (int w = 0; w < kCrtInvWords; ++w) {
+            unsigned long long a = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int pb = 4 * w + q;
+                const uint32_t bits = pb < 32 ? v[pb] : w8[pb - 32];
+                a += (unsigned long long)__float2uint_rn(__uint_as_float(bits)) << (8 * q);
+            }
+            acc[w] = a;
+        }
+        if (live && !(p.lower_only && i < j)) {
+            const int escale = EA[bl * sEA + i] - 2 * kCrtR + EB[bl * sEB + j];
+            crt_finish<N>(acc, escale, alpha_one, p, p.C + bg * p.sc + i + (long long)j * p.ldc);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 64);
+    }
+}
+
 // the reconstruction with the fewest lanes per output pair that still puts about
 // 80k threads in flight
+template <int N>
+void reconstruct_launch_tc(const uint16_t *Y, int Mpad, int Npad, const int *EA, const int *EB, long long sEA,
+                           long long sEB, int b0, int alpha_one, const GemmProblem<N> &p, int batch,
+                           const CrtDevice &dev, int *error, cudaStream_t s) {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        SDPG_CUDA(cudaFuncSetAttribute(tc_reconstruct_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kRecSmemLaunch));
+    });
+    const long long tiles = ((long long)p.M * p.Nn + kRecM - 1) / kRecM;
+    const int grid_x = (int)std::min<long long>(tiles, std::max<long long>(1, 4LL * dev.sms / std::max(1, batch) + 1));
+    tc_reconstruct_kernel<N><<<dim3(grid_x, batch), kRecM, kRecSmemLaunch, s>>>(
+        Y, Mpad, Npad, EA, EB, sEA, sEB, b0, alpha_one, p, dev.rec_table, error ? error : dev.error, dev.error);
+}
+
 template <int N>
 void reconstruct_launch(const uint16_t *Y, int Mpad, int Npad, const int *EA, const int *EB, long long sEA,
                         long long sEB, int b0, int alpha_one, const GemmProblem<N> &p, int batch, cudaStream_t s) {
@@ -657,7 +833,8 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
             }
             if (p.ev_after) SDPG_CUDA(cudaEventRecord(p.ev_after, s));
             SDPG_KT_BEGIN(s);
-            reconstruct_launch<N>(Y, L.Mpad, L.Npad, EA, EB, ab ? L.Mpad : 0, bb ? L.Npad : 0, b0, alpha_one, p, G, s);
+            reconstruct_launch_tc<N>(Y, L.Mpad, L.Npad, EA, EB, ab ? L.Mpad : 0, bb ? L.Npad : 0, b0, alpha_one, p, G,
+                                     dev, p.error, s);
             // every output: its kCrtL residues read, the result written, C read when beta != 0
             SDPG_CHECK_LAUNCH_KTW("crt_reconstruct_kernel", s,
                                   (double)G * p.M * p.Nn * (p.lower_only ? 0.5 : 1.0) *
@@ -799,7 +976,7 @@ void crt_cache_panel(const CrtCache &c, int k0, int kb, mlf<N> *A, long long lda
         p.beta = ml_one<N>();
         p.lower_only = 1;
         SDPG_KT_BEGIN(s);
-        reconstruct_launch<N>(c.Y, t.Mpad, t.Npad, c.E + k0, c.E + k0, 0, 0, 0, 0, p, 1, s);
+        reconstruct_launch_tc<N>(c.Y, t.Mpad, t.Npad, c.E + k0, c.E + k0, 0, 0, 0, 0, p, 1, dev, error, s);
         SDPG_CHECK_LAUNCH_KTW("crt_reconstruct_kernel", s,
                               (double)M * kb * (2.0 * kCrtL + 2.0 * sizeof(mlf<N>)));
     }
