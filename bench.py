@@ -44,14 +44,14 @@ RESIDUE_MODULI = 70  # primes of the 256-bit residue GEMM (csrc/crt_tables.h)
 # DRAM bytes (read + write) per algorithmic byte (or per launch for the tensor kernel),
 # from the ncu captures of a 500^3 product summarised in
 # profiles/residue_gemm_gemm500_256bit.md: tc_residue_kernel 20.1 + 16.2 MB against
-# 20.0 + 70.0 MB algorithmic; crt_reconstruct_kernel 35.9 MB against 45.0 MB;
+# 20.0 + 70.0 MB algorithmic; tc_reconstruct_kernel 35.9 MB against 45.0 MB;
 # crt_exp_kernel 20.0 MB against 20.0 MB; tc_modgemm_kernel 80.2 MB per launch.
 TC_TRAFFIC_BYTES = 80.2e6
-TRAFFIC_PER_ALG_BYTE = {"tc_residue_kernel": 36.3 / 90.0, "crt_reconstruct_kernel": 35.9 / 45.0,
+TRAFFIC_PER_ALG_BYTE = {"tc_residue_kernel": 36.3 / 90.0, "tc_reconstruct_kernel": 35.9 / 45.0,
                         "crt_exp_kernel": 20.0 / 20.0}
 # Kernel families with an algorithmic-work figure (sdpg_kernel_times' work column):
 # roofline bound and the unit of that work.
-FAMILY_BOUND = {"tc_residue_kernel": "hbm", "crt_exp_kernel": "hbm", "crt_reconstruct_kernel": "hbm",
+FAMILY_BOUND = {"tc_residue_kernel": "hbm", "crt_exp_kernel": "hbm", "tc_reconstruct_kernel": "hbm",
                 "lz_matvec_kernel": "hbm", "tc_modgemm_kernel": "tensor"}
 
 

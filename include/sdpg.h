@@ -277,7 +277,7 @@ int sdpg_tensor_error(int device, int *flag);
  * "name launches milliseconds work", sorted by name, into buf, forgets the records and
  * returns the number of lines (SDPG_ERR_TOO_LARGE if cap is too small).  `work` is the
  * launches' summed algorithmic work where the library states one: for
- * tc_residue_kernel, crt_exp_kernel, crt_reconstruct_kernel and lz_matvec_kernel the
+ * tc_residue_kernel, crt_exp_kernel, tc_reconstruct_kernel and lz_matvec_kernel the
  * bytes the kernel must move (multi-limb entries read, residue planes written, ...), for
  * tc_modgemm_kernel the fp16 tensor flops 2 M N K per residue GEMM; 0 elsewhere. */
 int sdpg_kernel_timing(int enable);

@@ -13,9 +13,9 @@
 //   4. Reconstruction: the exact sum V = sum_k X_ik X_kj satisfies
 //      V / M = sum_l y_l c_l / m_l (mod 1), c_l = (M / m_l)^-1 mod m_l, with
 //      |V / M| < K 2^(2R) / M < 1/4 (K <= 2^14, M >= 2^568), so V / M is the centred
-//      fractional part of that sum, formed in
-//      320-bit fixed point from the table floor(2^320 c_l / m_l); then
-//      C = alpha V 2^(EA_i + EB_j - 2R) + beta C.
+//      fractional part of that sum, formed in 320-bit fixed point from the table
+//      floor(2^320 c_l / m_l) -- on the tensor cores as well, the table's 40 bytes per
+//      modulus times the residues -- then C = alpha V 2^(EA_i + EB_j - 2R) + beta C.
 //
 // The only rounding is the truncation of the inputs to R bits (relative 2^-276 of
 // the row / column maximum) and the final conversion to 256 bits, so the error obeys
@@ -396,9 +396,9 @@ __global__ void __launch_bounds__(kResM) tc_residue_kernel(ResSrc<N> s0, ResSrc<
     }
 }
 
-// V / M as the centred fractional part of sum_l y_l c_l / m_l (320-bit fixed point), then
-// C = alpha V 2^(EA + EB - 2R) + beta C.  A group of lanes takes two neighbouring outputs
-// along j and reads both residues of a plane with one 32-bit load.
+// V / M as the centred fractional part of sum_l y_l c_l / m_l (320-bit fixed point, the
+// word sums acc[w] = sum_l y_l floor(2^320 c_l / m_l)[w]), then C = alpha V 2^(EA + EB - 2R)
+// + beta C.
 template <int N>
 __device__ __forceinline__ void crt_finish(const unsigned long long (&acc)[kCrtInvWords], int escale, int alpha_one,
                                            const GemmProblem<N> &p, mlf<N> *cp) {
@@ -431,78 +431,6 @@ __device__ __forceinline__ void crt_finish(const unsigned long long (&acc)[kCrtI
     if (!alpha_one) v = ml_mul(v, p.alpha);
     if (!ml_is_zero(p.beta)) v = ml_add(v, ml_mul(p.beta, *cp));
     *cp = v;
-}
-
-// G lanes share one output pair: lane g sums the moduli l = g, g + G, ...; the 64-bit
-// word sums are combined across the G lanes with shuffles and lanes 0 and 1 of the group
-// finish the pair's two outputs.  Small products (the narrow panels of the
-// factorisations) thus still spread over many SMs; large ones take G = 1.
-template <int N, int kRecLanes>
-__global__ void __launch_bounds__(128)
-    crt_reconstruct_kernel(const uint16_t *Y, int Mpad, int Npad, const int *EA, const int *EB, long long sEA,
-                           long long sEB, int b0, int alpha_one, GemmProblem<N> p) {
-    // outputs taken as (row, column pair) in row-major order, so narrow products
-    // still fill whole warps
-    const int npairs = (p.Nn + 1) >> 1;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long pair = t / kRecLanes;
-    const int g = (int)(t % kRecLanes);
-    const bool live = pair < (long long)p.M * npairs;
-    const int i = live ? (int)(pair / npairs) : 0;
-    const int j = live ? 2 * (int)(pair - (long long)i * npairs) : 0;
-    const int bl = blockIdx.y;
-    const bool ok0 = live && j < p.Nn && !(p.lower_only && i < j);
-    const bool ok1 = live && j + 1 < p.Nn && !(p.lower_only && i < j + 1);
-    // the table floor(2^320 c_l / m_l) in shared memory: lanes of a group read different rows
-    __shared__ uint32_t inv_s[kCrtL * kCrtInvWords];
-    for (int q = threadIdx.x; q < kCrtL * kCrtInvWords; q += blockDim.x) inv_s[q] = c_inv[q / kCrtInvWords][q % kCrtInvWords];
-    __syncthreads();
-    unsigned long long a0[kCrtInvWords], a1[kCrtInvWords];
-#pragma unroll
-    for (int w = 0; w < kCrtInvWords; ++w) a0[w] = a1[w] = 0;
-    if (ok0 || ok1) {
-        const uint32_t *y = reinterpret_cast<const uint32_t *>(Y + ((long long)bl * kCrtL * Mpad + i) * Npad + j);
-        const long long plane = (long long)Mpad * Npad / 2;  // in pairs
-        // ten residue loads in flight per thread before they are used
-        constexpr int kLoads = 10;
-        for (int l0 = g; l0 < kCrtL; l0 += kLoads * kRecLanes) {
-            uint32_t yy[kLoads];
-#pragma unroll
-            for (int q = 0; q < kLoads; ++q) {
-                const int l = l0 + q * kRecLanes;
-                yy[q] = l < kCrtL ? __ldg(y + l * plane) : 0u;
-            }
-#pragma unroll
-            for (int q = 0; q < kLoads; ++q) {
-                const int l = l0 + q * kRecLanes;
-                if (l >= kCrtL) break;
-                const uint32_t y0 = yy[q] & 0xFFFFu, y1 = yy[q] >> 16;
-#pragma unroll
-                for (int w = 0; w < kCrtInvWords; ++w) {
-                    const uint32_t c = inv_s[l * kCrtInvWords + w];
-                    a0[w] += (unsigned long long)y0 * c;
-                    a1[w] += (unsigned long long)y1 * c;
-                }
-            }
-        }
-    }
-    // every lane takes part in the shuffles (the group's lanes are consecutive)
-#pragma unroll
-    for (int off = kRecLanes / 2; off > 0; off >>= 1)
-#pragma unroll
-        for (int w = 0; w < kCrtInvWords; ++w) {
-            a0[w] += __shfl_xor_sync(0xffffffffu, a0[w], off);
-            a1[w] += __shfl_xor_sync(0xffffffffu, a1[w], off);
-        }
-    const int bg = b0 + bl;
-    if (g == 0 && ok0) {
-        const int ea = EA[bl * sEA + i] - 2 * kCrtR;
-        crt_finish<N>(a0, ea + EB[bl * sEB + j], alpha_one, p, p.C + bg * p.sc + i + (long long)j * p.ldc);
-    }
-    if (g == (kRecLanes > 1 ? 1 : 0) && ok1) {
-        const int ea = EA[bl * sEA + i] - 2 * kCrtR;
-        crt_finish<N>(a1, ea + EB[bl * sEB + j + 1], alpha_one, p, p.C + bg * p.sc + i + (long long)(j + 1) * p.ldc);
-    }
 }
 
 // The reconstruction on the tensor cores.  A CTA takes tiles of 128 consecutive outputs
@@ -628,8 +556,6 @@ __global__ void __launch_bounds__(kRecM) tc_reconstruct_kernel(const uint16_t *Y
     }
 }
 
-// the reconstruction with the fewest lanes per output pair that still puts about
-// 80k threads in flight
 template <int N>
 void reconstruct_launch_tc(const uint16_t *Y, int Mpad, int Npad, const int *EA, const int *EB, long long sEA,
                            long long sEB, int b0, int alpha_one, const GemmProblem<N> &p, int batch,
@@ -643,21 +569,6 @@ void reconstruct_launch_tc(const uint16_t *Y, int Mpad, int Npad, const int *EA,
     const int grid_x = (int)std::min<long long>(tiles, std::max<long long>(1, 4LL * dev.sms / std::max(1, batch) + 1));
     tc_reconstruct_kernel<N><<<dim3(grid_x, batch), kRecM, kRecSmemLaunch, s>>>(
         Y, Mpad, Npad, EA, EB, sEA, sEB, b0, alpha_one, p, dev.rec_table, error ? error : dev.error, dev.error);
-}
-
-template <int N>
-void reconstruct_launch(const uint16_t *Y, int Mpad, int Npad, const int *EA, const int *EB, long long sEA,
-                        long long sEB, int b0, int alpha_one, const GemmProblem<N> &p, int batch, cudaStream_t s) {
-    const long long pairs = (long long)p.M * ((p.Nn + 1) / 2);
-    const long long want = 80 * 1024;
-    const int G = pairs * batch >= want ? 1 : pairs * batch * 2 >= want ? 2 : pairs * batch * 4 >= want ? 4 : 8;
-    const dim3 grid((unsigned)ceil_div(pairs * G, 128), batch);
-    switch (G) {
-    case 1: crt_reconstruct_kernel<N, 1><<<grid, 128, 0, s>>>(Y, Mpad, Npad, EA, EB, sEA, sEB, b0, alpha_one, p); break;
-    case 2: crt_reconstruct_kernel<N, 2><<<grid, 128, 0, s>>>(Y, Mpad, Npad, EA, EB, sEA, sEB, b0, alpha_one, p); break;
-    case 4: crt_reconstruct_kernel<N, 4><<<grid, 128, 0, s>>>(Y, Mpad, Npad, EA, EB, sEA, sEB, b0, alpha_one, p); break;
-    default: crt_reconstruct_kernel<N, 8><<<grid, 128, 0, s>>>(Y, Mpad, Npad, EA, EB, sEA, sEB, b0, alpha_one, p); break;
-    }
 }
 
 struct CrtLayout {
@@ -836,7 +747,7 @@ void crt_gemm(const GemmProblem<N> &p, void *scratch, cudaStream_t s) {
             reconstruct_launch_tc<N>(Y, L.Mpad, L.Npad, EA, EB, ab ? L.Mpad : 0, bb ? L.Npad : 0, b0, alpha_one, p, G,
                                      dev, p.error, s);
             // every output: its kCrtL residues read, the result written, C read when beta != 0
-            SDPG_CHECK_LAUNCH_KTW("crt_reconstruct_kernel", s,
+            SDPG_CHECK_LAUNCH_KTW("tc_reconstruct_kernel", s,
                                   (double)G * p.M * p.Nn * (p.lower_only ? 0.5 : 1.0) *
                                       (2.0 * kCrtL + sizeof(mlf<N>) * (ml_is_zero(p.beta) ? 1 : 2)));
         }
@@ -977,7 +888,7 @@ void crt_cache_panel(const CrtCache &c, int k0, int kb, mlf<N> *A, long long lda
         p.lower_only = 1;
         SDPG_KT_BEGIN(s);
         reconstruct_launch_tc<N>(c.Y, t.Mpad, t.Npad, c.E + k0, c.E + k0, 0, 0, 0, 0, p, 1, dev, error, s);
-        SDPG_CHECK_LAUNCH_KTW("crt_reconstruct_kernel", s,
+        SDPG_CHECK_LAUNCH_KTW("tc_reconstruct_kernel", s,
                               (double)M * kb * (2.0 * kCrtL + 2.0 * sizeof(mlf<N>)));
     }
 }
