@@ -118,7 +118,8 @@ int sdpg_rgemm_device_noalloc(int limbs, char transa, char transb, int m, int n,
 
 /* In-place lower Cholesky; *info = 0 or the 1-based column of the first
  * non-positive pivot -- replaces Rpotrf("Lower") (mplapack/Rpotrf.cpp:32-154) as
- * called by Lal::choleskyFactorWithAdjust (sdpa_linear.cpp:608-616). */
+ * called by Lal::choleskyFactorWithAdjust (sdpa_linear.cpp:608-616).  Returns
+ * SDPG_ERR_TIMEOUT (with *info = -1) if a bounded wait inside a panel gave up. */
 int sdpg_rpotrf(int limbs, int n, void *A, int lda, int *info);
 /* Linv (n x n, ld n) = L^{-1} for lower-triangular L -- replaces
  * Lal::getInvLowTriangularMatrix (sdpa_linear.cpp:439-455, Rtrsm on I). */
@@ -263,11 +264,12 @@ unsigned long long sdpg_launch_count(void);
  * GEMM everywhere, 2 the residue path for every product with K <= 16384 (tests).
  * Returns the previous method.  Both paths meet the same error bound. */
 int sdpg_set_gemm_method(int method);
-/* *flag = non-zero if a tensor-core GEMM kernel on `device` ever gave up a bounded wait
- * (its results are then invalid).  The flag is sticky: it is never cleared, for the life
- * of the process.  Each solver also has its own word, cleared when it is created and
- * checked every iteration (a time-out there fails that solver with SDPG_ERR_TIMEOUT,
- * not the other solvers on the device). */
+/* *flag = non-zero if a tensor-core GEMM kernel or a standalone Cholesky (sdpg_rpotrf)
+ * on `device` ever gave up a bounded wait (its results are then invalid).  The flag is
+ * sticky: it is never cleared, for the life of the process.  Each solver also has its
+ * own word for its GEMMs and Cholesky panels, cleared when it is created and checked
+ * every iteration (a time-out there fails that solver with SDPG_ERR_TIMEOUT, not the
+ * other solvers on the device). */
 int sdpg_tensor_error(int device, int *flag);
 /* Per-kernel timing (no reference counterpart; the reference's ComputeTime times whole
  * phases).  While enabled, every kernel the library launches outside a stream capture is
@@ -283,7 +285,8 @@ int sdpg_tensor_error(int device, int *flag);
 int sdpg_kernel_timing(int enable);
 int sdpg_kernel_times(char *buf, int cap);
 /* Test hook (no reference counterpart): the budget, in GPU clock cycles, of the
- * tensor-core GEMM kernel's primary waits (TMA data arriving, ring stages freed);
+ * tensor-core GEMM kernel's primary waits (TMA data arriving, ring stages freed) and of
+ * the Cholesky panel's row waits (rows give up with *info = -1 and the error word set);
  * cycles <= 0 restores the default of about one second.  With a budget shorter than a
  * copy takes, those waits give up: the kernel records the time-out in the caller's
  * error word and the sticky device flag (sdpg_tensor_error), waits with the full

@@ -594,8 +594,8 @@ def tensor_error(device: int = 0) -> int:
 
 
 def set_tensor_wait_budget(cycles: int) -> int:
-    """Test hook: budget (clock cycles) of the tensor-core kernel's primary waits; 0 restores
-    the default.  Returns the previous setting."""
+    """Test hook: budget (clock cycles) of the tensor-core kernel's primary waits and the
+    Cholesky panel's row waits; 0 restores the default.  Returns the previous setting."""
     return int(lib().sdpg_set_tensor_wait_budget(cycles))
 
 

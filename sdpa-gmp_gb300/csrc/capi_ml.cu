@@ -262,6 +262,7 @@ int sdpg_rpotrf(int limbs, int n, void *A, int lda, int *info) {
                 return (int)SDPG_OK;
             });
             SDPG_CUDA(cudaMemcpy(info, dinfo.p, sizeof(int), cudaMemcpyDeviceToHost));
+            if (*info == -1) throw sdpg_error(SDPG_ERR_TIMEOUT, "Cholesky panel: a bounded wait timed out");
             return rc;
         });
     });

@@ -3,14 +3,15 @@
 // Lal::choleskyFactorWithAdjust, Lal::getCholesky, Lal::getInvLowTriangularMatrix
 // and Lal::solveSystems, sdpa_linear.cpp:342-455, 608-695).
 //
-// Blocked right-looking with 32-wide panels: the diagonal block is factored in
-// one CTA (pivot square roots and reciprocals in full multi-limb precision), the
-// panel below is solved one row per warp, and the trailing matrix is updated by
-// the block-floating-point GEMM (lower triangle only).
+// Blocked left-looking with 32-wide panels: each panel first receives the product of
+// the finished columns (the residue-path GEMM), then one cluster launch factors its
+// diagonal block and, a step behind, the rows below it, all by the same division-free
+// elimination with full multi-limb pivots.
 #include <cooperative_groups.h>
 
 #include "kernels.cuh"
 #include "mlwarp.cuh"
+#include "tc_gemm.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -20,116 +21,177 @@ namespace {
 
 constexpr int NB = 32;
 
-// Factor the kb x kb diagonal block at A (ld lda) in place; rinv[j] = 1/L[j][j] and
-// Lsc (ld NB) = diag(rinv) L, the row-scaled factor the panel solve uses.
-// info: 0, or (col0 + j + 1) for the first non-positive pivot.
+// One launch factors a whole 32-column panel: the kb x kb diagonal block and the rows
+// below it.
 //
-// Division-free elimination.  One thread per lower-triangle entry keeps it in
-// registers.  Step j updates every entry right of column j as
+// Division-free elimination.  Every entry of the panel's lower part is held in a
+// register by its own thread.  Step j updates every entry right of column j as
 //     s_it <- (p_j s_it - s_ij s_tj) * 2^-e_j,     p_j = s_jj in [2^(e_j-1), 2^e_j),
 // so S^(j) = c_j T^(j) where T^(j) is the usual Schur complement and
 // c_{j+1} = c_j p_j 2^-e_j.  No square root or reciprocal sits on the pivot chain
 // (one multiply-subtract and one barrier per step); at the end every column is
-// normalised at once with L[i][j] = s_ij / sqrt(c_j p_j).
-constexpr int kPotf2Threads = ((NB * (NB + 1) / 2 + 31) / 32) * 32;
+// normalised at once with L[i][t] = s_it / sqrt(c_t p_t).
+//
+// The diagonal block (528 entries, numbered column by column: column t holds rows
+// t..NB-1) is spread over a cluster of C CTAs (one per SM), entry q in CTA q mod C.  The
+// entries still active at step j (t > j) are the highest-numbered ones, so in every CTA
+// whole warps drop out as the elimination proceeds while the remaining work stays spread
+// over all C SMs.  The pivot column, the c_j and the pivots are replicated in every CTA's
+// shared memory; their owners write all copies through distributed shared memory and
+// one cluster barrier per step publishes them.
+//
+// The rows below take the same steps one warp per row (lane t holds s_it): s_ij is lane
+// j of the same warp and p_j, s_tj (column j of the diagonal block after j steps) come
+// from a history buffer in global memory that one warp of the diagonal cluster fills
+// after each barrier, behind a progress word.  So the rows run a step or so behind the
+// diagonal block rather than after it, and no separate triangular solve follows.
+//
+// Roles: each cluster draws a ticket when it starts; the first factors the diagonal
+// block, so a cluster that waits always waits on one that is running.  The row waits
+// are bounded by a cycle budget: on time-out the row sets *info = -1 (if it was 0) and
+// the error word, and returns.
+//
+// info: 0, or (col0 + j + 1) for the first non-positive pivot.
+// sync (two ints, zeroed once per factorisation): [0] ticket counter, [1] progress, which
+// for the panel with progress base `base` reads base + j + 1 once hist column j is out,
+// base + kPanelFinal once the normalisers are, and base + kPanelAbort after a bad pivot.
+// hist: NB x NB entries (column j at hist[j NB ..]), then the NB normalisers.
+constexpr int kPotf2Threads = ((NB * (NB + 1) / 2 + 31) / 32) * 32;  // one thread per entry of a block
+constexpr int kPanelFinal = 40;
+constexpr int kPanelAbort = 63;
+constexpr int kPanelTimeout = 6;                 // error-word code of a row wait that gave up
+constexpr long long kPanelWaitCycles = 1ll << 31;  // about one second at 2 GHz
+static_assert(kPanelAbort < 64 && kPanelFinal > NB, "progress values of one panel stay below the next base");
+
+// Launch shape for a cluster of C CTAs: the entries of the diagonal block dealt out
+// cyclically (entry q to CTA q mod C, local index q / C), so at every step the active
+// entries (the highest-numbered ones) are spread evenly over the cluster's SMs, and one
+// more warp per CTA, which holds no entry (in CTA 0 it fills the history).  A CTA of a
+// row cluster works R rows, one per warp, and its other warps leave.
+template <int C>
+struct PanelShape {
+    static constexpr int per_cta = (NB * (NB + 1) / 2 + C - 1) / C;
+    static constexpr int threads = ((per_cta + 31) / 32 + 1) * 32;
+};
+constexpr int kPanelCluster = 4;  // cluster size of ml_potrf's panels
+constexpr int kPanelRowWarps = 3;  // rows per CTA of the row clusters (at most threads / 32)
 
 template <int N>
-__global__ void __launch_bounds__(kPotf2Threads, 1)
-    potf2_kernel(mlf<N> *A, int lda, int kb, int col0, int *info, mlf<N> *rinv, mlf<N> *Lsc) {
+__device__ __forceinline__ mlf<N> ml_load_cg(const mlf<N> *p) {
+    mlf<N> r;
+    const unsigned *w = reinterpret_cast<const unsigned *>(p);
+    unsigned *o = reinterpret_cast<unsigned *>(&r);
+#pragma unroll
+    for (int k = 0; k < N + 2; ++k) o[k] = __ldcg(w + k);
+    return r;
+}
+
+// the calling warp's history stores, then the progress word (one warp, all lanes)
+__device__ __forceinline__ void panel_progress(int *prog, int v) {
+    __threadfence();
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) atomicExch(prog, v);
+}
+
+// wait (all lanes of a warp) until *prog >= target; the value seen, or -1 on time-out
+__device__ __forceinline__ int panel_wait(const int *prog, int target, long long budget) {
+    int v = *(volatile const int *)prog;
+    if (v < target) {
+        const long long t0 = clock64();
+        while ((v = *(volatile const int *)prog) < target) {
+            if (clock64() - t0 > budget) return -1;
+            __nanosleep(32);
+        }
+    }
+    __threadfence();
+    return v;
+}
+
+template <int N, int C, int R>
+__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(PanelShape<C>::threads)
+    panel_factor_kernel(mlf<N> *A, int lda, int col0, int kb, int rows, int *info, mlf<N> *hist, int *sync, int base,
+                        int ticket0, long long budget, int *err) {
     __shared__ mlf<N> col[2][NB];  // column j of S^(j), double-buffered across steps
     __shared__ mlf<N> cs[NB];      // c_j
     __shared__ mlf<N> pv[NB];      // p_j
     __shared__ mlf<N> rs[NB];      // 1/sqrt(c_j p_j)
-    __shared__ mlf<N> ri[NB];      // 1/L[j][j] = c_j / sqrt(c_j p_j)
-    if (*info != 0) return;
-    // entries numbered column by column (column t holds rows t..NB-1), so the entries
-    // still active at step j (t > j) are the highest-numbered threads and whole warps
-    // drop out as the factorisation proceeds
-    const int q = threadIdx.x;
-    int t = 0;
-    while (t + 1 < NB && NB * (t + 1) - (t + 1) * t / 2 <= q) ++t;
-    const int i = t + (q - (NB * t - t * (t - 1) / 2));  // entry (i, t), t <= i
-    const bool mine = q < NB * (NB + 1) / 2 && i < kb;
-    mlf<N> a = mine ? A[i + (long long)t * lda] : ml_zero<N>();
-    if (mine && t == 0) col[0][i] = a;
-    __syncthreads();
-    mlf<N> c = ml_one<N>();  // thread 0 (entry (0,0), idle after step 0) carries c_j
-    int bad = 0;
-    for (int j = 0; j < kb; ++j) {
-        const mlf<N> p = col[j & 1][j];
-        if (ml_sign(p) <= 0) {
-            bad = col0 + j + 1;
-            break;
-        }
-        if (q == 0) {
-            cs[j] = c;
-            c = ml_mul(c, ml_ldexp(p, -p.e));
-        }
-        if (mine && t > j) {
-            const mlf<N> u = ml_sub(ml_mul(p, a), ml_mul(col[j & 1][i], col[j & 1][t]));
-            a = ml_ldexp(u, -p.e);
-            if (t == j + 1) col[(j + 1) & 1][i] = a;
-        }
-        __syncthreads();
-    }
-    if (bad) {
-        if (q == 0) *info = bad;
-        return;
-    }
-    if (mine && i == t) pv[t] = a;
-    __syncthreads();
-    if (q < kb) {
-        const mlf<N> r = ml_rsqrt(ml_mul(cs[q], pv[q]));
-        rs[q] = r;
-        ri[q] = ml_mul(cs[q], r);
-    }
-    __syncthreads();
-    if (mine) {
-        a = ml_mul(a, rs[t]);
-        A[i + (long long)t * lda] = a;
-        if (i > t) Lsc[i + NB * t] = ml_mul(a, ri[i]);
-    }
-    if (q < kb) rinv[q] = ri[q];
-}
-
-// strict lower triangle of an NB x NB block, packed column by column
-__host__ __device__ constexpr int packed_lower(int i, int j) { return j * NB - j * (j + 1) / 2 + (i - j - 1); }
-constexpr int kPackedLower = NB * (NB - 1) / 2;
-
-// The same elimination spread over a cluster of kPotf2Cluster CTAs (one per SM): CTA r
-// holds entries r*Q .. r*Q+Q-1 of the column-by-column numbering.  The pivot column,
-// the scale factors c_j and the pivots are replicated in every CTA's shared memory;
-// their owners write all copies through distributed shared memory, and one cluster
-// barrier per step publishes them.  Per SM a step now issues a quarter of the
-// multi-limb operations, which is what bounds the single-CTA version.
-constexpr int kPotf2Cluster = 4;
-constexpr int kPotf2PerCta = (NB * (NB + 1) / 2 + kPotf2Cluster - 1) / kPotf2Cluster;  // 132
-constexpr int kPotf2ClusterThreads = ((kPotf2PerCta + 31) / 32) * 32;                  // 160
-
-template <int N>
-__global__ void __cluster_dims__(kPotf2Cluster, 1, 1) __launch_bounds__(kPotf2ClusterThreads)
-    potf2_cluster_kernel(mlf<N> *A, int lda, int kb, int col0, int *info, mlf<N> *rinv, mlf<N> *Lsc) {
-    __shared__ mlf<N> col[2][NB];
-    __shared__ mlf<N> cs[NB];
-    __shared__ mlf<N> pv[NB];
-    __shared__ mlf<N> rs[NB];
-    __shared__ mlf<N> ri[NB];
+    __shared__ int role[2];        // rank 0: this cluster's ticket in the launch, *info at start
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
-    if (*info != 0) return;  // the same value for every CTA of the cluster
-    const int q = rank * kPotf2PerCta + (int)threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int *prog = sync + 1;
+    if (rank == 0 && threadIdx.x == 0) {
+        role[0] = atomicAdd(&sync[0], 1) - ticket0;
+        role[1] = *(volatile int *)info;
+    }
+    cluster.sync();
+    const int tk = *cluster.map_shared_rank(&role[0], 0);
+    const int info0 = *cluster.map_shared_rank(&role[1], 0);
+    cluster.sync();     // rank 0's words are read before any CTA of the cluster leaves
+    if (info0 != 0) return;  // an earlier panel failed: the whole launch leaves
+
+    if (tk > 0) {  // ------------------------------------------------ rows below the block
+        const int w = (int)(threadIdx.x >> 5);
+        const int r = (tk - 1) * C * R + rank * R + w;
+        if (w >= R || r >= rows) return;
+        mlf<N> *row = A + col0 + kb + r + (long long)col0 * lda;  // entry t at row[t * lda]
+        mlf<N> a = lane < kb ? row[(long long)lane * lda] : ml_zero<N>();
+        int seen = 0;
+        // p_j and s_tj of the next step, loaded a step early whenever the progress word
+        // already showed them (the rows trail the diagonal block, so mostly they are)
+        mlf<N> pn = ml_zero<N>(), sn = ml_zero<N>();
+        bool have = false;
+        for (int j = 0; j <= kb; ++j) {
+            const int need = j + 1 < kb ? base + j + 1 : base + kPanelFinal;
+            if (!have && seen < need) {
+                seen = panel_wait(prog, need, budget);
+                if (seen < 0) {
+                    if (lane == 0) {
+                        atomicCAS(info, 0, -1);
+                        atomicExch(err, kPanelTimeout);
+                    }
+                    return;
+                }
+                if (seen >= base + kPanelAbort) return;  // the diagonal block failed
+            }
+            if (j + 1 >= kb) break;  // normalisers published
+            if (!have) {
+                pn = ml_load_cg(hist + (long long)j * NB + j);
+                sn = lane > j && lane < kb ? ml_load_cg(hist + (long long)j * NB + lane) : ml_zero<N>();
+            }
+            const mlf<N> p = pn, stj = sn;
+            have = j + 2 < kb && seen >= base + j + 2 && seen < base + kPanelAbort;
+            if (have) {
+                pn = ml_load_cg(hist + (long long)(j + 1) * NB + j + 1);
+                sn = lane > j + 1 && lane < kb ? ml_load_cg(hist + (long long)(j + 1) * NB + lane) : ml_zero<N>();
+            }
+            const mlf<N> sij = ml_shfl(a, j);
+            if (lane > j && lane < kb) a = ml_ldexp(ml_sub(ml_mul(p, a), ml_mul(sij, stj)), -p.e);
+        }
+        if (lane < kb) row[(long long)lane * lda] = ml_mul(a, ml_load_cg(hist + NB * NB + lane));
+        return;
+    }
+
+    // ---------------------------------------------------------------- the diagonal block
+    mlf<N> *Akk = A + col0 + (long long)col0 * lda;
+    const bool signal = rank == 0 && (int)threadIdx.x >= PanelShape<C>::threads - 32;  // fills hist
+    const int q = (int)threadIdx.x * C + rank;
     int t = 0;
     while (t + 1 < NB && NB * (t + 1) - (t + 1) * t / 2 <= q) ++t;
     const int i = t + (q - (NB * t - t * (t - 1) / 2));  // entry (i, t), t <= i
-    const bool mine = (int)threadIdx.x < kPotf2PerCta && q < NB * (NB + 1) / 2 && i < kb;
-    mlf<N> a = mine ? A[i + (long long)t * lda] : ml_zero<N>();
+    const bool mine = (int)threadIdx.x < PanelShape<C>::per_cta && q < NB * (NB + 1) / 2 && i < kb;
+    mlf<N> a = mine ? Akk[i + (long long)t * lda] : ml_zero<N>();
     // publish v at the same shared-memory slot of every CTA in the cluster
     auto publish = [&](mlf<N> *slot, const mlf<N> &v) {
 #pragma unroll
-        for (int r = 0; r < kPotf2Cluster; ++r) *cluster.map_shared_rank(slot, r) = v;
+        for (int r = 0; r < C; ++r) *cluster.map_shared_rank(slot, r) = v;
     };
     if (mine && t == 0) publish(&col[0][i], a);
     cluster.sync();
+    if (signal) {
+        if (lane < kb) hist[lane] = col[0][lane];
+        panel_progress(prog, base + 1);
+    }
     mlf<N> c = ml_one<N>();  // carried by entry (0, 0) (rank 0, thread 0), idle after step 0
     int bad = 0;
     for (int j = 0; j < kb; ++j) {
@@ -148,52 +210,33 @@ __global__ void __cluster_dims__(kPotf2Cluster, 1, 1) __launch_bounds__(kPotf2Cl
             if (t == j + 1) publish(&col[(j + 1) & 1][i], a);
         }
         cluster.sync();
+        // column j + 1 is complete in col[(j + 1) & 1] and stays there until step j + 2
+        // writes it, after the next barrier, which this warp has not yet reached
+        if (signal && j + 2 < kb) {
+            if (lane > j && lane < kb) hist[(long long)(j + 1) * NB + lane] = col[(j + 1) & 1][lane];
+            panel_progress(prog, base + j + 2);
+        }
     }
     if (!bad) {
         if (mine && i == t) publish(&pv[t], a);
         cluster.sync();
-        if ((int)threadIdx.x < kb) {  // every CTA forms the normalisers it needs
-            const mlf<N> r = ml_rsqrt(ml_mul(cs[threadIdx.x], pv[threadIdx.x]));
-            rs[threadIdx.x] = r;
-            ri[threadIdx.x] = ml_mul(cs[threadIdx.x], r);
-        }
+        if ((int)threadIdx.x < kb) rs[threadIdx.x] = ml_rsqrt(ml_mul(cs[threadIdx.x], pv[threadIdx.x]));
         __syncthreads();
-        if (mine) {
-            a = ml_mul(a, rs[t]);
-            A[i + (long long)t * lda] = a;
-            if (i > t) Lsc[i + NB * t] = ml_mul(a, ri[i]);
+        if (mine) Akk[i + (long long)t * lda] = ml_mul(a, rs[t]);
+        if (signal) {
+            if (lane < kb) hist[NB * NB + lane] = rs[lane];
+            panel_progress(prog, base + kPanelFinal);
         }
-        if (rank == 0 && (int)threadIdx.x < kb) rinv[threadIdx.x] = ri[threadIdx.x];
-    } else if (q == 0) {
-        *info = bad;
+    } else {
+        if (q == 0) *info = bad;
+        if (signal) panel_progress(prog, base + kPanelAbort);
     }
     cluster.sync();  // no CTA leaves while another may still write its shared memory
 }
 
-// Rows below the diagonal block: solve x L11^T = a for each row, one warp per row.
-// With a~ = a / diag(L11) and Lsc = diag(L11)^-1 L11 (unit lower), x_j = a~_j -
-// sum_{t<j} Lsc[j][t] x_t: each step is a broadcast and one multiply-subtract, with
-// Lsc read from shared memory (staged once per block).
-template <int N>
-__global__ void panel_trsm_kernel(const mlf<N> *Lsc, mlf<N> *R, int lda, int kb, int nrows, const int *info,
-                                  const mlf<N> *rinv) {
-    __shared__ mlf<N> ls[kPackedLower];
-    if (*info != 0) return;
-    for (int q = threadIdx.x; q < NB * NB; q += blockDim.x) {
-        const int i = q % NB, j = q / NB;
-        if (i > j && i < kb) ls[packed_lower(i, j)] = Lsc[i + NB * j];
-    }
-    __syncthreads();
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= nrows) return;
-    mlf<N> *row = R + warp;  // element t at row[t * lda]
-    mlf<N> a = lane < kb ? ml_mul(row[(long long)lane * lda], rinv[lane]) : ml_zero<N>();
-    for (int j = 0; j + 1 < kb; ++j) {
-        const mlf<N> xj = ml_shfl(a, j);
-        if (lane > j && lane < kb) a = ml_sub(a, ml_mul(xj, ls[packed_lower(lane, j)]));
-    }
-    if (lane < kb) row[(long long)lane * lda] = a;
-}
+// strict lower triangle of an NB x NB block, packed column by column
+__host__ __device__ constexpr int packed_lower(int i, int j) { return j * NB - j * (j + 1) / 2 + (i - j - 1); }
+constexpr int kPackedLower = NB * (NB - 1) / 2;
 
 // Invert every NB x NB diagonal block of the lower-triangular L (n a multiple of NB)
 // into Linv, one block per CTA and one thread per lower-triangle entry of the inverse,
@@ -214,7 +257,7 @@ __global__ void __launch_bounds__(kPotf2Threads, 1) trtri_diag_kernel(const mlf<
         if (i > j) ts[packed_lower(i, j)] = T[i + (long long)j * ldl];
     }
     if (q < NB) rv[q] = ml_recip(T[q + (long long)q * ldl]);
-    // entry (i, c), c <= i, numbered column by column as in potf2_kernel
+    // entry (i, c), c <= i, numbered column by column as in the diagonal block of panel_factor_kernel
     int c = 0;
     while (c + 1 < NB && NB * (c + 1) - (c + 1) * c / 2 <= q) ++c;
     const int i = c + (q - (NB * c - c * (c - 1) / 2));
@@ -282,16 +325,6 @@ __global__ void trtri_diag_packed_kernel(const mlf<N> *L, int ldl, mlf<N> *Dinv,
 //
 // sync (ints, zeroed before each launch): [0] ticket counter, [1 + b] block b done.
 constexpr int kTrsvThreads = 256;
-
-template <int N>
-__device__ __forceinline__ mlf<N> ml_load_cg(const mlf<N> *p) {
-    mlf<N> r;
-    const unsigned *w = reinterpret_cast<const unsigned *>(p);
-    unsigned *o = reinterpret_cast<unsigned *>(&r);
-#pragma unroll
-    for (int k = 0; k < N + 2; ++k) o[k] = __ldcg(w + k);
-    return r;
-}
 
 constexpr int kTrsvWarps = kTrsvThreads / 32;
 constexpr long long kSpinLimit = 1ll << 24;
@@ -433,18 +466,23 @@ GemmProblem<N> gemm_nn(int M, int Nn, int K, const mlf<N> &alpha, const mlf<N> *
 //     A[k0:, k0:k0+kb] -= L[k0:, :k0] L[k0:k0+kb, :k0]^T,
 // so the factorisation costs one exact (residue-path) product per panel whose output is
 // only the panel, not the whole trailing matrix.
-template <int N>
-void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t s) {
+template <int N, int C, int R>
+void potrf_panels(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t s) {
     SDPG_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
     const size_t mark = ws.used;
-    mlf<N> *rinv = (mlf<N> *)ws.carve(NB * sizeof(mlf<N>));
-    mlf<N> *Lsc = (mlf<N> *)ws.carve(NB * NB * sizeof(mlf<N>));
+    int *sync = (int *)ws.carve(2 * sizeof(int));
+    mlf<N> *hist = (mlf<N> *)ws.carve((NB * NB + NB) * sizeof(mlf<N>));
+    SDPG_CUDA(cudaMemsetAsync(sync, 0, 2 * sizeof(int), s));
+    int *err = ws.error ? ws.error : crt_error_word();
+    // the test hook that shortens the tensor-core waits shortens these too
+    const long long budget = g_tc_wait_cycles > 0 ? g_tc_wait_cycles : kPanelWaitCycles;
     const mlf<N> mone = ml_from_int<N>(-1), one = ml_one<N>();
     // 256-bit factors of at least 128 rows: the panel products read the residues of the
     // finished columns, converted once each (crt_cache_*)
     const bool cached = crt_cache_applies<N>(n);
     CrtCache cache;
     if (cached) cache = crt_cache_init<N>(n, A, lda, ws.carve(crt_cache_bytes(n)), s);
+    int ticket0 = 0;
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int kb = min(NB, n - k0);
         const int rows = n - k0 - kb;
@@ -458,17 +496,21 @@ void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t 
             ml_gemm<N>(p, ws, s);
             ws.used = m2;
         }
+        const int clusters = 1 + ceil_div(rows, C * R);
         SDPG_KT_BEGIN(s);
-        potf2_cluster_kernel<N><<<kPotf2Cluster, kPotf2ClusterThreads, 0, s>>>(Akk, lda, kb, k0, info, rinv, Lsc);
-        SDPG_CHECK_LAUNCH_KT("potf2_cluster_kernel", s);
-        if (rows <= 0) break;
-        SDPG_KT_BEGIN(s);
-        panel_trsm_kernel<N><<<ceil_div((long long)rows * 32, 256), 256, 0, s>>>(Lsc, Akk + kb, lda, kb, rows, info,
-                                                                               rinv);
-        SDPG_CHECK_LAUNCH_KT("panel_trsm_kernel", s);
-        if (cached) crt_cache_put<N>(cache, A, lda, k0, kb, ws.error, s);
+        panel_factor_kernel<N, C, R><<<clusters * C, PanelShape<C>::threads, 0, s>>>(
+            A, lda, k0, kb, rows, info, hist, sync, 2 * k0, ticket0, budget, err);
+        SDPG_CHECK_LAUNCH_KT("panel_factor_kernel", s);
+        ticket0 += clusters;
+        if (cached && rows > 0) crt_cache_put<N>(cache, A, lda, k0, kb, ws.error, s);
     }
     ws.used = mark;
+}
+
+template <int N>
+void ml_potrf(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t s) {
+    static_assert(kPanelRowWarps * 32 <= PanelShape<kPanelCluster>::threads, "one row per warp");
+    potrf_panels<N, kPanelCluster, kPanelRowWarps>(n, A, lda, info, ws, s);
 }
 
 template <int N>
@@ -480,7 +522,7 @@ size_t ml_potrf_workspace_bytes(int n) {
     p.batch = 1;
     size_t b = gemm_workspace_bytes<N>(p);
     if (crt_cache_applies<N>(n)) b = std::max(b, crt_cache_bytes(n));
-    return b + (size_t)(NB + NB * NB) * sizeof(mlf<N>) + 4096;
+    return b + (size_t)(NB + NB * NB) * sizeof(mlf<N>) + 4096;  // history, progress words, alignment
 }
 
 namespace {

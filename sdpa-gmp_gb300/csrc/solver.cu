@@ -401,8 +401,9 @@ class Solver final : public SolverBase {
         max_ws = std::max(max_ws, ml_potrf_workspace_bytes<N>(m_));
         ws_.reserve(max_ws + (64u << 20));
         ws2_.reserve(max_ws + (64u << 20));
-        // this solver's own tensor-core time-out word (zeroed by dalloc_raw): a wait that
-        // gives up in another solver on the device does not fail this one
+        // this solver's own time-out word (zeroed by dalloc_raw) for the bounded waits of its
+        // tensor-core GEMMs and Cholesky panels: a wait that gives up in another solver on
+        // the device does not fail this one
         tc_error_ = (int *)dalloc_raw(sizeof(int));
         ws_.error = ws2_.error = tc_error_;
         SDPG_CUDA(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
@@ -1397,15 +1398,15 @@ class Solver final : public SolverBase {
         fflush(trace_);
     }
 
-    // SDPG_ERR_TIMEOUT if a tensor-core GEMM of this solver gave up a bounded wait (its
-    // products, and everything computed from them, are then invalid)
+    // SDPG_ERR_TIMEOUT if a tensor-core GEMM or a Cholesky panel of this solver gave up a
+    // bounded wait (its results, and everything computed from them, are then invalid)
     void check_tensor_timeout() {
-        if (N != 8 || !tc_error_) return;
+        if (!tc_error_) return;
         int st = 0;
         d2h_ += (long long)sizeof(int);
         SDPG_CUDA(cudaMemcpyAsync(&st, tc_error_, sizeof(int), cudaMemcpyDeviceToHost, st_));
         SDPG_CUDA(cudaStreamSynchronize(st_));
-        if (st != 0) throw sdpg_error(SDPG_ERR_TIMEOUT, "tensor-core GEMM: a bounded wait timed out");
+        if (st != 0) throw sdpg_error(SDPG_ERR_TIMEOUT, "tensor-core GEMM or Cholesky panel: a bounded wait timed out");
     }
 
     // A time-out takes precedence over whatever the invalid products made happen next
@@ -1453,8 +1454,9 @@ class Solver final : public SolverBase {
                 step_length(1);
             }
         }
-        // the tensor-core GEMMs' bounded waits (step_length has synchronised the streams)
-        if (g_gemm_method != 1) check_tensor_timeout();
+        // the bounded waits of the tensor-core GEMMs and the Cholesky panels (step_length
+        // has synchronised the streams)
+        check_tensor_timeout();
         record_iteration();
         feats_.push_back(feat);
         lastAP_ = aP_;
@@ -1486,7 +1488,7 @@ class Solver final : public SolverBase {
     }
     bool loop_corrector_break() const override { return phase_ == pdFEAS && (betaV_ > R(5) || objP_ < objD_); }
     void loop_record(FILE *out, FILE *display) override {
-        if (g_gemm_method != 1) check_tensor_timeout();
+        check_tensor_timeout();
         record_iteration();
         feats_.push_back(policy_features(betaV_));
         lastAP_ = aP_;
@@ -1810,7 +1812,7 @@ class Solver final : public SolverBase {
     int dev_;
     cudaStream_t st_;
     Workspace ws_, ws2_;  // ws2_ serves work issued on the second stream
-    int *tc_error_ = nullptr;  // device word: a tensor-core GEMM of this solver gave up a bounded wait
+    int *tc_error_ = nullptr;  // device word: a tensor-core GEMM or Cholesky panel gave up a bounded wait
 
     cudaStream_t st2_ = nullptr;
     cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;

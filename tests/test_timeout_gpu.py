@@ -1,16 +1,19 @@
-"""Failure detection of the tensor-core GEMM's bounded waits, without a GPU fault.
+"""Failure detection of the bounded waits, without a GPU fault.
 
-A child process shortens the kernel's primary wait budget (TMA data, free ring
-stages) to fewer cycles than a copy takes, so those waits give up while the data is
-still legitimately on its way.  The kernel then records the time-out, waits with the
-full budget for the copies and products it already issued, frees its tensor memory
-and returns; nothing is left running and the context stays usable.  Checked:
+A child process shortens the tensor-core GEMM's primary wait budget (TMA data, free
+ring stages) to fewer cycles than a copy takes, so those waits give up while the data
+is still legitimately on its way.  The kernel then records the time-out, waits with
+the full budget for the copies and products it already issued, frees its tensor
+memory and returns; nothing is left running and the context stays usable.  The same
+budget bounds the Cholesky panel's row waits (the rows of a panel wait for the
+columns of its diagonal block), which then give up with info = -1.  Checked:
 
   * a standalone product reports the time-out in the sticky device flag;
+  * a standalone Cholesky returns SDPG_ERR_TIMEOUT;
   * a solver fails with SDPG_ERR_TIMEOUT at the first iteration;
-  * with the default budget restored, a new product is exact again and a new solver
-    (its own, fresh error word) solves the problem as the reference does, although
-    the device-wide flag stays set.
+  * with the default budget restored, a new product is exact again, the Cholesky
+    succeeds, and a new solver (its own, fresh error word) solves the problem as the
+    reference does, although the device-wide flag stays set.
 
 It runs in a child process so that the sticky flag does not reach the other tests.
 """
@@ -43,6 +46,14 @@ CHILD = textwrap.dedent("""
     sdpg.set_tensor_wait_budget(16)  # far shorter than a TMA copy takes
     sdpg.rgemm("N", "N", m, n, k, one, A, m, B, k, zero, C, m)
     assert sdpg.tensor_error(0) != 0, "the time-out was not recorded"
+    import numpy as np
+    nc = 64                          # two panels: the first one's rows wait on its diagonal block
+    S = sdpg.ml_from_double((np.ones((nc, nc)) + nc * np.eye(nc)).reshape(-1), 8)
+    try:
+        sdpg.rpotrf(S, nc, nc)
+        raise SystemExit("the Cholesky panel did not report the time-out")
+    except sdpg.SdpgError as e:
+        assert e.code == -8, e.code
     dat, par, g = write_inputs("maxcut20", {tmp!r})
     s = sdpg.Solver(sdpg.Problem.read(dat), sdpg.Param.read(par))
     try:
@@ -57,6 +68,7 @@ CHILD = textwrap.dedent("""
                             exact.ml_decode(zero)[0], exact.ml_decode(C), m)
     err = exact.max_rel_err(got, ref, scale)
     assert err <= 2.0 ** -240, err
+    assert sdpg.rpotrf(S, nc, nc)[1] == 0
     s = sdpg.Solver(sdpg.Problem.read(dat), sdpg.Param.read(par))
     s.run()
     info = s.info()
