@@ -12,6 +12,7 @@
 #include "kernels.cuh"
 #include "mlwarp.cuh"
 #include "tc_gemm.cuh"
+#include "tcgen05.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -28,28 +29,30 @@ constexpr int NB = 32;
 // register by its own thread.  Step j updates every entry right of column j as
 //     s_it <- (p_j s_it - s_ij s_tj) * 2^-e_j,     p_j = s_jj in [2^(e_j-1), 2^e_j),
 // so S^(j) = c_j T^(j) where T^(j) is the usual Schur complement and
-// c_{j+1} = c_j p_j 2^-e_j.  No square root or reciprocal sits on the pivot chain
-// (one multiply-subtract and one barrier per step); at the end every column is
-// normalised at once with L[i][t] = s_it / sqrt(c_t p_t).
+// c_{j+1} = c_j p_j 2^-e_j.  No square root or reciprocal sits on the pivot chain; at
+// the end every column is normalised at once with L[i][t] = s_it / sqrt(c_t p_t).
 //
 // The diagonal block (528 entries, numbered column by column: column t holds rows
 // t..NB-1) is spread over a cluster of C CTAs (one per SM), entry q in CTA q mod C.  The
 // entries still active at step j (t > j) are the highest-numbered ones, so in every CTA
 // whole warps drop out as the elimination proceeds while the remaining work stays spread
-// over all C SMs.  The pivot column, the c_j and the pivots are replicated in every CTA's
-// shared memory; their owners write all copies through distributed shared memory and
-// one cluster barrier per step publishes them.
+// over all C SMs.  Every CTA keeps a copy of the columns of S^(j) (each column j in the
+// pivot's step): an entry that becomes final stores itself into all copies with
+// st.async, and each column's mbarrier tells a CTA when the column has arrived.  A
+// thread waits only for the columns it reads, so a step costs one update and one remote
+// store instead of the slowest thread's update plus a cluster barrier.
 //
 // The rows below take the same steps one warp per row (lane t holds s_it): s_ij is lane
 // j of the same warp and p_j, s_tj (column j of the diagonal block after j steps) come
-// from a history buffer in global memory that one warp of the diagonal cluster fills
-// after each barrier, behind a progress word.  So the rows run a step or so behind the
+// from a history buffer in global memory that one warp of the diagonal cluster fills as
+// the columns arrive, behind a progress word.  So the rows run a few steps behind the
 // diagonal block rather than after it, and no separate triangular solve follows.
 //
 // Roles: each cluster draws a ticket when it starts; the first factors the diagonal
 // block, so a cluster that waits always waits on one that is running.  The row waits
 // are bounded by a cycle budget: on time-out the row sets *info = -1 (if it was 0) and
-// the error word, and returns.
+// the error word, and returns (the diagonal block's own waits have the full budget and
+// do the same).
 //
 // info: 0, or (col0 + j + 1) for the first non-positive pivot.
 // sync (two ints, zeroed once per factorisation): [0] ticket counter, [1] progress, which
@@ -74,7 +77,7 @@ struct PanelShape {
     static constexpr int threads = ((per_cta + 31) / 32 + 1) * 32;
 };
 constexpr int kPanelCluster = 4;  // cluster size of ml_potrf's panels
-constexpr int kPanelRowWarps = 3;  // rows per CTA of the row clusters (at most threads / 32)
+constexpr int kPanelRowWarps = 4;  // rows per CTA of the row clusters (at most threads / 32)
 
 template <int N>
 __device__ __forceinline__ mlf<N> ml_load_cg(const mlf<N> *p) {
@@ -84,6 +87,42 @@ __device__ __forceinline__ mlf<N> ml_load_cg(const mlf<N> *p) {
 #pragma unroll
     for (int k = 0; k < N + 2; ++k) o[k] = __ldcg(w + k);
     return r;
+}
+
+// one multi-limb value in shared memory, padded to the 16-byte unit of st.async
+template <int N>
+struct alignas(16) PanelSlot {
+    mlf<N> v;
+};
+
+// packed column-major lower triangle with the diagonal: column t holds rows t..NB-1
+__host__ __device__ constexpr int packed_col(int i, int t) { return NB * t - t * (t - 1) / 2 + (i - t); }
+
+// the shared::cluster address of a shared-memory location of CTA `rank`
+__device__ __forceinline__ uint32_t cluster_addr(uint32_t local, int rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+    return r;
+}
+
+// v into the cluster shared-memory address dst (16-byte aligned), completing its
+// sizeof(mlf<N>) bytes on the mbarrier at bar (same CTA as dst)
+template <int N>
+__device__ __forceinline__ void st_async_ml(uint32_t dst, const mlf<N> &v, uint32_t bar) {
+    constexpr int W = (int)sizeof(mlf<N>) / 4;  // 10 or 18 words: 16-byte pieces, then 8
+    static_assert(W % 4 == 2, "layout of mlf");
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(&v);
+#pragma unroll
+    for (int k = 0; k + 4 <= W; k += 4)
+        asm volatile(
+            "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
+                dst + 4u * k),
+            "r"(w[k]), "r"(w[k + 1]), "r"(w[k + 2]), "r"(w[k + 3]), "r"(bar)
+            : "memory");
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.b32 [%0], {%1, %2}, [%3];" ::"r"(
+                     dst + 4u * (W - 2)),
+                 "r"(w[W - 2]), "r"(w[W - 1]), "r"(bar)
+                 : "memory");
 }
 
 // the calling warp's history stores, then the progress word (one warp, all lanes)
@@ -111,20 +150,27 @@ template <int N, int C, int R>
 __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(PanelShape<C>::threads)
     panel_factor_kernel(mlf<N> *A, int lda, int col0, int kb, int rows, int *info, mlf<N> *hist, int *sync, int base,
                         int ticket0, long long budget, int *err) {
-    __shared__ mlf<N> col[2][NB];  // column j of S^(j), double-buffered across steps
-    __shared__ mlf<N> cs[NB];      // c_j
-    __shared__ mlf<N> pv[NB];      // p_j
-    __shared__ mlf<N> rs[NB];      // 1/sqrt(c_j p_j)
-    __shared__ int role[2];        // rank 0: this cluster's ticket in the launch, *info at start
+    __shared__ PanelSlot<N> colv[NB * (NB + 1) / 2];      // column j of S^(j) at colv[packed_col(i, j)]
+    __shared__ __align__(8) unsigned long long bars[NB];  // bars[j]: column j has arrived here
+    __shared__ mlf<N> cs[NB];                             // c_j
+    __shared__ mlf<N> rs[NB];                             // 1/sqrt(c_j p_j)
+    __shared__ int role[2];  // rank 0: this cluster's ticket in the launch, *info at start
+    __shared__ int status;   // thread 0: 0, the failing column's info value, or -1 (a wait gave up)
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     const int lane = threadIdx.x & 31;
     int *prog = sync + 1;
+    const uint32_t colv0 = tc::smem_u32(colv), bars0 = tc::smem_u32(bars);
+    if (threadIdx.x == 0) {  // column j brings kb - j entries into every CTA of the cluster
+        for (int j = 0; j < kb; ++j) tc::mbar_init(bars0 + 8u * j, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int j = 0; j < kb; ++j) tc::mbar_expect_tx(bars0 + 8u * j, (kb - j) * (uint32_t)sizeof(mlf<N>));
+    }
     if (rank == 0 && threadIdx.x == 0) {
         role[0] = atomicAdd(&sync[0], 1) - ticket0;
         role[1] = *(volatile int *)info;
     }
-    cluster.sync();
+    cluster.sync();  // also: every CTA's barriers are initialised before any remote store
     const int tk = *cluster.map_shared_rank(&role[0], 0);
     const int info0 = *cluster.map_shared_rank(&role[1], 0);
     cluster.sync();     // rank 0's words are read before any CTA of the cluster leaves
@@ -175,52 +221,60 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(PanelShape<C>::threa
     // ---------------------------------------------------------------- the diagonal block
     mlf<N> *Akk = A + col0 + (long long)col0 * lda;
     const bool signal = rank == 0 && (int)threadIdx.x >= PanelShape<C>::threads - 32;  // fills hist
-    const int q = (int)threadIdx.x * C + rank;
+    const int q = (int)threadIdx.x * C + rank;  // packed_col(i, t) of this thread's entry
     int t = 0;
     while (t + 1 < NB && NB * (t + 1) - (t + 1) * t / 2 <= q) ++t;
     const int i = t + (q - (NB * t - t * (t - 1) / 2));  // entry (i, t), t <= i
     const bool mine = (int)threadIdx.x < PanelShape<C>::per_cta && q < NB * (NB + 1) / 2 && i < kb;
     mlf<N> a = mine ? Akk[i + (long long)t * lda] : ml_zero<N>();
-    // publish v at the same shared-memory slot of every CTA in the cluster
-    auto publish = [&](mlf<N> *slot, const mlf<N> &v) {
+    // v into slot q of every CTA, completing bars[col] there
+    auto publish = [&](const mlf<N> &v, int col) {
 #pragma unroll
-        for (int r = 0; r < C; ++r) *cluster.map_shared_rank(slot, r) = v;
+        for (int r = 0; r < C; ++r)
+            st_async_ml<N>(cluster_addr(colv0 + q * (uint32_t)sizeof(PanelSlot<N>), r), v,
+                           cluster_addr(bars0 + 8u * col, r));
     };
-    if (mine && t == 0) publish(&col[0][i], a);
-    cluster.sync();
-    if (signal) {
-        if (lane < kb) hist[lane] = col[0][lane];
-        panel_progress(prog, base + 1);
-    }
-    mlf<N> c = ml_one<N>();  // carried by entry (0, 0) (rank 0, thread 0), idle after step 0
+    if (mine && t == 0) publish(a, 0);
+    // thread 0 of every CTA follows every column: it carries c_j and the status
+    const int steps = threadIdx.x == 0 ? kb : (mine ? t : 0);
+    mlf<N> c = ml_one<N>();
     int bad = 0;
-    for (int j = 0; j < kb; ++j) {
-        const mlf<N> p = col[j & 1][j];
+    for (int j = 0; j < steps; ++j) {
+        if (!tc::mbar_wait_acq_cluster(bars0 + 8u * j, 0, kPanelWaitCycles)) {
+            bad = -1;
+            break;
+        }
+        const mlf<N> p = colv[packed_col(j, j)].v;
         if (ml_sign(p) <= 0) {
             bad = col0 + j + 1;
             break;
         }
-        if (q == 0) {
-            publish(&cs[j], c);
+        if (threadIdx.x == 0) {
+            cs[j] = c;
             c = ml_mul(c, ml_ldexp(p, -p.e));
         }
-        if (mine && t > j) {
-            const mlf<N> u = ml_sub(ml_mul(p, a), ml_mul(col[j & 1][i], col[j & 1][t]));
+        if (mine && t > j) {  // (thread 0 runs every step for c_j; its own entry is in column 0)
+            const mlf<N> u = ml_sub(ml_mul(p, a), ml_mul(colv[packed_col(i, j)].v, colv[packed_col(t, j)].v));
             a = ml_ldexp(u, -p.e);
-            if (t == j + 1) publish(&col[(j + 1) & 1][i], a);
-        }
-        cluster.sync();
-        // column j + 1 is complete in col[(j + 1) & 1] and stays there until step j + 2
-        // writes it, after the next barrier, which this warp has not yet reached
-        if (signal && j + 2 < kb) {
-            if (lane > j && lane < kb) hist[(long long)(j + 1) * NB + lane] = col[(j + 1) & 1][lane];
-            panel_progress(prog, base + j + 2);
+            if (t == j + 1) publish(a, t);
         }
     }
+    if (signal) {  // hist column j as soon as it is here, behind the progress word
+        for (int j = 0; j + 1 < kb; ++j) {
+            if (!tc::mbar_wait_acq_cluster(bars0 + 8u * j, 0, kPanelWaitCycles)) break;
+            if (ml_sign(colv[packed_col(j, j)].v) <= 0) break;
+            if (lane >= j && lane < kb) hist[(long long)j * NB + lane] = colv[packed_col(lane, j)].v;
+            panel_progress(prog, base + j + 1);
+        }
+    }
+    if (threadIdx.x == 0) status = bad;
+    __syncthreads();
+    bad = status;
     if (!bad) {
-        if (mine && i == t) publish(&pv[t], a);
-        cluster.sync();
-        if ((int)threadIdx.x < kb) rs[threadIdx.x] = ml_rsqrt(ml_mul(cs[threadIdx.x], pv[threadIdx.x]));
+        if ((int)threadIdx.x < kb) {  // p_t is the diagonal entry of column t
+            const mlf<N> pt = colv[packed_col(threadIdx.x, threadIdx.x)].v;
+            rs[threadIdx.x] = ml_rsqrt(ml_mul(cs[threadIdx.x], pt));
+        }
         __syncthreads();
         if (mine) Akk[i + (long long)t * lda] = ml_mul(a, rs[t]);
         if (signal) {
@@ -228,10 +282,57 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(PanelShape<C>::threa
             panel_progress(prog, base + kPanelFinal);
         }
     } else {
-        if (q == 0) *info = bad;
+        if (rank == 0 && threadIdx.x == 0) {
+            if (bad > 0) {
+                *info = bad;
+            } else {
+                atomicCAS(info, 0, -1);
+                atomicExch(err, kPanelTimeout);
+            }
+        }
         if (signal) panel_progress(prog, base + kPanelAbort);
     }
     cluster.sync();  // no CTA leaves while another may still write its shared memory
+}
+
+// The previous panel's share of panel k0's update, on the CUDA cores (the look-ahead
+// product on the tensor cores has taken every earlier column):
+//     A[i][k0 + t] -= sum_{m < 32} L[i][kc + m] L[k0 + t][kc + m],  i in [k0, n), t < kb,
+// lower part of the diagonal block only.  Four threads per entry, eight terms each
+// (two partial sums), combined through shared memory: x runs down 32 consecutive rows
+// (L[i][kc + m] coalesced), y over four columns t (L[k0 + t][kc + m] is one address for a
+// whole warp), z over the quarters of m.  The multi-limb add and multiply have latencies
+// of several hundred cycles, so the short sums and the extra warps are what keep the
+// issue slots busy.
+constexpr int kUpdQuarters = 4;
+
+template <int N>
+__global__ void __launch_bounds__(32 * 4 * kUpdQuarters)
+    panel_update_kernel(mlf<N> *A, int lda, int n, int k0, int kb, int kc) {
+    __shared__ mlf<N> part[kUpdQuarters - 1][4][32];
+    const int x = threadIdx.x, y = threadIdx.y, z = threadIdx.z;
+    const int i = k0 + (int)blockIdx.x * 32 + x;
+    const int t = (int)blockIdx.y * 4 + y;
+    const bool live = i < n && t < kb && i - k0 >= t;
+    mlf<N> s0 = ml_zero<N>(), s1 = ml_zero<N>();
+    if (live) {
+        const int m0 = kc + z * (NB / kUpdQuarters);
+        const mlf<N> *Li = A + i + (long long)m0 * lda;       // L[i][m0 + m] at Li[m lda]
+        const mlf<N> *Lt = A + k0 + t + (long long)m0 * lda;  // L[k0 + t][m0 + m]
+#pragma unroll
+        for (int m = 0; m < NB / kUpdQuarters; m += 2) {
+            s0 = ml_add(s0, ml_mul(Li[(long long)m * lda], Lt[(long long)m * lda]));
+            s1 = ml_add(s1, ml_mul(Li[(long long)(m + 1) * lda], Lt[(long long)(m + 1) * lda]));
+        }
+        s0 = ml_add(s0, s1);
+        if (z > 0) part[z - 1][y][x] = s0;
+    }
+    __syncthreads();
+    if (live && z == 0) {
+        const mlf<N> r = ml_add(ml_add(s0, part[0][y][x]), ml_add(part[1][y][x], part[2][y][x]));
+        mlf<N> *c = A + i + (long long)(k0 + t) * lda;
+        *c = ml_sub(*c, r);
+    }
 }
 
 // strict lower triangle of an NB x NB block, packed column by column
@@ -461,11 +562,14 @@ GemmProblem<N> gemm_nn(int M, int Nn, int K, const mlf<N> &alpha, const mlf<N> *
 
 }  // namespace
 
-// Left-looking blocked Cholesky: before its diagonal block is factored, each 32-column
-// panel receives the contribution of every earlier panel in one GEMM,
-//     A[k0:, k0:k0+kb] -= L[k0:, :k0] L[k0:k0+kb, :k0]^T,
-// so the factorisation costs one exact (residue-path) product per panel whose output is
-// only the panel, not the whole trailing matrix.
+// Left-looking blocked Cholesky with look-ahead.  Panel k (columns k0 = 32k ..) needs
+//     A[k0:, k0:k0+kb] -= L[k0:, :k0] L[k0:k0+kb, :k0]^T
+// before it is factored.  The part from the columns of panels 0 .. k-2 is one exact
+// (residue-path) product on a side stream, issued as soon as panel k-2 is finished, so it
+// runs while panel k-1 is factored; only the previous panel's 32 columns are applied on
+// the critical path (panel_update_kernel), then the panel kernel factors panel k.  For
+// 256-bit factors of at least 128 rows the products read the residues of the finished
+// columns, converted once each (crt_cache_*).
 template <int N, int C, int R>
 void potrf_panels(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStream_t s) {
     SDPG_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
@@ -474,27 +578,29 @@ void potrf_panels(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStrea
     mlf<N> *hist = (mlf<N> *)ws.carve((NB * NB + NB) * sizeof(mlf<N>));
     SDPG_CUDA(cudaMemsetAsync(sync, 0, 2 * sizeof(int), s));
     int *err = ws.error ? ws.error : crt_error_word();
-    // the test hook that shortens the tensor-core waits shortens these too
+    // the test hook that shortens the tensor-core waits shortens the rows' waits too
     const long long budget = g_tc_wait_cycles > 0 ? g_tc_wait_cycles : kPanelWaitCycles;
     const mlf<N> mone = ml_from_int<N>(-1), one = ml_one<N>();
-    // 256-bit factors of at least 128 rows: the panel products read the residues of the
-    // finished columns, converted once each (crt_cache_*)
     const bool cached = crt_cache_applies<N>(n);
     CrtCache cache;
     if (cached) cache = crt_cache_init<N>(n, A, lda, ws.carve(crt_cache_bytes(n)), s);
+    const int panels = ceil_div(n, NB);
+    cudaStream_t h = nullptr;  // the side stream, forked from s after the set-up above
+    if (panels > 2) {
+        ws.ensure_side();
+        h = ws.side;
+        SDPG_CUDA(cudaEventRecord(ws.ev[0], s));
+        SDPG_CUDA(cudaStreamWaitEvent(h, ws.ev[0], 0));
+    }
     int ticket0 = 0;
-    for (int k0 = 0; k0 < n; k0 += NB) {
-        const int kb = min(NB, n - k0);
-        const int rows = n - k0 - kb;
-        mlf<N> *Akk = A + k0 + (long long)k0 * lda;
-        if (k0 > 0 && cached) {
-            crt_cache_panel<N>(cache, k0, kb, A, lda, ws.error, s);
-        } else if (k0 > 0) {
-            GemmProblem<N> p = gemm_nn<N>(n - k0, kb, k0, mone, A + k0, lda, 'N', A + k0, lda, 'T', one, Akk, lda);
-            p.lower_only = 1;
-            const size_t m2 = ws.used;
-            ml_gemm<N>(p, ws, s);
-            ws.used = m2;
+    for (int k = 0; k < panels; ++k) {
+        const int k0 = k * NB, kb = min(NB, n - k0), rows = n - k0 - kb;
+        if (k >= 2) SDPG_CUDA(cudaStreamWaitEvent(s, ws.ev[2 + (k & 1)], 0));  // product of panels < k-1
+        if (k >= 1) {
+            SDPG_KT_BEGIN(s);
+            panel_update_kernel<N><<<dim3(ceil_div(n - k0, 32), ceil_div(kb, 4)), dim3(32, 4, kUpdQuarters), 0, s>>>(
+                A, lda, n, k0, kb, k0 - NB);
+            SDPG_CHECK_LAUNCH_KT("panel_update_kernel", s);
         }
         const int clusters = 1 + ceil_div(rows, C * R);
         SDPG_KT_BEGIN(s);
@@ -502,7 +608,27 @@ void potrf_panels(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStrea
             A, lda, k0, kb, rows, info, hist, sync, 2 * k0, ticket0, budget, err);
         SDPG_CHECK_LAUNCH_KT("panel_factor_kernel", s);
         ticket0 += clusters;
-        if (cached && rows > 0) crt_cache_put<N>(cache, A, lda, k0, kb, ws.error, s);
+        if (k + 2 < panels) {  // panel k + 2's product with the columns of panels 0 .. k
+            SDPG_CUDA(cudaEventRecord(ws.ev[1], s));
+            SDPG_CUDA(cudaStreamWaitEvent(h, ws.ev[1], 0));
+            const int k2 = k0 + 2 * NB, kb2 = min(NB, n - k2), kend = k0 + NB;
+            if (cached) {
+                crt_cache_put<N>(cache, A, lda, k0, kb, ws.error, h);
+                crt_cache_panel<N>(cache, k2, kb2, kend, A, lda, ws.error, h);
+            } else {
+                GemmProblem<N> p = gemm_nn<N>(n - k2, kb2, kend, mone, A + k2, lda, 'N', A + k2, lda, 'T', one,
+                                              A + k2 + (long long)k2 * lda, lda);
+                p.lower_only = 1;
+                const size_t m2 = ws.used;
+                ml_gemm<N>(p, ws, h);
+                ws.used = m2;
+            }
+            SDPG_CUDA(cudaEventRecord(ws.ev[2 + ((k + 2) & 1)], h));
+        }
+    }
+    if (h) {  // join
+        SDPG_CUDA(cudaEventRecord(ws.ev[1], h));
+        SDPG_CUDA(cudaStreamWaitEvent(s, ws.ev[1], 0));
     }
     ws.used = mark;
 }

@@ -70,7 +70,24 @@ struct Workspace {
     // device word that tensor-core GEMMs run out of this workspace set when one of their
     // bounded waits gives up (null: only the device-wide flag of crt_error_word())
     int *error = nullptr;
-    ~Workspace() { release(); }
+    // side stream and events of the look-ahead Cholesky (ml_potrf), created on first use
+    // (a factorisation's first run is never inside a stream capture)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    Workspace() = default;
+    Workspace(const Workspace &) = delete;
+    Workspace &operator=(const Workspace &) = delete;
+    ~Workspace() {
+        release();
+        if (side) cudaStreamDestroy(side);
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    void ensure_side() {
+        if (side) return;
+        SDPG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        for (cudaEvent_t &e : ev) SDPG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
     void release() {
         if (base) {
             if (stream) cudaFreeAsync(base, stream);

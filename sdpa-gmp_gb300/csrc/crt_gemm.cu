@@ -846,7 +846,8 @@ void crt_cache_put(const CrtCache &c, const mlf<N> *A, long long lda, int k0, in
 }
 
 template <int N>
-void crt_cache_panel(const CrtCache &c, int k0, int kb, mlf<N> *A, long long lda, int *error, cudaStream_t s) {
+void crt_cache_panel(const CrtCache &c, int k0, int kb, int kend, mlf<N> *A, long long lda, int *error,
+                     cudaStream_t s) {
     if constexpr (N != 8) {
         throw sdpg_error(SDPG_ERR_ARG, "residue path is for 256-bit operands");
     } else {
@@ -863,22 +864,23 @@ void crt_cache_panel(const CrtCache &c, int k0, int kb, mlf<N> *A, long long lda
         t.a_rows = t.b_rows = c.rows;
         t.a_skip = t.b_skip = k0;
         t.kpitch = c.kpitch;
+        t.kext = kend;  // columns from kend on (not yet in the cache, or applied elsewhere) read as zero
         t.lower_only = 1;
         t.moduli = dev.moduli;
         t.error = error ? error : dev.error;
         t.sticky = dev.error;
-        const int Kpad = (int)round_up(k0, kTcBK);
+        const int Kpad = (int)round_up(kend, kTcBK);
         for (int q0 = 0; q0 < Kpad; q0 += kTcMaxK) {
             t.k0 = q0;
             t.Kpad = std::min(kTcMaxK, Kpad - q0);
             t.accumulate = q0 > 0;
-            t.alg_flops = 2.0 * kCrtL * (double)M * kb * std::min(kTcMaxK, k0 - q0);
+            t.alg_flops = 2.0 * kCrtL * (double)M * kb * std::min(kTcMaxK, kend - q0);
             tc_modgemm(t, s);
         }
         GemmProblem<N> p{};
         p.M = M;
         p.Nn = kb;
-        p.K = k0;
+        p.K = kend;
         p.batch = 1;
         p.C = A + k0 + (long long)k0 * lda;
         p.ldc = lda;
@@ -899,8 +901,8 @@ template CrtCache crt_cache_init<8>(int, const mlf<8> *, long long, void *, cuda
 template CrtCache crt_cache_init<16>(int, const mlf<16> *, long long, void *, cudaStream_t);
 template void crt_cache_put<8>(const CrtCache &, const mlf<8> *, long long, int, int, int *, cudaStream_t);
 template void crt_cache_put<16>(const CrtCache &, const mlf<16> *, long long, int, int, int *, cudaStream_t);
-template void crt_cache_panel<8>(const CrtCache &, int, int, mlf<8> *, long long, int *, cudaStream_t);
-template void crt_cache_panel<16>(const CrtCache &, int, int, mlf<16> *, long long, int *, cudaStream_t);
+template void crt_cache_panel<8>(const CrtCache &, int, int, int, mlf<8> *, long long, int *, cudaStream_t);
+template void crt_cache_panel<16>(const CrtCache &, int, int, int, mlf<16> *, long long, int *, cudaStream_t);
 
 // device-wide sticky word: set by every tensor-core kernel that gave up a bounded wait
 int *crt_error_word() { return crt_device().error; }

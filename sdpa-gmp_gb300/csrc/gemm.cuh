@@ -115,10 +115,11 @@ CrtCache crt_cache_init(int n, const mlf<N> *A, long long lda, void *mem, cudaSt
 // block's upper part read as zero)
 template <int N>
 void crt_cache_put(const CrtCache &c, const mlf<N> *A, long long lda, int k0, int kb, int *error, cudaStream_t s);
-// A[k0:n, k0:k0+kb] -= L[k0:n, :k0] L[k0:k0+kb, :k0]^T (lower part of the top block) from
-// the cached residues
+// A[k0:n, k0:k0+kb] -= L[k0:n, :kend] L[k0:k0+kb, :kend]^T (lower part of the top block)
+// from the cached residues of columns 0 .. kend - 1 (kend <= k0; later columns are not read)
 template <int N>
-void crt_cache_panel(const CrtCache &c, int k0, int kb, mlf<N> *A, long long lda, int *error, cudaStream_t s);
+void crt_cache_panel(const CrtCache &c, int k0, int kb, int kend, mlf<N> *A, long long lda, int *error,
+                     cudaStream_t s);
 
 // Device-wide sticky flag: set (and never cleared) when any tensor-core kernel on the
 // current device gave up a bounded wait, in addition to the product's own error word.

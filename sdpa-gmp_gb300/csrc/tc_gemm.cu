@@ -220,11 +220,12 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// 2D fp16 map over `rows` rows of `cols` (contiguous) elements, box 64 x 128, 128-byte swizzle
-CUtensorMap make_map(const __half *base, long long rows, int cols) {
+// 2D fp16 map over `rows` rows of `cols` elements (rows `pitch` elements apart), box
+// 64 x 128, 128-byte swizzle; a box reaching past column `cols` reads zeros there
+CUtensorMap make_map(const __half *base, long long rows, int cols, int pitch) {
     CUtensorMap m;
     const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch * 2};
     const cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)kTcBM};
     const cuuint32_t estr[2] = {1, 1};
     const CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, (void *)base, dims, strides, box, estr,
@@ -240,7 +241,8 @@ long long g_tc_wait_cycles = 0;
 
 void tc_modgemm(const TcModGemm &p, cudaStream_t s) {
     if (p.Mpad % kTcBM || p.Npad % kTcBN || p.Kpad % kTcBK || p.Kpad <= 0 || p.Kpad > kTcMaxK || p.L <= 0 ||
-        p.batch <= 0 || p.k0 % kTcBK || p.k0 < 0 || p.kpitch % kTcBK || p.k0 + p.Kpad > p.kpitch)
+        p.batch <= 0 || p.k0 % kTcBK || p.k0 < 0 || p.kpitch % kTcBK || p.k0 + p.Kpad > p.kpitch || p.kext < 0 ||
+        p.kext > p.kpitch)
         throw sdpg_error(SDPG_ERR_ARG, "tc_modgemm: unsupported shape");
     if (((uintptr_t)p.A | (uintptr_t)p.B | (uintptr_t)p.Y) & 15)
         throw sdpg_error(SDPG_ERR_ARG, "tc_modgemm: operands must be 16-byte aligned");
@@ -256,8 +258,9 @@ void tc_modgemm(const TcModGemm &p, cudaStream_t s) {
     // plane's end reads the fill value there)
     const long long arows = (long long)(p.a_batched ? p.batch : 1) * p.L * q.a_rows - p.a_skip;
     const long long brows = (long long)(p.b_batched ? p.batch : 1) * p.L * q.b_rows - p.b_skip;
-    const CUtensorMap ma = make_map(p.A, arows, p.kpitch);
-    const CUtensorMap mb = make_map(p.B, brows, p.kpitch);
+    const int kext = p.kext > 0 ? p.kext : p.kpitch;
+    const CUtensorMap ma = make_map(p.A, arows, kext, p.kpitch);
+    const CUtensorMap mb = make_map(p.B, brows, kext, p.kpitch);
     dim3 grid(p.Npad / kTcBN, p.Mpad / kTcBM, p.batch * p.L);
     q.wait_cycles = g_tc_wait_cycles > 0 ? g_tc_wait_cycles : kWaitCycles;
     SDPG_KT_BEGIN(s);

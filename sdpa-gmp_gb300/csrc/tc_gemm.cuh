@@ -35,6 +35,7 @@ struct TcModGemm {
                            // into a plane store whose planes are a_rows / b_rows apart)
     int k0;                // first K index of this call within the planes (a multiple of 64)
     int kpitch;            // K extent of the planes (their row length)
+    int kext;              // columns the maps may read (0: kpitch); from kext on they read as zero
     int accumulate;        // 1: Y = (Y + new) mod m (a later K chunk of the same product)
     int lower_only;        // 1: skip tiles strictly above the diagonal (their Y is not written)
     const int *moduli;     // device, L entries
