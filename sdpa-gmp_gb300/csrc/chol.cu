@@ -298,41 +298,181 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(PanelShape<C>::threa
 // The previous panel's share of panel k0's update, on the CUDA cores (the look-ahead
 // product on the tensor cores has taken every earlier column):
 //     A[i][k0 + t] -= sum_{m < 32} L[i][kc + m] L[k0 + t][kc + m],  i in [k0, n), t < kb,
-// lower part of the diagonal block only.  Four threads per entry, eight terms each
-// (two partial sums), combined through shared memory: x runs down 32 consecutive rows
-// (L[i][kc + m] coalesced), y over four columns t (L[k0 + t][kc + m] is one address for a
-// whole warp), z over the quarters of m.  The multi-limb add and multiply have latencies
-// of several hundred cycles, so the short sums and the extra warps are what keep the
-// issue slots busy.
-constexpr int kUpdQuarters = 4;
+// lower part of the diagonal block only.
+//
+// Block floating point: each row's 32 values become signed fixed-point fractions
+// x 2^-E_row (E_row the row's largest exponent) held as D digits of 28 bits, so a term is
+// 64 (N = 8) digit products accumulated exactly in 64-bit columns, with no per-term
+// normalisation; the columns below the top D + 1 are dropped and the sum is rounded to
+// N limbs once.  The truncation is relative to 2^(E_i + E_t), about 2^-270 of
+// sqrt(A_ii A_tt) for a Cholesky factor: the form of the factorisation's backward error.
+//
+// CTA: 32 rows i (lane) x 8 columns t (warp).  Its rows' digits go to shared memory as
+// [m][digit][row] (a warp's 32 lanes read 32 consecutive words), the columns' as
+// [t][m][digit] (one address per warp).
+template <int N>
+struct BfpShape {
+    using G = MulDigits<N>;
+    static constexpr int D = G::D;              // digits per value
+    static constexpr int CK = G::CK;            // lowest product column kept
+    static constexpr int NC = 2 * D - 1 - CK + 2;  // kept columns plus two for carries
+    static constexpr int LW = (28 * NC + 31) / 32;
+    static constexpr int EVERY = N <= 8 ? 8 : 4;   // terms between carry passes (no int64 overflow)
+    static constexpr size_t smem = (size_t)(32 * 32 + 8 * 32) * D * sizeof(int32_t);
+};
+static_assert(8 * 10 * (1ll << 56) / 8 < (1ll << 62) && BfpShape<16>::EVERY * 19 <= 119, "column sums fit int64");
+
+// x 2^-E as D signed digits of 28 bits (x's sign on every digit); E >= x.e
+template <int N>
+MLHD void bfp_digits(const mlf<N> &x, int E, int32_t (&d)[BfpShape<N>::D]) {
+    constexpr int D = BfpShape<N>::D, L = N + 1;
+    constexpr int up = 28 * D - 32 * N;  // the mantissa's place in the 28 D-bit fraction
+    static_assert(up > 0 && up < 32, "digit frame");
+    uint32_t a[L];
+    a[0] = x.m[0] << up;
+#pragma unroll
+    for (int k = 1; k < N; ++k) a[k] = (x.m[k] << up) | (x.m[k - 1] >> (32 - up));
+    a[N] = x.m[N - 1] >> (32 - up);
+    const int delta = E - x.e;
+    const bool zero = x.m[N - 1] == 0u || delta >= 32 * L;
+    ml_limb_shr<L>(a, zero ? 0 : (delta >> 5));
+    ml_bit_shr<L>(a, zero ? 0 : (delta & 31));
+#pragma unroll
+    for (int p = 0; p < D; ++p) {
+        const int bit = 28 * p, w = bit >> 5, r = bit & 31;
+        const uint32_t lo = a[w] >> r;
+        const uint32_t hi = (r > 4 && w + 1 < L) ? (a[w + 1] << (32 - r)) : 0u;
+        const int32_t v = zero ? 0 : (int32_t)((lo | hi) & 0x0FFFFFFFu);
+        d[p] = x.s ? -v : v;
+    }
+}
+
+// signed carry pass: columns 0 .. NC-2 into [0, 2^28), the top one keeps the sign
+template <int NC>
+MLHD void bfp_carry(long long (&acc)[NC]) {
+#pragma unroll
+    for (int c = 0; c + 1 < NC; ++c) {
+        const long long carry = acc[c] >> 28;
+        acc[c] -= carry << 28;
+        acc[c + 1] += carry;
+    }
+}
+
+// acc (columns CK .. of the products) += a b, digits of two fixed-point fractions
+template <int N>
+MLHD void bfp_term(long long (&acc)[BfpShape<N>::NC], const int32_t (&a)[BfpShape<N>::D],
+                   const int32_t (&b)[BfpShape<N>::D]) {
+    constexpr int D = BfpShape<N>::D, CK = BfpShape<N>::CK;
+#ifdef __CUDA_ARCH__
+#pragma unroll
+#endif
+    for (int c = CK; c <= 2 * D - 2; ++c) {
+#ifdef __CUDA_ARCH__
+#pragma unroll
+#endif
+        for (int p = 0; p < D; ++p) {
+            const int q = c - p;
+            if (q >= 0 && q < D) acc[c - CK] += (long long)a[p] * b[q];
+        }
+    }
+}
+
+// the sum held in acc (fractions x 2^-Er and y 2^-Ey) rounded to N limbs; kNone exponents
+// mean an all-zero row
+constexpr int kBfpNone = -(1 << 30);
+template <int N>
+MLHD mlf<N> bfp_result(long long (&acc)[BfpShape<N>::NC], int Er, int Ey) {
+    using B = BfpShape<N>;
+    constexpr int D = B::D, CK = B::CK, NC = B::NC;
+    bfp_carry<NC>(acc);
+    const bool neg = acc[NC - 1] < 0;
+    if (neg) {
+        for (int c = 0; c < NC; ++c) acc[c] = -acc[c];
+        bfp_carry<NC>(acc);
+    }
+    uint32_t W[B::LW];
+    for (int w = 0; w < B::LW; ++w) W[w] = 0;
+    for (int c = 0; c < NC; ++c) {  // every column is below 2^28 here
+        const int bit = 28 * c, w = bit >> 5, r = bit & 31;
+        const unsigned long long v = (unsigned long long)acc[c] << r;
+        W[w] |= (uint32_t)v;
+        if (w + 1 < B::LW) W[w + 1] |= (uint32_t)(v >> 32);
+    }
+    // the sum is W 2^(28 CK - 56 D) 2^(Er + Ey)
+    const long long e_top = (long long)Er + Ey + 28 * CK - 56 * D + 32 * B::LW;
+    if (Er == kBfpNone || Ey == kBfpNone) return ml_zero<N>();
+    return ml_pack<N, B::LW>(W, (int)e_top, neg ? 1u : 0u);
+}
 
 template <int N>
-__global__ void __launch_bounds__(32 * 4 * kUpdQuarters)
-    panel_update_kernel(mlf<N> *A, int lda, int n, int k0, int kb, int kc) {
-    __shared__ mlf<N> part[kUpdQuarters - 1][4][32];
-    const int x = threadIdx.x, y = threadIdx.y, z = threadIdx.z;
-    const int i = k0 + (int)blockIdx.x * 32 + x;
-    const int t = (int)blockIdx.y * 4 + y;
-    const bool live = i < n && t < kb && i - k0 >= t;
-    mlf<N> s0 = ml_zero<N>(), s1 = ml_zero<N>();
-    if (live) {
-        const int m0 = kc + z * (NB / kUpdQuarters);
-        const mlf<N> *Li = A + i + (long long)m0 * lda;       // L[i][m0 + m] at Li[m lda]
-        const mlf<N> *Lt = A + k0 + t + (long long)m0 * lda;  // L[k0 + t][m0 + m]
+__global__ void __launch_bounds__(256) panel_update_kernel(mlf<N> *A, int lda, int n, int k0, int kb, int kc) {
+    using B = BfpShape<N>;
+    constexpr int D = B::D, NC = B::NC;
+    extern __shared__ int32_t bfp_sm[];
+    int32_t *di = bfp_sm;                // rows:    di[(m * D + p) * 32 + r]
+    int32_t *dt = bfp_sm + 32 * 32 * D;  // columns: dt[(w * 32 + m) * D + p]
+    __shared__ int emax[8][32];          // partial row maxima, then E_r in emax[0]
+    __shared__ int et[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int i0 = k0 + (int)blockIdx.x * 32, t0 = (int)blockIdx.y * 8;
+    constexpr int kNone = kBfpNone;
+    // rows: lane = row, warp w takes m = 4w .. 4w + 3
+    const int ri = i0 + lane;
+    mlf<N> xv[4];
 #pragma unroll
-        for (int m = 0; m < NB / kUpdQuarters; m += 2) {
-            s0 = ml_add(s0, ml_mul(Li[(long long)m * lda], Lt[(long long)m * lda]));
-            s1 = ml_add(s1, ml_mul(Li[(long long)(m + 1) * lda], Lt[(long long)(m + 1) * lda]));
+    for (int k = 0; k < 4; ++k) {
+        const int m = 4 * warp + k;
+        xv[k] = ri < n ? A[ri + (long long)(kc + m) * lda] : ml_zero<N>();
+    }
+    int e = kNone;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) e = xv[k].m[N - 1] ? max(e, xv[k].e) : e;
+    emax[warp][lane] = e;
+    // columns: warp w = column t0 + w, lane = m
+    const int tw = t0 + warp;
+    const mlf<N> yv = tw < kb ? A[k0 + tw + (long long)(kc + lane) * lda] : ml_zero<N>();
+    int ey = yv.m[N - 1] ? yv.e : kNone;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ey = max(ey, __shfl_xor_sync(0xffffffffu, ey, o));
+    if (lane == 0) et[warp] = ey;
+    __syncthreads();
+    int Er = emax[0][lane];
+#pragma unroll
+    for (int w = 1; w < 8; ++w) Er = max(Er, emax[w][lane]);
+    const int Ey = et[warp];
+    {
+        int32_t d[D];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            bfp_digits<N>(xv[k], Er, d);
+            const int m = 4 * warp + k;
+#pragma unroll
+            for (int p = 0; p < D; ++p) di[(m * D + p) * 32 + lane] = d[p];
         }
-        s0 = ml_add(s0, s1);
-        if (z > 0) part[z - 1][y][x] = s0;
+        bfp_digits<N>(yv, Ey, d);
+#pragma unroll
+        for (int p = 0; p < D; ++p) dt[(warp * 32 + lane) * D + p] = d[p];
     }
     __syncthreads();
-    if (live && z == 0) {
-        const mlf<N> r = ml_add(ml_add(s0, part[0][y][x]), ml_add(part[1][y][x], part[2][y][x]));
-        mlf<N> *c = A + i + (long long)(k0 + t) * lda;
-        *c = ml_sub(*c, r);
+    // entry (i0 + lane, t0 + warp)
+    const int i = i0 + lane, t = tw;
+    if (i >= n || t >= kb || i - k0 < t) return;
+    long long acc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[c] = 0;
+    for (int m = 0; m < NB; ++m) {
+        int32_t a[D], b[D];
+#pragma unroll
+        for (int p = 0; p < D; ++p) {
+            a[p] = di[(m * D + p) * 32 + lane];
+            b[p] = dt[(warp * 32 + m) * D + p];
+        }
+        bfp_term<N>(acc, a, b);
+        if (m % B::EVERY == B::EVERY - 1) bfp_carry<NC>(acc);
     }
+    const mlf<N> dot = bfp_result<N>(acc, Er, Ey);
+    mlf<N> *cp = A + i + (long long)(k0 + t) * lda;
+    *cp = ml_sub(*cp, dot);
 }
 
 // strict lower triangle of an NB x NB block, packed column by column
@@ -585,6 +725,12 @@ void potrf_panels(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStrea
     CrtCache cache;
     if (cached) cache = crt_cache_init<N>(n, A, lda, ws.carve(crt_cache_bytes(n)), s);
     const int panels = ceil_div(n, NB);
+    static bool attr_set = false;  // dynamic shared memory of the update kernel (97 KB at N = 16)
+    if (!attr_set) {
+        SDPG_CUDA(cudaFuncSetAttribute(panel_update_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)BfpShape<N>::smem));
+        attr_set = true;
+    }
     cudaStream_t h = nullptr;  // the side stream, forked from s after the set-up above
     if (panels > 2) {
         ws.ensure_side();
@@ -598,7 +744,7 @@ void potrf_panels(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStrea
         if (k >= 2) SDPG_CUDA(cudaStreamWaitEvent(s, ws.ev[2 + (k & 1)], 0));  // product of panels < k-1
         if (k >= 1) {
             SDPG_KT_BEGIN(s);
-            panel_update_kernel<N><<<dim3(ceil_div(n - k0, 32), ceil_div(kb, 4)), dim3(32, 4, kUpdQuarters), 0, s>>>(
+            panel_update_kernel<N><<<dim3(ceil_div(n - k0, 32), ceil_div(kb, 8)), 256, BfpShape<N>::smem, s>>>(
                 A, lda, n, k0, kb, k0 - NB);
             SDPG_CHECK_LAUNCH_KT("panel_update_kernel", s);
         }
