@@ -37,6 +37,10 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# Hardware work queues for the solver's streams (four per solve, 64 and more with
+# concurrent batched solves); read by CUDA when the context is created, so set before
+# any CUDA call.  The default of 8 makes unrelated streams wait on one another.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "256-bit IPM iters/s (gpp n=500 m=501)"
 UNIT = "iters/s"
@@ -510,6 +514,7 @@ def bench_batch(args) -> None:
     gen_s = time.perf_counter() - t0
     param = sdpg.Param.default()
     param.precision = args.precision
+    sdpg.set_gemm_method(args.gemm_method)
     # warm-up: one small solve (library set-up, tensor-core tables)
     if mine:
         sdpg.solve_batch([probs[mine[0]]], param, device=local, concurrency=1)
@@ -636,8 +641,9 @@ def main():
     ap.add_argument("--kernel", choices=["gemm"], default=None,
                     help="kernel mode: time repeated multi-limb GEMMs instead of IPM iterations")
     ap.add_argument("--gemm-n", type=int, default=500)
-    ap.add_argument("--gemm-method", type=int, default=0, choices=[0, 1],
-                    help="kernel mode: 0 tensor-core residue path (256-bit), 1 integer digit GEMM")
+    ap.add_argument("--gemm-method", type=int, default=0, choices=[0, 1, 2],
+                    help="GEMM method (kernel and batch modes): 0 tensor-core residue path where it applies "
+                         "(default), 1 integer digit GEMM, 2 residue path for every 256-bit product")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)

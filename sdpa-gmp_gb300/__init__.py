@@ -17,6 +17,10 @@ import numpy as np
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "libsdpg.so")
 
+# A solve keeps four streams busy (batched solves many more); CUDA reads this when the
+# context is created, so it only takes effect if nothing in the process has used CUDA yet.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_SQRT = 0, 1, 2, 3, 4
 
 
