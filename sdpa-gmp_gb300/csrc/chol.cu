@@ -318,7 +318,8 @@ struct BfpShape {
     static constexpr int NC = 2 * D - 1 - CK + 2;  // kept columns plus two for carries
     static constexpr int LW = (28 * NC + 31) / 32;
     static constexpr int EVERY = N <= 8 ? 8 : 4;   // terms between carry passes (no int64 overflow)
-    static constexpr size_t smem = (size_t)(32 * 32 + 8 * 32) * D * sizeof(int32_t);
+    // update kernel: digits of 32 rows and 8 columns, then the second half-sums
+    static constexpr size_t smem = (size_t)(32 * 32 + 8 * 32) * D * sizeof(int32_t) + (size_t)NC * 8 * 32 * 8;
 };
 static_assert(8 * 10 * (1ll << 56) / 8 < (1ll << 62) && BfpShape<16>::EVERY * 19 <= 119, "column sums fit int64");
 
@@ -404,72 +405,91 @@ MLHD mlf<N> bfp_result(long long (&acc)[BfpShape<N>::NC], int Er, int Ey) {
     return ml_pack<N, B::LW>(W, (int)e_top, neg ? 1u : 0u);
 }
 
+// CTA: 32 rows i (lane) x 8 columns t, two warps per column, each summing 16 of the 32
+// terms; the second adds its exact column sums to the first's through shared memory.
 template <int N>
-__global__ void __launch_bounds__(256) panel_update_kernel(mlf<N> *A, int lda, int n, int k0, int kb, int kc) {
+__global__ void __launch_bounds__(512) panel_update_kernel(mlf<N> *A, int lda, int n, int k0, int kb, int kc) {
     using B = BfpShape<N>;
     constexpr int D = B::D, NC = B::NC;
     extern __shared__ int32_t bfp_sm[];
     int32_t *di = bfp_sm;                // rows:    di[(m * D + p) * 32 + r]
     int32_t *dt = bfp_sm + 32 * 32 * D;  // columns: dt[(w * 32 + m) * D + p]
-    __shared__ int emax[8][32];          // partial row maxima, then E_r in emax[0]
+    long long *part = reinterpret_cast<long long *>(bfp_sm + (32 * 32 + 8 * 32) * D);  // [c][t][r]
+    __shared__ int emax[16][32];  // partial row maxima
     __shared__ int et[8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int i0 = k0 + (int)blockIdx.x * 32, t0 = (int)blockIdx.y * 8;
     constexpr int kNone = kBfpNone;
-    // rows: lane = row, warp w takes m = 4w .. 4w + 3
+    // rows: lane = row, warp w takes m = 2w, 2w + 1
     const int ri = i0 + lane;
-    mlf<N> xv[4];
+    mlf<N> xv[2];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int m = 4 * warp + k;
+    for (int k = 0; k < 2; ++k) {
+        const int m = 2 * warp + k;
         xv[k] = ri < n ? A[ri + (long long)(kc + m) * lda] : ml_zero<N>();
     }
     int e = kNone;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) e = xv[k].m[N - 1] ? max(e, xv[k].e) : e;
+    for (int k = 0; k < 2; ++k) e = xv[k].m[N - 1] ? max(e, xv[k].e) : e;
     emax[warp][lane] = e;
-    // columns: warp w = column t0 + w, lane = m
-    const int tw = t0 + warp;
-    const mlf<N> yv = tw < kb ? A[k0 + tw + (long long)(kc + lane) * lda] : ml_zero<N>();
-    int ey = yv.m[N - 1] ? yv.e : kNone;
+    // columns: warp w < 8 reads column t0 + w, lane = m
+    const int tw = t0 + (warp & 7);
+    mlf<N> yv = ml_zero<N>();
+    if (warp < 8) {
+        yv = tw < kb ? A[k0 + tw + (long long)(kc + lane) * lda] : ml_zero<N>();
+        int ey = yv.m[N - 1] ? yv.e : kNone;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) ey = max(ey, __shfl_xor_sync(0xffffffffu, ey, o));
-    if (lane == 0) et[warp] = ey;
+        for (int o = 16; o > 0; o >>= 1) ey = max(ey, __shfl_xor_sync(0xffffffffu, ey, o));
+        if (lane == 0) et[warp] = ey;
+    }
     __syncthreads();
     int Er = emax[0][lane];
 #pragma unroll
-    for (int w = 1; w < 8; ++w) Er = max(Er, emax[w][lane]);
-    const int Ey = et[warp];
+    for (int w = 1; w < 16; ++w) Er = max(Er, emax[w][lane]);
+    const int Ey = et[warp & 7];
     {
         int32_t d[D];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < 2; ++k) {
             bfp_digits<N>(xv[k], Er, d);
-            const int m = 4 * warp + k;
+            const int m = 2 * warp + k;
 #pragma unroll
             for (int p = 0; p < D; ++p) di[(m * D + p) * 32 + lane] = d[p];
         }
-        bfp_digits<N>(yv, Ey, d);
+        if (warp < 8) {
+            bfp_digits<N>(yv, Ey, d);
 #pragma unroll
-        for (int p = 0; p < D; ++p) dt[(warp * 32 + lane) * D + p] = d[p];
+            for (int p = 0; p < D; ++p) dt[(warp * 32 + lane) * D + p] = d[p];
+        }
     }
     __syncthreads();
-    // entry (i0 + lane, t0 + warp)
-    const int i = i0 + lane, t = tw;
-    if (i >= n || t >= kb || i - k0 < t) return;
+    // entry (i0 + lane, t0 + tl); this warp's half of the terms
+    const int tl = warp & 7, half = warp >> 3;
+    const int i = i0 + lane, t = t0 + tl;
+    const bool live = i < n && t < kb && i - k0 >= t;
     long long acc[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) acc[c] = 0;
-    for (int m = 0; m < NB; ++m) {
-        int32_t a[D], b[D];
+    if (live) {
+        for (int m = half * (NB / 2); m < (half + 1) * (NB / 2); ++m) {
+            int32_t a[D], b[D];
 #pragma unroll
-        for (int p = 0; p < D; ++p) {
-            a[p] = di[(m * D + p) * 32 + lane];
-            b[p] = dt[(warp * 32 + m) * D + p];
+            for (int p = 0; p < D; ++p) {
+                a[p] = di[(m * D + p) * 32 + lane];
+                b[p] = dt[(tl * 32 + m) * D + p];
+            }
+            bfp_term<N>(acc, a, b);
+            if (m % B::EVERY == B::EVERY - 1) bfp_carry<NC>(acc);
         }
-        bfp_term<N>(acc, a, b);
-        if (m % B::EVERY == B::EVERY - 1) bfp_carry<NC>(acc);
+        if (half) {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) part[(c * 8 + tl) * 32 + lane] = acc[c];
+        }
     }
+    __syncthreads();
+    if (!live || half) return;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[c] += part[(c * 8 + tl) * 32 + lane];  // both halves carried: no overflow
     const mlf<N> dot = bfp_result<N>(acc, Er, Ey);
     mlf<N> *cp = A + i + (long long)(k0 + t) * lda;
     *cp = ml_sub(*cp, dot);
@@ -744,7 +764,7 @@ void potrf_panels(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStrea
         if (k >= 2) SDPG_CUDA(cudaStreamWaitEvent(s, ws.ev[2 + (k & 1)], 0));  // product of panels < k-1
         if (k >= 1) {
             SDPG_KT_BEGIN(s);
-            panel_update_kernel<N><<<dim3(ceil_div(n - k0, 32), ceil_div(kb, 8)), 256, BfpShape<N>::smem, s>>>(
+            panel_update_kernel<N><<<dim3(ceil_div(n - k0, 32), ceil_div(kb, 8)), 512, BfpShape<N>::smem, s>>>(
                 A, lda, n, k0, kb, k0 - NB);
             SDPG_CHECK_LAUNCH_KT("panel_update_kernel", s);
         }

@@ -801,10 +801,10 @@ class Solver final : public SolverBase {
 
     // One Lanczos run (Lal::getMinEigen, sdpa_linear.cpp:27-124) on L Xm L^T for one block
     // and side.  The steps and the loop test run on the device (k_lanczos_step); the host
-    // enqueues a few steps ahead and reads the loop flags once per batch.
+    // enqueues every step the run can take and reads the result once.
     struct Lz {
         Blk *B;
-        int side, n, k, kgo;
+        int side, n, kgo;
         V *L, *Xm, *Lt;
         cudaStream_t st;
         Workspace *ws;
@@ -813,9 +813,8 @@ class Solver final : public SolverBase {
         std::vector<int> eig;  // steps with a tridiagonal eigenvalue solve
         bool active;
     };
-    static constexpr int kLanczosBatch = 4;
 
-    // all runs advance together: one host synchronisation per batch of steps for all of them
+    // all runs at once: one host synchronisation for all of them
     void lanczos_all(std::vector<Lz> &T) {
         if (16 * T.size() > (size_t)kPinned - 8) throw sdpg_error(SDPG_ERR_TOO_LARGE, "too many Lanczos runs at once");
         for (size_t i = 0; i < T.size(); ++i) {
@@ -856,7 +855,6 @@ class Solver final : public SolverBase {
                 t.eig[k] = (R(kk) >= rsqrt_(R(k)) || k == t.n - 1 || R(k) > sq_n9) ? 1 : 0;
                 if (t.eig[k]) kk = 0;
             }
-            t.k = 0;
             t.active = t.n > 0 && kmax > 1;
         }
         // (the pinned slots are next written by stream-ordered copies, after the uploads)
@@ -889,38 +887,6 @@ class Solver final : public SolverBase {
                     k_lanczos_step<N>(t.n, B.Mop[s], B.r[s], B.q[s], B.qold[s], B.w[s], B.td[s], B.te[s], B.sl[s],
                                       B.lzctl[s], status_, k, t.eig[k], t.kgo, B.lanczos_kmax, t.st);
             });
-        }
-    }
-
-    // step-by-step launches: the host enqueues a few steps ahead and reads the loop flags
-    // once per batch
-    void lanczos_stepwise(std::vector<Lz> &T) {
-        while (true) {
-            bool any = false;
-            for (Lz &t : T) {
-                if (!t.active) continue;
-                Blk &B = *t.B;
-                const int s = t.side;
-                for (int b = 0; b < kLanczosBatch; ++b) {
-                    const int k = t.k + b;
-                    if (k >= t.n || k + 1 >= B.lanczos_kmax) break;
-                    k_lanczos_step<N>(t.n, B.Mop[s], B.r[s], B.q[s], B.qold[s], B.w[s], B.td[s], B.te[s], B.sl[s],
-                                      B.lzctl[s], status_, k, t.eig[k], t.kgo, B.lanczos_kmax, t.st);
-                }
-                int *flags = reinterpret_cast<int *>(t.hp + 12);
-                d2h_ += 2 * (long long)sizeof(int);
-                SDPG_CUDA(cudaMemcpyAsync(flags, B.lzctl[s], 2 * sizeof(int), cudaMemcpyDeviceToHost, t.st));
-                any = true;
-            }
-            if (!any) break;
-            SDPG_CUDA(cudaStreamSynchronize(st_));
-            SDPG_CUDA(cudaStreamSynchronize(st2_));
-            for (Lz &t : T) {
-                if (!t.active) continue;
-                const int *flags = reinterpret_cast<const int *>(t.hp + 12);
-                t.k = flags[1];
-                if (!flags[0] || t.k >= t.n || t.k + 1 >= t.B->lanczos_kmax) t.active = false;
-            }
         }
     }
 

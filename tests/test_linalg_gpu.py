@@ -59,7 +59,7 @@ def _spd(exact, n, limbs, rng):
 
 
 @gpu
-@pytest.mark.parametrize("limbs,n", [(8, 1), (8, 5), (8, 32), (8, 33), (8, 97), (16, 40)])
+@pytest.mark.parametrize("limbs,n", [(8, 1), (8, 5), (8, 32), (8, 33), (8, 97), (16, 40), (16, 97)])
 def test_rpotrf_residual(sdpg, exact, limbs, n):
     rng = random.Random(1000 * limbs + n)
     A = _spd(exact, n, limbs, rng)
