@@ -310,6 +310,9 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(PanelShape<C>::threa
 // CTA: 32 rows i (lane) x 8 columns t (warp).  Its rows' digits go to shared memory as
 // [m][digit][row] (a warp's 32 lanes read 32 consecutive words), the columns' as
 // [t][m][digit] (one address per warp).
+constexpr int kUpdCols = 4;  // columns t per CTA of the update kernel (two warps each)
+constexpr int kUpdWarps = 2 * kUpdCols;
+
 template <int N>
 struct BfpShape {
     using G = MulDigits<N>;
@@ -318,8 +321,9 @@ struct BfpShape {
     static constexpr int NC = 2 * D - 1 - CK + 2;  // kept columns plus two for carries
     static constexpr int LW = (28 * NC + 31) / 32;
     static constexpr int EVERY = N <= 8 ? 8 : 4;   // terms between carry passes (no int64 overflow)
-    // update kernel: digits of 32 rows and 8 columns, then the second half-sums
-    static constexpr size_t smem = (size_t)(32 * 32 + 8 * 32) * D * sizeof(int32_t) + (size_t)NC * 8 * 32 * 8;
+    // update kernel: digits of 32 rows and kUpdCols columns, then the second half-sums
+    static constexpr size_t smem =
+        (size_t)(32 + kUpdCols) * 32 * D * sizeof(int32_t) + (size_t)NC * kUpdCols * 32 * sizeof(long long);
 };
 static_assert(8 * 10 * (1ll << 56) / 8 < (1ll << 62) && BfpShape<16>::EVERY * 19 <= 119, "column sums fit int64");
 
@@ -405,37 +409,41 @@ MLHD mlf<N> bfp_result(long long (&acc)[BfpShape<N>::NC], int Er, int Ey) {
     return ml_pack<N, B::LW>(W, (int)e_top, neg ? 1u : 0u);
 }
 
-// CTA: 32 rows i (lane) x 8 columns t, two warps per column, each summing 16 of the 32
-// terms; the second adds its exact column sums to the first's through shared memory.
+// CTA: 32 rows i (lane) x kUpdCols columns t, two warps per column, each summing 16 of
+// the 32 terms; the second adds its exact column sums to the first's through shared
+// memory.  Few columns per CTA spread the integer multiply-adds over many SMs.
+
 template <int N>
-__global__ void __launch_bounds__(512) panel_update_kernel(mlf<N> *A, int lda, int n, int k0, int kb, int kc) {
+__global__ void __launch_bounds__(32 * kUpdWarps) panel_update_kernel(mlf<N> *A, int lda, int n, int k0, int kb,
+                                                                     int kc) {
     using B = BfpShape<N>;
     constexpr int D = B::D, NC = B::NC;
+    constexpr int MW = NB / kUpdWarps;  // row values each warp converts
     extern __shared__ int32_t bfp_sm[];
     int32_t *di = bfp_sm;                // rows:    di[(m * D + p) * 32 + r]
-    int32_t *dt = bfp_sm + 32 * 32 * D;  // columns: dt[(w * 32 + m) * D + p]
-    long long *part = reinterpret_cast<long long *>(bfp_sm + (32 * 32 + 8 * 32) * D);  // [c][t][r]
-    __shared__ int emax[16][32];  // partial row maxima
-    __shared__ int et[8];
+    int32_t *dt = bfp_sm + 32 * 32 * D;  // columns: dt[(c * 32 + m) * D + p]
+    long long *part = reinterpret_cast<long long *>(bfp_sm + (32 + kUpdCols) * 32 * D);  // [col][c][r]
+    __shared__ int emax[kUpdWarps][32];  // partial row maxima
+    __shared__ int et[kUpdCols];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int i0 = k0 + (int)blockIdx.x * 32, t0 = (int)blockIdx.y * 8;
+    const int i0 = k0 + (int)blockIdx.x * 32, t0 = (int)blockIdx.y * kUpdCols;
     constexpr int kNone = kBfpNone;
-    // rows: lane = row, warp w takes m = 2w, 2w + 1
+    // rows: lane = row, warp w takes m = MW w .. MW w + MW - 1
     const int ri = i0 + lane;
-    mlf<N> xv[2];
+    mlf<N> xv[MW];
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const int m = 2 * warp + k;
+    for (int k = 0; k < MW; ++k) {
+        const int m = MW * warp + k;
         xv[k] = ri < n ? A[ri + (long long)(kc + m) * lda] : ml_zero<N>();
     }
     int e = kNone;
 #pragma unroll
-    for (int k = 0; k < 2; ++k) e = xv[k].m[N - 1] ? max(e, xv[k].e) : e;
+    for (int k = 0; k < MW; ++k) e = xv[k].m[N - 1] ? max(e, xv[k].e) : e;
     emax[warp][lane] = e;
-    // columns: warp w < 8 reads column t0 + w, lane = m
-    const int tw = t0 + (warp & 7);
+    // columns: warp w < kUpdCols reads column t0 + w, lane = m
     mlf<N> yv = ml_zero<N>();
-    if (warp < 8) {
+    if (warp < kUpdCols) {
+        const int tw = t0 + warp;
         yv = tw < kb ? A[k0 + tw + (long long)(kc + lane) * lda] : ml_zero<N>();
         int ey = yv.m[N - 1] ? yv.e : kNone;
 #pragma unroll
@@ -445,18 +453,19 @@ __global__ void __launch_bounds__(512) panel_update_kernel(mlf<N> *A, int lda, i
     __syncthreads();
     int Er = emax[0][lane];
 #pragma unroll
-    for (int w = 1; w < 16; ++w) Er = max(Er, emax[w][lane]);
-    const int Ey = et[warp & 7];
+    for (int w = 1; w < kUpdWarps; ++w) Er = max(Er, emax[w][lane]);
+    const int tl = warp % kUpdCols, half = warp / kUpdCols;
+    const int Ey = et[tl];
     {
         int32_t d[D];
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
+        for (int k = 0; k < MW; ++k) {
             bfp_digits<N>(xv[k], Er, d);
-            const int m = 2 * warp + k;
+            const int m = MW * warp + k;
 #pragma unroll
             for (int p = 0; p < D; ++p) di[(m * D + p) * 32 + lane] = d[p];
         }
-        if (warp < 8) {
+        if (warp < kUpdCols) {
             bfp_digits<N>(yv, Ey, d);
 #pragma unroll
             for (int p = 0; p < D; ++p) dt[(warp * 32 + lane) * D + p] = d[p];
@@ -464,7 +473,6 @@ __global__ void __launch_bounds__(512) panel_update_kernel(mlf<N> *A, int lda, i
     }
     __syncthreads();
     // entry (i0 + lane, t0 + tl); this warp's half of the terms
-    const int tl = warp & 7, half = warp >> 3;
     const int i = i0 + lane, t = t0 + tl;
     const bool live = i < n && t < kb && i - k0 >= t;
     long long acc[NC];
@@ -483,13 +491,13 @@ __global__ void __launch_bounds__(512) panel_update_kernel(mlf<N> *A, int lda, i
         }
         if (half) {
 #pragma unroll
-            for (int c = 0; c < NC; ++c) part[(c * 8 + tl) * 32 + lane] = acc[c];
+            for (int c = 0; c < NC; ++c) part[(tl * NC + c) * 32 + lane] = acc[c];
         }
     }
     __syncthreads();
     if (!live || half) return;
 #pragma unroll
-    for (int c = 0; c < NC; ++c) acc[c] += part[(c * 8 + tl) * 32 + lane];  // both halves carried: no overflow
+    for (int c = 0; c < NC; ++c) acc[c] += part[(tl * NC + c) * 32 + lane];  // both halves carried: no overflow
     const mlf<N> dot = bfp_result<N>(acc, Er, Ey);
     mlf<N> *cp = A + i + (long long)(k0 + t) * lda;
     *cp = ml_sub(*cp, dot);
@@ -764,7 +772,8 @@ void potrf_panels(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStrea
         if (k >= 2) SDPG_CUDA(cudaStreamWaitEvent(s, ws.ev[2 + (k & 1)], 0));  // product of panels < k-1
         if (k >= 1) {
             SDPG_KT_BEGIN(s);
-            panel_update_kernel<N><<<dim3(ceil_div(n - k0, 32), ceil_div(kb, 8)), 512, BfpShape<N>::smem, s>>>(
+            panel_update_kernel<N><<<dim3(ceil_div(n - k0, 32), ceil_div(kb, kUpdCols)), 32 * kUpdWarps,
+                                     BfpShape<N>::smem, s>>>(
                 A, lda, n, k0, kb, k0 - NB);
             SDPG_CHECK_LAUNCH_KT("panel_update_kernel", s);
         }
