@@ -10,6 +10,7 @@
 #include <cooperative_groups.h>
 
 #include "kernels.cuh"
+#include "mlfix.cuh"
 #include "mlwarp.cuh"
 #include "tc_gemm.cuh"
 #include "tcgen05.cuh"
@@ -300,113 +301,21 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(PanelShape<C>::threa
 //     A[i][k0 + t] -= sum_{m < 32} L[i][kc + m] L[k0 + t][kc + m],  i in [k0, n), t < kb,
 // lower part of the diagonal block only.
 //
-// Block floating point: each row's 32 values become signed fixed-point fractions
-// x 2^-E_row (E_row the row's largest exponent) held as D digits of 28 bits, so a term is
-// 64 (N = 8) digit products accumulated exactly in 64-bit columns, with no per-term
-// normalisation; the columns below the top D + 1 are dropped and the sum is rounded to
-// N limbs once.  The truncation is relative to 2^(E_i + E_t), about 2^-270 of
-// sqrt(A_ii A_tt) for a Cholesky factor: the form of the factorisation's backward error.
-//
-// CTA: 32 rows i (lane) x 8 columns t (warp).  Its rows' digits go to shared memory as
-// [m][digit][row] (a warp's 32 lanes read 32 consecutive words), the columns' as
-// [t][m][digit] (one address per warp).
+// In block floating point (mlfix.cuh: each row's 32 values as 28-bit digits relative to
+// the row's largest exponent, digit products summed exactly, one rounding per entry): the
+// truncation is relative to 2^(E_i + E_t), about 2^-270 of sqrt(A_ii A_tt) for a Cholesky
+// factor, the form of the factorisation's backward error.  The rows' digits go to shared
+// memory as [m][digit][row] (a warp's 32 lanes read 32 consecutive words), the columns'
+// as [t][m][digit] (one address per warp).
 constexpr int kUpdCols = 4;  // columns t per CTA of the update kernel (two warps each)
 constexpr int kUpdWarps = 2 * kUpdCols;
 
+// dynamic shared memory of the update kernel: digits of 32 rows and kUpdCols columns,
+// then the second warps' half-sums
 template <int N>
-struct BfpShape {
-    using G = MulDigits<N>;
-    static constexpr int D = G::D;              // digits per value
-    static constexpr int CK = G::CK;            // lowest product column kept
-    static constexpr int NC = 2 * D - 1 - CK + 2;  // kept columns plus two for carries
-    static constexpr int LW = (28 * NC + 31) / 32;
-    static constexpr int EVERY = N <= 8 ? 8 : 4;   // terms between carry passes (no int64 overflow)
-    // update kernel: digits of 32 rows and kUpdCols columns, then the second half-sums
-    static constexpr size_t smem =
-        (size_t)(32 + kUpdCols) * 32 * D * sizeof(int32_t) + (size_t)NC * kUpdCols * 32 * sizeof(long long);
-};
-static_assert(8 * 10 * (1ll << 56) / 8 < (1ll << 62) && BfpShape<16>::EVERY * 19 <= 119, "column sums fit int64");
-
-// x 2^-E as D signed digits of 28 bits (x's sign on every digit); E >= x.e
-template <int N>
-MLHD void bfp_digits(const mlf<N> &x, int E, int32_t (&d)[BfpShape<N>::D]) {
-    constexpr int D = BfpShape<N>::D, L = N + 1;
-    constexpr int up = 28 * D - 32 * N;  // the mantissa's place in the 28 D-bit fraction
-    static_assert(up > 0 && up < 32, "digit frame");
-    uint32_t a[L];
-    a[0] = x.m[0] << up;
-#pragma unroll
-    for (int k = 1; k < N; ++k) a[k] = (x.m[k] << up) | (x.m[k - 1] >> (32 - up));
-    a[N] = x.m[N - 1] >> (32 - up);
-    const int delta = E - x.e;
-    const bool zero = x.m[N - 1] == 0u || delta >= 32 * L;
-    ml_limb_shr<L>(a, zero ? 0 : (delta >> 5));
-    ml_bit_shr<L>(a, zero ? 0 : (delta & 31));
-#pragma unroll
-    for (int p = 0; p < D; ++p) {
-        const int bit = 28 * p, w = bit >> 5, r = bit & 31;
-        const uint32_t lo = a[w] >> r;
-        const uint32_t hi = (r > 4 && w + 1 < L) ? (a[w + 1] << (32 - r)) : 0u;
-        const int32_t v = zero ? 0 : (int32_t)((lo | hi) & 0x0FFFFFFFu);
-        d[p] = x.s ? -v : v;
-    }
-}
-
-// signed carry pass: columns 0 .. NC-2 into [0, 2^28), the top one keeps the sign
-template <int NC>
-MLHD void bfp_carry(long long (&acc)[NC]) {
-#pragma unroll
-    for (int c = 0; c + 1 < NC; ++c) {
-        const long long carry = acc[c] >> 28;
-        acc[c] -= carry << 28;
-        acc[c + 1] += carry;
-    }
-}
-
-// acc (columns CK .. of the products) += a b, digits of two fixed-point fractions
-template <int N>
-MLHD void bfp_term(long long (&acc)[BfpShape<N>::NC], const int32_t (&a)[BfpShape<N>::D],
-                   const int32_t (&b)[BfpShape<N>::D]) {
-    constexpr int D = BfpShape<N>::D, CK = BfpShape<N>::CK;
-#ifdef __CUDA_ARCH__
-#pragma unroll
-#endif
-    for (int c = CK; c <= 2 * D - 2; ++c) {
-#ifdef __CUDA_ARCH__
-#pragma unroll
-#endif
-        for (int p = 0; p < D; ++p) {
-            const int q = c - p;
-            if (q >= 0 && q < D) acc[c - CK] += (long long)a[p] * b[q];
-        }
-    }
-}
-
-// the sum held in acc (fractions x 2^-Er and y 2^-Ey) rounded to N limbs; kNone exponents
-// mean an all-zero row
-constexpr int kBfpNone = -(1 << 30);
-template <int N>
-MLHD mlf<N> bfp_result(long long (&acc)[BfpShape<N>::NC], int Er, int Ey) {
-    using B = BfpShape<N>;
-    constexpr int D = B::D, CK = B::CK, NC = B::NC;
-    bfp_carry<NC>(acc);
-    const bool neg = acc[NC - 1] < 0;
-    if (neg) {
-        for (int c = 0; c < NC; ++c) acc[c] = -acc[c];
-        bfp_carry<NC>(acc);
-    }
-    uint32_t W[B::LW];
-    for (int w = 0; w < B::LW; ++w) W[w] = 0;
-    for (int c = 0; c < NC; ++c) {  // every column is below 2^28 here
-        const int bit = 28 * c, w = bit >> 5, r = bit & 31;
-        const unsigned long long v = (unsigned long long)acc[c] << r;
-        W[w] |= (uint32_t)v;
-        if (w + 1 < B::LW) W[w + 1] |= (uint32_t)(v >> 32);
-    }
-    // the sum is W 2^(28 CK - 56 D) 2^(Er + Ey)
-    const long long e_top = (long long)Er + Ey + 28 * CK - 56 * D + 32 * B::LW;
-    if (Er == kBfpNone || Ey == kBfpNone) return ml_zero<N>();
-    return ml_pack<N, B::LW>(W, (int)e_top, neg ? 1u : 0u);
+constexpr size_t panel_update_smem() {
+    return (size_t)(32 + kUpdCols) * 32 * BfpShape<N>::D * sizeof(int32_t) +
+           (size_t)BfpShape<N>::NC * kUpdCols * 32 * sizeof(long long);
 }
 
 // CTA: 32 rows i (lane) x kUpdCols columns t, two warps per column, each summing 16 of
@@ -756,7 +665,7 @@ void potrf_panels(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStrea
     static bool attr_set = false;  // dynamic shared memory of the update kernel (97 KB at N = 16)
     if (!attr_set) {
         SDPG_CUDA(cudaFuncSetAttribute(panel_update_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)BfpShape<N>::smem));
+                                       (int)panel_update_smem<N>()));
         attr_set = true;
     }
     cudaStream_t h = nullptr;  // the side stream, forked from s after the set-up above
@@ -773,7 +682,7 @@ void potrf_panels(int n, mlf<N> *A, int lda, int *info, Workspace &ws, cudaStrea
         if (k >= 1) {
             SDPG_KT_BEGIN(s);
             panel_update_kernel<N><<<dim3(ceil_div(n - k0, 32), ceil_div(kb, kUpdCols)), 32 * kUpdWarps,
-                                     BfpShape<N>::smem, s>>>(
+                                     panel_update_smem<N>(), s>>>(
                 A, lda, n, k0, kb, k0 - NB);
             SDPG_CHECK_LAUNCH_KT("panel_update_kernel", s);
         }

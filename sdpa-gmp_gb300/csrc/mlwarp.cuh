@@ -1,6 +1,7 @@
 // Warp / block level helpers for mlf values (device only).
 #pragma once
 #include "ml.cuh"
+#include "mlfix.cuh"
 
 namespace sdpg {
 
@@ -22,62 +23,6 @@ __device__ __forceinline__ mlf<N> ml_shfl(const mlf<N> &v, int src) {
 #pragma unroll
     for (int k = 0; k < N; ++k) r.m[k] = __shfl_sync(0xffffffffu, v.m[k], src);
     return r;
-}
-
-// ---- exact sums in signed fixed point ----
-// A group of values is summed as two's-complement integers of W = N + 2 words relative to
-// the group's largest exponent E (a value of exponent E has its mantissa in words 1..N,
-// the top word is headroom and sign), so the tree needs only word-wise integer adds and
-// the sum is rounded to N limbs once.  Each value loses the bits below 2^-32 of the
-// frame's last mantissa word, about 2^-(32N+32) of the largest value.
-constexpr int kFixNone = -(1 << 30);  // exponent of a group with no nonzero value
-
-template <int N>
-MLHD void ml_to_fix(const mlf<N> &v, int E, uint32_t (&a)[N + 2]) {
-    constexpr int W = N + 2;
-    a[0] = 0u;
-    ML_UNROLL
-    for (int k = 0; k < N; ++k) a[k + 1] = v.m[k];
-    a[N + 1] = 0u;
-    const int delta = E - v.e;
-    const bool zero = v.m[N - 1] == 0u || delta >= 32 * W || delta < 0;
-    ml_limb_shr<W>(a, zero ? 0 : (delta >> 5));
-    ml_bit_shr<W>(a, zero ? 0 : (delta & 31));
-    uint32_t carry = v.s ? 1u : 0u;  // negative: ~a + 1
-    ML_UNROLL
-    for (int k = 0; k < W; ++k) {
-        const uint32_t x = zero ? 0u : (v.s ? ~a[k] : a[k]);
-        const uint64_t t = (uint64_t)x + (zero ? 0u : carry);
-        a[k] = (uint32_t)t;
-        carry = (uint32_t)(t >> 32);
-    }
-}
-
-template <int W>
-MLHD void ml_fix_add(uint32_t (&a)[W], const uint32_t (&b)[W]) {
-    uint32_t carry = 0u;
-    ML_UNROLL
-    for (int k = 0; k < W; ++k) {
-        const uint64_t t = (uint64_t)a[k] + b[k] + carry;
-        a[k] = (uint32_t)t;
-        carry = (uint32_t)(t >> 32);
-    }
-}
-
-// the fixed-point sum of a group with largest exponent E, rounded to N limbs
-template <int N>
-MLHD mlf<N> ml_from_fix(uint32_t (&a)[N + 2], int E) {
-    constexpr int W = N + 2;
-    if (E == kFixNone) return ml_zero<N>();
-    const bool neg = (a[W - 1] >> 31) != 0u;
-    uint32_t carry = 1u;
-    ML_UNROLL
-    for (int k = 0; k < W; ++k) {  // |a|
-        const uint64_t t = (uint64_t)(neg ? ~a[k] : a[k]) + (neg ? carry : 0u);
-        a[k] = (uint32_t)t;
-        carry = (uint32_t)(t >> 32);
-    }
-    return ml_pack<N, W>(a, E + 32, neg ? 1u : 0u);
 }
 
 __device__ __forceinline__ int warp_max_int(int e) {
