@@ -37,9 +37,9 @@ constexpr int NB = 32;
 // t..NB-1) is spread over a cluster of C CTAs (one per SM), entry q in CTA q mod C.  The
 // entries still active at step j (t > j) are the highest-numbered ones, so in every CTA
 // whole warps drop out as the elimination proceeds while the remaining work stays spread
-// over all C SMs.  Every CTA keeps a copy of the columns of S^(j) (each column j in the
-// pivot's step): an entry that becomes final stores itself into all copies with
-// st.async, and each column's mbarrier tells a CTA when the column has arrived.  A
+// over all C SMs.  Every CTA keeps a copy of the columns (column j as it stands at step
+// j, when it holds the pivot): an entry that becomes final stores itself into all copies
+// with st.async, and each column's mbarrier tells a CTA when the column has arrived.  A
 // thread waits only for the columns it reads, so a step costs one update and one remote
 // store instead of the slowest thread's update plus a cluster barrier.
 //
@@ -60,7 +60,7 @@ constexpr int NB = 32;
 // for the panel with progress base `base` reads base + j + 1 once hist column j is out,
 // base + kPanelFinal once the normalisers are, and base + kPanelAbort after a bad pivot.
 // hist: NB x NB entries (column j at hist[j NB ..]), then the NB normalisers.
-constexpr int kPotf2Threads = ((NB * (NB + 1) / 2 + 31) / 32) * 32;  // one thread per entry of a block
+constexpr int kBlockThreads = ((NB * (NB + 1) / 2 + 31) / 32) * 32;  // one thread per entry of a block
 constexpr int kPanelFinal = 40;
 constexpr int kPanelAbort = 63;
 constexpr int kPanelTimeout = 6;                 // error-word code of a row wait that gave up
@@ -422,7 +422,7 @@ constexpr int kPackedLower = NB * (NB - 1) / 2;
 // X is final; its owners scale it by 1/T[j][j] and publish it, then every entry below
 // subtracts T[i][j] X[j][c] (T from shared memory): one barrier per step.
 template <int N>
-__global__ void __launch_bounds__(kPotf2Threads, 1) trtri_diag_kernel(const mlf<N> *L, int ldl, mlf<N> *Linv, int ldi, int n) {
+__global__ void __launch_bounds__(kBlockThreads, 1) trtri_diag_kernel(const mlf<N> *L, int ldl, mlf<N> *Linv, int ldi, int n) {
     __shared__ mlf<N> ts[kPackedLower];
     __shared__ mlf<N> rv[NB];
     __shared__ mlf<N> xrow[2][NB];
@@ -798,7 +798,7 @@ void ml_trtri_lower(int n, const mlf<N> *L, int ldl, mlf<N> *Linv, Workspace &ws
     SDPG_CHECK_LAUNCH_KT("pad_lower_kernel", s);
     SDPG_CUDA(cudaMemsetAsync(Xp, 0, pp * sizeof(mlf<N>), s));
     SDPG_KT_BEGIN(s);
-    trtri_diag_kernel<N><<<P / NB, kPotf2Threads, 0, s>>>(Lp, P, Xp, P, P);
+    trtri_diag_kernel<N><<<P / NB, kBlockThreads, 0, s>>>(Lp, P, Xp, P, P);
     SDPG_CHECK_LAUNCH_KT("trtri_diag_kernel", s);
     const mlf<N> one = ml_one<N>(), zero = ml_zero<N>(), mone = ml_from_int<N>(-1);
     for (int b = 2 * NB; b <= P; b *= 2) {
