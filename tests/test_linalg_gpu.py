@@ -113,9 +113,11 @@ def test_rpotrf_residual_large(sdpg, n, spread):
 
 
 @gpu
-@pytest.mark.parametrize("n,bad", [(40, 17), (70, 0), (70, 69)])
+@pytest.mark.parametrize("n,bad", [(40, 17), (70, 0), (70, 69), (200, 100)])
 def test_rpotrf_reports_first_bad_pivot(sdpg, exact, n, bad):
-    """A non-positive pivot at column `bad` gives info = bad + 1, like Rpotrf."""
+    """A non-positive pivot at column `bad` gives info = bad + 1, like Rpotrf (n = 200: the
+    look-ahead products and cached residues are in flight when panel 3 fails; the later
+    panels leave at once)."""
     vals = [(0, 0)] * (n * n)
     for i in range(n):
         vals[i + i * n] = (-1, 0) if i == bad else (1, 0)
