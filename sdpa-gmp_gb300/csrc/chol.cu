@@ -60,7 +60,6 @@ constexpr int NB = 32;
 // for the panel with progress base `base` reads base + j + 1 once hist column j is out,
 // base + kPanelFinal once the normalisers are, and base + kPanelAbort after a bad pivot.
 // hist: NB x NB entries (column j at hist[j NB ..]), then the NB normalisers.
-constexpr int kBlockThreads = ((NB * (NB + 1) / 2 + 31) / 32) * 32;  // one thread per entry of a block
 constexpr int kPanelFinal = 40;
 constexpr int kPanelAbort = 63;
 constexpr int kPanelTimeout = 6;                 // error-word code of a row wait that gave up
@@ -412,56 +411,82 @@ __global__ void __launch_bounds__(32 * kUpdWarps) panel_update_kernel(mlf<N> *A,
     *cp = ml_sub(*cp, dot);
 }
 
-// strict lower triangle of an NB x NB block, packed column by column
-__host__ __device__ constexpr int packed_lower(int i, int j) { return j * NB - j * (j + 1) / 2 + (i - j - 1); }
-constexpr int kPackedLower = NB * (NB - 1) / 2;
 
 // Invert every NB x NB diagonal block of the lower-triangular L (n a multiple of NB)
-// into Linv, one block per CTA and one thread per lower-triangle entry of the inverse,
-// held in registers.  Column-oriented substitution X = T^-1: after step j - 1 row j of
-// X is final; its owners scale it by 1/T[j][j] and publish it, then every entry below
-// subtracts T[i][j] X[j][c] (T from shared memory): one barrier per step.
+// into Linv, one cluster of kPanelCluster CTAs per block and one thread per
+// lower-triangle entry of the inverse, dealt cyclically over the cluster as in
+// panel_factor_kernel.  Row-oriented substitution X = T^-1: entry (i, c) subtracts
+// T[i][j] X[j][c] for j = c .. i-1 as each row j of X arrives, scales by 1/T[i][i], and
+// stores X[i][c] into every CTA of the cluster with st.async, completing row i's
+// mbarrier there: a thread waits only for the rows it reads, no barrier per step.
+// T is read through the cache, each next value loaded before the wait for its row.
+// A wait that gives up (about a second) sets *err to kTrtriTimeout; the rows it should
+// have produced are then not written.
+constexpr int kTrtriTimeout = 7;
+
+// packed row-major lower triangle with the diagonal: row i holds columns 0..i
+__host__ __device__ constexpr int packed_row(int i, int c) { return i * (i + 1) / 2 + c; }
+
 template <int N>
-__global__ void __launch_bounds__(kBlockThreads, 1) trtri_diag_kernel(const mlf<N> *L, int ldl, mlf<N> *Linv, int ldi, int n) {
-    __shared__ mlf<N> ts[kPackedLower];
-    __shared__ mlf<N> rv[NB];
-    __shared__ mlf<N> xrow[2][NB];
-    const int o = blockIdx.x * NB;
+__global__ void __cluster_dims__(kPanelCluster, 1, 1) __launch_bounds__(PanelShape<kPanelCluster>::threads)
+    trtri_diag_kernel(const mlf<N> *L, int ldl, mlf<N> *Linv, int ldi, int *err) {
+    constexpr int C = kPanelCluster;
+    __shared__ mlf<N> rv[NB];                             // 1 / T[i][i]
+    __shared__ PanelSlot<N> xr[NB * (NB + 1) / 2];        // X[i][c] at packed_row(i, c)
+    __shared__ __align__(8) unsigned long long bars[NB];  // bars[i]: row i of X has arrived
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int o = (int)(blockIdx.x / C) * NB;
     const mlf<N> *T = L + o + (long long)o * ldl;
     mlf<N> *X = Linv + o + (long long)o * ldi;
-    const int q = threadIdx.x;
-    for (int p = q; p < NB * NB; p += blockDim.x) {
-        const int i = p % NB, j = p / NB;
-        if (i > j) ts[packed_lower(i, j)] = T[i + (long long)j * ldl];
+    const uint32_t xr0 = tc::smem_u32(xr), bars0 = tc::smem_u32(bars);
+    if (threadIdx.x == 0) {  // row i brings i + 1 entries into every CTA
+        for (int r = 0; r < NB; ++r) tc::mbar_init(bars0 + 8u * r, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int r = 0; r < NB; ++r) tc::mbar_expect_tx(bars0 + 8u * r, (r + 1) * (uint32_t)sizeof(mlf<N>));
     }
-    if (q < NB) rv[q] = ml_recip(T[q + (long long)q * ldl]);
-    // entry (i, c), c <= i, numbered column by column as in the diagonal block of panel_factor_kernel
-    int c = 0;
-    while (c + 1 < NB && NB * (c + 1) - (c + 1) * c / 2 <= q) ++c;
-    const int i = c + (q - (NB * c - c * (c - 1) / 2));
-    const bool mine = q < NB * (NB + 1) / 2;
-    mlf<N> x = (mine && i == c) ? ml_one<N>() : ml_zero<N>();
+    if (threadIdx.x < NB) rv[threadIdx.x] = ml_recip(T[threadIdx.x + (long long)threadIdx.x * ldl]);
     __syncthreads();
-    // row 0 is final at the start: X[0][0] = 1 / T[0][0]
-    if (mine && i == 0) {
-        x = ml_mul(x, rv[0]);
-        xrow[0][c] = x;
-    }
-    __syncthreads();
-    for (int j = 0; j + 1 < NB; ++j) {
-        if (mine && i > j && c <= j) {
-            x = ml_sub(x, ml_mul(ts[packed_lower(i, j)], xrow[j & 1][c]));
-            if (i == j + 1) {  // row j + 1 is now final
-                x = ml_mul(x, rv[j + 1]);
-                xrow[(j + 1) & 1][c] = x;
+    cluster.sync();  // every CTA's barriers are initialised before any remote store
+    const int q = (int)threadIdx.x * C + rank;  // packed_row(i, c) of this thread's entry
+    int i = 0;
+    while (i + 1 < NB && packed_row(i + 1, 0) <= q) ++i;
+    const int c = q - packed_row(i, 0);
+    const bool mine = (int)threadIdx.x < PanelShape<C>::per_cta && q < NB * (NB + 1) / 2;
+    mlf<N> x = ml_zero<N>();
+    bool ok = true;
+    if (mine) {
+        x = i == c ? ml_one<N>() : ml_zero<N>();
+        mlf<N> tn = c < i ? T[i + (long long)c * ldl] : ml_zero<N>();
+        for (int j = c; j < i; ++j) {
+            const mlf<N> tj = tn;
+            if (j + 1 < i) tn = T[i + (long long)(j + 1) * ldl];
+            if (!tc::mbar_wait_acq_cluster(bars0 + 8u * j, 0, kPanelWaitCycles)) {
+                ok = false;
+                break;
             }
-        } else if (mine && i == j + 1 && c == j + 1) {  // the diagonal entry of row j + 1
-            x = ml_mul(x, rv[j + 1]);
-            xrow[(j + 1) & 1][c] = x;
+            x = ml_sub(x, ml_mul(tj, xr[packed_row(j, c)].v));
         }
-        __syncthreads();
+        if (ok) {
+            x = ml_mul(x, rv[i]);
+#pragma unroll
+            for (int r = 0; r < C; ++r)
+                st_async_ml<N>(cluster_addr(xr0 + q * (uint32_t)sizeof(PanelSlot<N>), r), x,
+                               cluster_addr(bars0 + 8u * i, r));
+        } else {
+            atomicExch(err, kTrtriTimeout);
+        }
     }
-    if (mine) X[i + (long long)c * ldi] = x;
+    // every row stored into this CTA has arrived before it leaves (bounded)
+    if (threadIdx.x == 0)
+        for (int r = 0; r < NB; ++r)
+            if (!tc::mbar_wait_acq_cluster(bars0 + 8u * r, 0, kPanelWaitCycles)) {
+                atomicExch(err, kTrtriTimeout);
+                break;
+            }
+    __syncthreads();
+    cluster.sync();
+    if (mine && ok) X[i + (long long)c * ldi] = x;
 }
 
 // Inverses of the NB x NB diagonal blocks of the lower-triangular L, packed:
@@ -798,7 +823,8 @@ void ml_trtri_lower(int n, const mlf<N> *L, int ldl, mlf<N> *Linv, Workspace &ws
     SDPG_CHECK_LAUNCH_KT("pad_lower_kernel", s);
     SDPG_CUDA(cudaMemsetAsync(Xp, 0, pp * sizeof(mlf<N>), s));
     SDPG_KT_BEGIN(s);
-    trtri_diag_kernel<N><<<P / NB, kBlockThreads, 0, s>>>(Lp, P, Xp, P, P);
+    trtri_diag_kernel<N><<<(P / NB) * kPanelCluster, PanelShape<kPanelCluster>::threads, 0, s>>>(
+        Lp, P, Xp, P, ws.error ? ws.error : crt_error_word());
     SDPG_CHECK_LAUNCH_KT("trtri_diag_kernel", s);
     const mlf<N> one = ml_one<N>(), zero = ml_zero<N>(), mone = ml_from_int<N>(-1);
     for (int b = 2 * NB; b <= P; b *= 2) {
