@@ -462,16 +462,13 @@ __global__ void lz_next_kernel(int n, const mlf<N> *r, const mlf<N> *sl, mlf<N> 
 }
 
 // The loop control after step k: the new beta from r.r, the Ritz value of an eigenvalue
-// step, and the loop condition for step k + 1 (Lal::getMinEigen's while test).
+// step, and the loop condition for step k + 1 (Lal::getMinEigen's while test), in three
+// parts so that an eigenvalue step can form beta beside the tridiagonal solve.
+
+// beta = sqrt(r.r) and 1/beta from one inverse square root: y = (r.r)^(-1/2) is 1/beta,
+// beta = (r.r) y refined by half a Newton step; into te[k], sl[1], sl[0]
 template <int N>
-__device__ void lz_control(mlf<N> *sl, mlf<N> *te, int *ctl, int k, int eig, int n, int kgo, int kmax) {
-    if (eig) {
-        sl[9] = sl[8];
-        sl[8] = sl[4];
-        sl[10] = sl[5];
-    }
-    // beta = sqrt(r.r) and 1/beta from one inverse square root: y = (r.r)^(-1/2) is 1/beta,
-    // beta = (r.r) y refined by half a Newton step
+__device__ mlf<N> lz_beta(mlf<N> *sl, mlf<N> *te, int *ctl, int k) {
     const mlf<N> rr = sl[6];
     const mlf<N> y = mlc_rsqrt(rr);
     mlf<N> beta = mlc_mul(rr, y);
@@ -481,6 +478,21 @@ __device__ void lz_control(mlf<N> *sl, mlf<N> *te, int *ctl, int k, int eig, int
     sl[1] = beta;
     sl[0] = ml_is_zero(beta) ? ml_zero<N>() : y;
     ctl[1] = k + 1;
+    return beta;
+}
+
+// the Ritz value of an eigenvalue step becomes the current minimum, its error term the
+// current error
+template <int N>
+__device__ void lz_ritz(mlf<N> *sl) {
+    sl[9] = sl[8];
+    sl[8] = sl[4];
+    sl[10] = sl[5];
+}
+
+// the loop condition for step k + 1
+template <int N>
+__device__ void lz_go(const mlf<N> *sl, int *ctl, int k, int n, int kgo, int kmax, const mlf<N> &beta) {
     const int kn = k + 1;
     const mlf<N> mn = sl[8], mo = sl[9], er = sl[10];
     bool go = kn < n && kn < kgo && ml_cmp(beta, ml_from_double<N>(1.0e-16)) > 0;
@@ -494,6 +506,71 @@ __device__ void lz_control(mlf<N> *sl, mlf<N> *te, int *ctl, int k, int eig, int
     }
     if (kn + 1 >= kmax) go = false;
     ctl[0] = go ? 1 : 0;
+}
+
+template <int N>
+__device__ void lz_control(mlf<N> *sl, mlf<N> *te, int *ctl, int k, int eig, int n, int kgo, int kmax) {
+    if (eig) lz_ritz(sl);
+    const mlf<N> beta = lz_beta(sl, te, ctl, k);
+    lz_go(sl, ctl, k, n, kgo, kmax, beta);
+}
+
+// alpha = q.w into td[k] (the first part of an eigenvalue step's update)
+template <int N>
+__global__ void __launch_bounds__(256) lz_alpha_kernel(int n, const mlf<N> *w, const mlf<N> *q, mlf<N> *td,
+                                                       const int *ctl, int k) {
+    if (!ctl[0]) return;
+    const int stride = blockDim.x;
+    mlf<N> a0 = ml_zero<N>(), a1 = ml_zero<N>();
+    int i = threadIdx.x;
+    for (; i + stride < n; i += 2 * stride) {
+        a0 = mlc_add(a0, mlc_mul(q[i], w[i]));
+        a1 = mlc_add(a1, mlc_mul(q[i + stride], w[i + stride]));
+    }
+    if (i < n) a0 = mlc_add(a0, mlc_mul(q[i], w[i]));
+    const mlf<N> alpha = mlc_block_sum(mlc_add(a0, a1));
+    if (threadIdx.x == 0) td[k] = alpha;
+}
+
+// r = (w - alpha q) - beta qold, r.r and the new beta (the second part, beside the
+// tridiagonal solve, which reads td[0..k] and te[0..k-1] only)
+template <int N>
+__global__ void __launch_bounds__(256) lz_rest_kernel(int n, const mlf<N> *w, const mlf<N> *q, const mlf<N> *qold,
+                                                      const mlf<N> *td, mlf<N> *te, mlf<N> *sl, mlf<N> *r, int *ctl,
+                                                      int k) {
+    if (!ctl[0]) return;
+    const int stride = blockDim.x;
+    const mlf<N> al = td[k], be = sl[1];
+    for (int j = threadIdx.x; j < n; j += stride) r[j] = mlc_sub(mlc_sub(w[j], mlc_mul(q[j], al)), mlc_mul(qold[j], be));
+    __syncthreads();
+    mlf<N> a0 = ml_zero<N>(), a1 = ml_zero<N>();
+    int i = threadIdx.x;
+    for (; i + stride < n; i += 2 * stride) {
+        a0 = mlc_add(a0, mlc_mul(r[i], r[i]));
+        a1 = mlc_add(a1, mlc_mul(r[i + stride], r[i + stride]));
+    }
+    if (i < n) a0 = mlc_add(a0, mlc_mul(r[i], r[i]));
+    const mlf<N> rr = mlc_block_sum(mlc_add(a0, a1));
+    if (threadIdx.x == 0) {
+        sl[6] = rr;
+        lz_beta(sl, te, ctl, k);
+    }
+}
+
+// after the tridiagonal solve: the Ritz value, the loop test and the next step's vectors
+template <int N>
+__global__ void __launch_bounds__(256) lz_decide_kernel(int n, const mlf<N> *r, mlf<N> *q, mlf<N> *qold, mlf<N> *sl,
+                                                        int *ctl, int k, int kgo, int kmax) {
+    // every thread reads the flag before thread 0 may rewrite it
+    const int go = ctl[0];
+    __syncthreads();
+    if (!go) return;
+    if (threadIdx.x == 0) {
+        lz_ritz(sl);
+        lz_go(sl, ctl, k, n, kgo, kmax, sl[1]);
+    }
+    __syncthreads();
+    lz_advance(n, r, sl, q, qold, ctl);
 }
 
 // alpha = q.w (into the tridiagonal's diagonal td[k]), r = (w - alpha q) - beta qold, and
@@ -555,7 +632,8 @@ __global__ void __launch_bounds__(256) lz_control_kernel(int n, const mlf<N> *r,
 
 template <int N>
 void k_lanczos_step(int n, const mlf<N> *M, mlf<N> *r, mlf<N> *q, mlf<N> *qold, mlf<N> *w, mlf<N> *td, mlf<N> *te,
-                    mlf<N> *sl, int *ctl, int *status, int k, int eig, int kgo, int kmax, cudaStream_t s) {
+                    mlf<N> *sl, int *ctl, int *status, int k, int eig, int kgo, int kmax, cudaStream_t s,
+                    cudaStream_t side, cudaEvent_t ev_fork, cudaEvent_t ev_join) {
     if (k == 0) {  // later steps get q from the previous step's update or control kernel
         SDPG_KT_BEGIN(s);
         lz_next_kernel<N><<<ceil_div(n, 128), 128, 0, s>>>(n, r, sl, q, qold, ctl);
@@ -570,6 +648,24 @@ void k_lanczos_step(int n, const mlf<N> *M, mlf<N> *r, mlf<N> *q, mlf<N> *qold, 
         matvec_t_kernel<N><<<ceil_div(n, kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(n, M, 0, q, w, ctl);
     }
     SDPG_CHECK_LAUNCH_KTW("lz_matvec_kernel", s, ((double)n * n + 2.0 * n) * sizeof(mlf<N>));
+    if (eig && side) {
+        // alpha, then the tridiagonal solve on the side stream beside r, r.r and beta
+        SDPG_KT_BEGIN(s);
+        lz_alpha_kernel<N><<<1, 256, 0, s>>>(n, w, q, td, ctl, k);
+        SDPG_CHECK_LAUNCH_KT("lz_update_kernel", s);
+        SDPG_CUDA(cudaEventRecord(ev_fork, s));
+        SDPG_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+        k_tridiag_min<N>(k + 1, td, te, sl + 4, status, side, ctl);
+        SDPG_KT_BEGIN(s);
+        lz_rest_kernel<N><<<1, 256, 0, s>>>(n, w, q, qold, td, te, sl, r, ctl, k);
+        SDPG_CHECK_LAUNCH_KT("lz_update_kernel", s);
+        SDPG_CUDA(cudaEventRecord(ev_join, side));
+        SDPG_CUDA(cudaStreamWaitEvent(s, ev_join, 0));
+        SDPG_KT_BEGIN(s);
+        lz_decide_kernel<N><<<1, 256, 0, s>>>(n, r, q, qold, sl, ctl, k, kgo, kmax);
+        SDPG_CHECK_LAUNCH_KT("lz_control_kernel", s);
+        return;
+    }
     SDPG_KT_BEGIN(s);
     lz_update_kernel<N><<<1, 256, 0, s>>>(n, w, q, qold, td, te, sl, r, ctl, k, eig, kgo, kmax);
     SDPG_CHECK_LAUNCH_KT("lz_update_kernel", s);
@@ -639,7 +735,8 @@ void k_tridiagonalize_small(int n, mlf<N> *A, mlf<N> *d, mlf<N> *e, cudaStream_t
     template void k_tridiag_min<N>(int, const mlf<N> *, const mlf<N> *, mlf<N> *, int *, cudaStream_t,     \
                                    const int *);                                                          \
     template void k_lanczos_step<N>(int, const mlf<N> *, mlf<N> *, mlf<N> *, mlf<N> *, mlf<N> *, mlf<N> *, \
-                                    mlf<N> *, mlf<N> *, int *, int *, int, int, int, int, cudaStream_t);   \
+                                    mlf<N> *, mlf<N> *, int *, int *, int, int, int, int, cudaStream_t,    \
+                                    cudaStream_t, cudaEvent_t, cudaEvent_t);                               \
     template void k_tridiagonalize_small<N>(int, mlf<N> *, mlf<N> *, mlf<N> *, cudaStream_t);              \
     template void k_lp_ratio_min<N>(int, const mlf<N> *, const mlf<N> *, mlf<N> *, cudaStream_t);
 SDPG_INST_EIG(8)

@@ -137,10 +137,13 @@ void k_tridiag_min(int k, const mlf<N> *d, const mlf<N> *e, mlf<N> *out, int *st
 // sqrt(r.r) -> te[k], with the tridiagonal eigenvalue solve when `eig`, then the loop
 // test for step k + 1 (k + 1 < n, k + 1 < kgo, beta' > 1e-16, the Ritz value or its
 // error bound still moving, k + 2 < kmax).  Slots and flags in sl / ctl as described in
-// eig.cu; every kernel of the step does nothing once ctl[0] is 0.
+// eig.cu; every kernel of the step does nothing once ctl[0] is 0.  With a side stream,
+// an eigenvalue step runs the tridiagonal solve there (forked after alpha, joined before
+// the loop test) beside r, r.r and beta on s.
 template <int N>
 void k_lanczos_step(int n, const mlf<N> *M, mlf<N> *r, mlf<N> *q, mlf<N> *qold, mlf<N> *w, mlf<N> *td, mlf<N> *te,
-                    mlf<N> *sl, int *ctl, int *status, int k, int eig, int kgo, int kmax, cudaStream_t s);
+                    mlf<N> *sl, int *ctl, int *status, int k, int eig, int kgo, int kmax, cudaStream_t s,
+                    cudaStream_t side = nullptr, cudaEvent_t ev_fork = nullptr, cudaEvent_t ev_join = nullptr);
 // Householder tridiagonalisation of a dense symmetric n x n (n <= 64) in place; writes
 // d[0..n-1], e[0..n-2].  (Rsytrd 'L', the first stage of Rsyev.)
 template <int N>

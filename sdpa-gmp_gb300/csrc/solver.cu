@@ -856,6 +856,7 @@ class Solver final : public SolverBase {
                 if (t.eig[k]) kk = 0;
             }
             t.active = t.n > 0 && kmax > 1;
+            t.ws->ensure_side();  // the eigenvalue steps' tridiagonal solves run there
         }
         // (the pinned slots are next written by stream-ordered copies, after the uploads)
         lanczos_graphed(T);
@@ -885,7 +886,8 @@ class Solver final : public SolverBase {
             graphed(g_lanczos_[slot], t.st, [&] {
                 for (int k = 0; k < t.n && k + 1 < B.lanczos_kmax; ++k)
                     k_lanczos_step<N>(t.n, B.Mop[s], B.r[s], B.q[s], B.qold[s], B.w[s], B.td[s], B.te[s], B.sl[s],
-                                      B.lzctl[s], status_, k, t.eig[k], t.kgo, B.lanczos_kmax, t.st);
+                                      B.lzctl[s], status_, k, t.eig[k], t.kgo, B.lanczos_kmax, t.st, t.ws->side,
+                                      t.ws->ev[0], t.ws->ev[1]);
             });
         }
     }
