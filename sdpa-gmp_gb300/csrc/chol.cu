@@ -62,7 +62,7 @@ constexpr int NB = 32;
 // hist: NB x NB entries (column j at hist[j NB ..]), then the NB normalisers.
 constexpr int kPanelFinal = 40;
 constexpr int kPanelAbort = 63;
-constexpr int kPanelTimeout = 6;                 // error-word code of a row wait that gave up
+constexpr int kPanelTimeout = 6;                 // error-word code of a panel wait that gave up
 constexpr long long kPanelWaitCycles = 1ll << 31;  // about one second at 2 GHz
 static_assert(kPanelAbort < 64 && kPanelFinal > NB, "progress values of one panel stay below the next base");
 
